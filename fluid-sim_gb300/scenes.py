@@ -1,0 +1,66 @@
+"""Synthetic scene generator for the FluidSim2D step.
+
+The reference ships a single hard-coded demo scene (demo/App.cpp:133-160);
+the workloads used here are seeded synthetic scenes in the same unit-domain
+form: dx = 1/sizeX, a one-cell SOLID border, and cell (i, j) FLUID when its
+centre ((i+0.5)dx, (j+0.5)dx) lies inside the fluid region.  Labels are
+written row-major, index j*sizeX + i, which is the layout
+FluidSim2D::create copies (src/FluidSim2D.cpp:47).  (The demo writes its
+array transposed, i*sizeY + j; that only matters for asymmetric scenes.)
+"""
+from __future__ import annotations
+
+import numpy as np
+
+EMPTY, FLUID, SOLID = 0, 1, 2
+SEMILAGRANGIAN, PICFLIP = 0, 1
+
+
+def labels(nx, ny, fluid_fn):
+    """Cell labels for a unit-width domain with a one-cell solid border."""
+    dx = 1.0 / nx
+    i = np.arange(nx)
+    j = np.arange(ny)
+    cx = (i[None, :] + 0.5) * dx
+    cy = (j[:, None] + 0.5) * dx
+    cells = np.where(fluid_fn(cx, cy), FLUID, EMPTY).astype(np.uint8)
+    cells[0, :] = SOLID
+    cells[-1, :] = SOLID
+    cells[:, 0] = SOLID
+    cells[:, -1] = SOLID
+    return cells.reshape(-1)
+
+
+def dam_break(nx, ny=None, *, mode=SEMILAGRANGIAN, dt=1.0 / 120, extent=(0.4, 0.6), disk=None,
+              ppc_sqrt=2, pic_flip_alpha=0.05, rho=997.0, gravity=(0.0, -9.8)):
+    """Dam break: fluid where x < extent[0] and y < extent[1], optionally
+    united with a disk (cx, cy, r)."""
+    ny = nx if ny is None else ny
+
+    def fluid(cx, cy):
+        m = (cx < extent[0]) & (cy < extent[1])
+        if disk is not None:
+            dcx, dcy, r = disk
+            m = m | ((cx - dcx) ** 2 + (cy - dcy) ** 2 < r * r)
+        return m
+
+    return {
+        "sizeX": nx, "sizeY": ny, "ppcSqrt": ppc_sqrt, "dt": dt, "dx": 1.0 / nx, "rho": rho,
+        "gravityX": gravity[0], "gravityY": gravity[1], "mode": mode,
+        "picFlipAlpha": pic_flip_alpha, "cells": labels(nx, ny, fluid),
+    }
+
+
+def sl_dam_break(nx=64, dt=1.0 / 120):
+    """Plain semi-Lagrangian dam break (x < 0.4, y < 0.6), 64x64, dt 1/120."""
+    return dam_break(nx, mode=SEMILAGRANGIAN, dt=dt)
+
+
+def pic_dam_break_disk(nx=256, dt=None):
+    """PIC/FLIP dam break united with a disk of radius 0.1 at (0.7, 0.7);
+    FLIP ratio 0.95 (the reference's picFlipAlpha is the PIC weight, so
+    0.05), 4 particles per cell.  dt = 1/240 at 256^2 and scales with dx
+    (1/960 at 1024^2) so the CFL number stays the same."""
+    if dt is None:
+        dt = (1.0 / 240) * (256.0 / nx)
+    return dam_break(nx, mode=PICFLIP, dt=dt, disk=(0.7, 0.7, 0.1), pic_flip_alpha=0.05)

@@ -1,0 +1,222 @@
+/*
+ * fs2d.h — C ABI of the GB300 FluidSim2D time step.
+ *
+ * This is the drop-in boundary for the reference simulator's per-frame step
+ * (lasagnaphil/fluid-sim, `FluidSim2D` in include/FluidSim2D.h and
+ * src/FluidSim2D.cpp).  Every entry point is `extern "C"`, takes plain
+ * pointers and sizes, never throws, and returns an `int` status (FS2D_OK = 0).
+ * All simulation work runs as CUDA kernels on one GPU, on the stream the
+ * handle owns (or the one given to fs2d_set_stream).  There is no CPU
+ * fallback: if no CUDA device is usable, fs2d_create fails with
+ * FS2D_ERR_CUDA.
+ *
+ * Threading: a handle is used by one host thread at a time; the library
+ * starts no host threads.
+ *
+ * Layout conventions follow the reference exactly:
+ *   - grids are row-major, element (i, j) at index j*NX + i
+ *     (Array2D::operator(), include/Array2D.h:41-49);
+ *   - the MAC grid stores u with (sizeX+1) x sizeY faces and v with
+ *     sizeX x (sizeY+1) faces (MACGrid2D::create, include/MACGrid2D.h:19-25);
+ *   - particles are interleaved (x, y) doubles, one vec2d per particle
+ *     (FluidSim2D::particles, include/FluidSim2D.h:75-76);
+ *   - cell labels are one byte: 0 EMPTY, 1 FLUID, 2 SOLID
+ *     (FluidCellType, include/FluidSim2D.h:44-46).
+ */
+#ifndef FS2D_H
+#define FS2D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference exits or logs instead, src/FluidSim2D.cpp:464-466,598-601) ---- */
+#define FS2D_OK                 0
+#define FS2D_ERR_INVALID        1  /* bad argument or configuration */
+#define FS2D_ERR_ALLOC          2  /* device or pinned-host allocation failed */
+#define FS2D_ERR_CUDA           3  /* a CUDA runtime call or kernel launch failed */
+#define FS2D_ERR_NOT_CONVERGED  4  /* PCG hit its iteration cap (the frame still completes) */
+#define FS2D_ERR_NONFINITE      5  /* a NaN/Inf particle position was produced */
+#define FS2D_ERR_TIMEOUT        6  /* a wavefront kernel gave up waiting on a neighbour tile */
+
+/* ---- cell labels: FluidCellType, include/FluidSim2D.h:44-46 ---- */
+#define FS2D_EMPTY 0
+#define FS2D_FLUID 1
+#define FS2D_SOLID 2
+
+/* ---- modes: FluidSimMode, include/FluidSim2D.h:40-42 ---- */
+#define FS2D_SEMILAGRANGIAN 0
+#define FS2D_PICFLIP        1
+
+/* ---- stage ids: FluidSim2D::StageType, include/FluidSim2D.h:93-97 ---- */
+#define FS2D_STAGE_INIT                            0
+#define FS2D_STAGE_CREATE_WATER_LEVEL_SET          1
+#define FS2D_STAGE_TRANSFER_VELOCITY_TO_GRID       2
+#define FS2D_STAGE_APPLY_SEMI_LAGRANGIAN_ADVECTION 3
+#define FS2D_STAGE_APPLY_GRAVITY                   4
+#define FS2D_STAGE_CREATE_SOLID_LEVEL_SET          5
+#define FS2D_STAGE_APPLY_PROJECTION                6
+#define FS2D_STAGE_UPDATE_VELOCITY                 7
+#define FS2D_STAGE_UPDATE_PARTICLE_VELOCITIES      8
+#define FS2D_STAGE_APPLY_ADVECTION                 9
+
+/* ---- precision of the device path ---- */
+#define FS2D_PRECISION_FP64  0  /* every stage in FP64 with the reference's operation order */
+#define FS2D_PRECISION_MIXED 1  /* FP32 fields/transfers/SpMV/preconditioner, FP64 dots, norms
+                                   and outer iterative-refinement residual */
+
+/* ---- P2G accumulation ---- */
+#define FS2D_P2G_ORDERED 0  /* per-face sums in particle-index order: reproducible, matches the reference */
+#define FS2D_P2G_ATOMIC  1  /* warp-aggregated atomics: fastest, order not reproducible */
+
+/*
+ * Scene configuration.  Byte-compatible with FluidSim2DConfig
+ * (include/FluidSim2D.h:48-63): same fields, same order, same types
+ * (`mode` is the FluidSimMode enum, an int; `initialValues` is the
+ * caller-owned FluidCellType array, copied at create time as the reference
+ * does at src/FluidSim2D.cpp:47).
+ */
+typedef struct fs2d_config {
+    int sizeX;
+    int sizeY;
+    int particlesPerCellSqrt;
+    double dt;
+    double dx;
+    double rho;
+    double gravityX;
+    double gravityY;
+    int mode;
+    double picFlipAlpha;   /* weight of the PIC velocity: v = a*pic + (1-a)*flip (src/FluidSim2D.cpp:564) */
+    const uint8_t* initialValues;
+} fs2d_config;
+
+/*
+ * Options the reference hard-codes (src/FluidSim2D.cpp:369-370,429,447-453).
+ * fs2d_default_options fills in the reference's values.
+ */
+typedef struct fs2d_options {
+    int precision;          /* FS2D_PRECISION_*; default FP64 */
+    double mic_tau;         /* MIC(0) modification parameter; reference 0.999 */
+    double mic_sigma;       /* MIC(0) safety parameter; reference 0.25 */
+    double pcg_tol;         /* stop when ||r||inf <= tol * ||b||inf; reference 1e-12 */
+    int pcg_max_iters;      /* reference 200 */
+    double ir_inner_tol;    /* MIXED only: relative tolerance of each FP32 inner solve; default 1e-4 */
+    int ir_max_outer;       /* MIXED only: cap on refinement sweeps; default 30 */
+    int p2g_mode;           /* FS2D_P2G_*; default ORDERED */
+    int extrapolate_band;   /* 0 = every BFS layer (the reference); k > 0 = layers <= k only */
+    int use_seed;           /* 1: srand(seed) before seeding particles; 0: use libc rand() as it stands,
+                               exactly like the reference's create (src/FluidSim2D.cpp:19-21,52-64) */
+    unsigned int seed;
+    int device;             /* CUDA device ordinal; default 0 */
+} fs2d_options;
+
+/*
+ * A view of caller-owned host buffers holding the full simulation state.
+ * Any pointer may be NULL, in which case that field is skipped.
+ */
+typedef struct fs2d_state {
+    uint8_t* cell;          /* sizeX*sizeY labels */
+    double* phi;            /* sizeX*sizeY water level set (negative inside) */
+    double* p;              /* sizeX*sizeY pressure */
+    double* u;              /* (sizeX+1)*sizeY  mac.u */
+    double* v;              /* sizeX*(sizeY+1)  mac.v */
+    double* newU;           /* (sizeX+1)*sizeY  newMac.u */
+    double* newV;           /* sizeX*(sizeY+1)  newMac.v */
+    double* particles;      /* 2*numParticles interleaved (x, y) */
+    double* particleVels;   /* 2*numParticles interleaved (vx, vy) */
+    size_t numParticles;    /* on upload: particle count to install; on download: capacity check */
+} fs2d_state;
+
+/* Per-frame conservation statistics and solver diagnostics. */
+typedef struct fs2d_stats {
+    double waterVolume;          /* src/FluidSim2D.cpp:709-716 */
+    double totalEnergy;          /* src/FluidSim2D.cpp:717-719 */
+    double particleTotalEnergy;  /* src/FluidSim2D.cpp:723-728 */
+    double origWaterVolume;      /* src/FluidSim2D.cpp:71-72 */
+    double currentTime;          /* src/FluidSim2D.cpp:135 */
+    long long frames;            /* frames run so far */
+    int pcgIterations;           /* iterations of the last pressure solve (sum over refinement sweeps) */
+    int irOuterIterations;       /* MIXED: refinement sweeps of the last solve; FP64: 0 */
+    double pcgRelResidual;       /* ||r||inf / ||b||inf at exit of the last solve (FP64 residual) */
+    int lastStatus;              /* status of the last frame */
+} fs2d_stats;
+
+typedef struct fs2d_sim fs2d_sim;
+
+/* Fills `opt` with the reference's hard-coded values (FP64, tau 0.999, sigma 0.25,
+ * tol 1e-12, 200 iterations, ordered P2G, exact extrapolation). */
+void fs2d_default_options(fs2d_options* opt);
+
+/* FluidSim2D::create (include/FluidSim2D.h:116, src/FluidSim2D.cpp:23-76).
+ * Seeds particles on the host with libc rand() exactly as the reference does,
+ * then uploads the state.  The border cells of initialValues must be SOLID
+ * (the reference reads outside its arrays otherwise).  `opt` may be NULL. */
+int fs2d_create(const fs2d_config* cfg, const fs2d_options* opt, fs2d_sim** out);
+
+/* FluidSim2D::free (include/FluidSim2D.h:118, src/FluidSim2D.cpp:78-92). */
+int fs2d_destroy(fs2d_sim* sim);
+
+/* FluidSim2D::runFrame / update (include/FluidSim2D.h:120-122, src/FluidSim2D.cpp:94-142).
+ * Enqueues the frame's kernels; returns after the frame's device work
+ * completed.  Returns FS2D_ERR_NOT_CONVERGED if the pressure solve hit its
+ * cap (the reference logs and continues; so does this call). */
+int fs2d_run_frame(fs2d_sim* sim);
+
+/* Runs `nframes` frames back to back without host synchronisation between them
+ * (except the pressure solver's convergence polls). */
+int fs2d_step(fs2d_sim* sim, int nframes);
+
+/* Runs one stage method (createWaterLevelSet, transferVelocityToGrid, ...;
+ * include/FluidSim2D.h:124-140) on the current device state. */
+int fs2d_run_stage(fs2d_sim* sim, int stage);
+
+/* Host <-> device state transfer (the reference's public fields). */
+int fs2d_upload_state(fs2d_sim* sim, const fs2d_state* st);
+int fs2d_download_state(fs2d_sim* sim, fs2d_state* st);
+int fs2d_num_particles(fs2d_sim* sim, size_t* n);
+
+/* The fields a caller may change between frames (FluidSim2D::gravity,
+ * picFlipAlpha, dt; written by demo/FluidRenderer2D.cpp:322,388). */
+int fs2d_set_params(fs2d_sim* sim, double gravityX, double gravityY, double picFlipAlpha, double dt);
+
+/* Statistics of the last frame, and the per-frame conservation series
+ * (waterVolumeData, totalEnergyData, particleTotalEnergyData;
+ * include/FluidSim2D.h:106-114).  `history` copies up to `cap` frames into
+ * each non-NULL array and stores the frame count in *n. */
+int fs2d_get_stats(fs2d_sim* sim, fs2d_stats* out);
+int fs2d_get_history(fs2d_sim* sim, double* volume, double* energy, double* particleEnergy,
+                     size_t cap, size_t* n);
+
+/* Diagnostics (src/FluidSim2D.cpp:607-638): device reductions. */
+int fs2d_avg_pressure(fs2d_sim* sim, double* out);
+int fs2d_avg_pressure_in_fluid(fs2d_sim* sim, double* out);
+int fs2d_max_velocity(fs2d_sim* sim, double* out);
+
+/* Per-stage device times (ms, CUDA events) of the last frame, in the
+ * reference's stage order (src/FluidSim2D.cpp:100-133); *n = stage count
+ * (7 semi-Lagrangian, 8 PIC/FLIP). */
+int fs2d_get_stage_times(fs2d_sim* sim, float* ms, int cap, int* n);
+
+/* FluidSim2D::saveStats (src/FluidSim2D.cpp:738-750,
+ * src/PerformanceCounter.cpp:58-74): writes perf and conservation CSV files
+ * in the reference's formats.  Either path may be NULL to skip that file. */
+int fs2d_save_stats(fs2d_sim* sim, const char* perfPath, const char* conservationPath);
+
+/* Use `stream` (a cudaStream_t) for all subsequent work of this handle;
+ * NULL restores the handle's own stream. */
+int fs2d_set_stream(fs2d_sim* sim, void* stream);
+
+/* Number of kernels this handle has launched so far. */
+int fs2d_launch_count(fs2d_sim* sim, unsigned long long* out);
+
+/* Message of the last error on the calling thread ("" if none). */
+const char* fs2d_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FS2D_H */
