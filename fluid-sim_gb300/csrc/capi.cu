@@ -1,0 +1,659 @@
+// capi.cu — the C ABI (include/fs2d.h): handle lifetime, frame and stage
+// drivers, host <-> device state transfer, statistics and CSV output.
+//
+// Mirrors FluidSim2D (include/FluidSim2D.h:65-176, src/FluidSim2D.cpp):
+// create seeds particles on the host with libc rand() in the reference's
+// loop order, so the same rand() state gives the same particles; every
+// stage then runs on the device.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fs2d_internal.cuh"
+
+namespace fs2d {
+
+static thread_local char g_err[1024] = "";
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+int check_cuda(cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return 0;
+    set_error("%s: %s", what, cudaGetErrorString(e));
+    return e == cudaErrorMemoryAllocation ? FS2D_ERR_ALLOC : FS2D_ERR_CUDA;
+}
+
+unsigned long long wave_begin(Sim* s) {
+    // progress values are base + (columns done); columns < 2^24
+    s->wave_launch++;
+    return s->wave_launch << 24;
+}
+
+namespace {
+
+struct Host {
+    Sim sim;
+    std::vector<float> frame_stage_ms;  // numStages per frame
+    bool stats_pending = false;
+};
+
+template <typename T>
+int dalloc(T** p, size_t n) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+        return FS2D_ERR_ALLOC;
+    }
+    e = cudaMemset(*p, 0, n * sizeof(T));
+    return check_cuda(e, "cudaMemset");
+}
+
+int num_stages(const Sim* s) { return s->mode == FS2D_SEMILAGRANGIAN ? 7 : 8; }
+
+const int kSlStages[7] = {FS2D_STAGE_CREATE_WATER_LEVEL_SET, FS2D_STAGE_APPLY_SEMI_LAGRANGIAN_ADVECTION,
+                          FS2D_STAGE_APPLY_GRAVITY,          FS2D_STAGE_CREATE_SOLID_LEVEL_SET,
+                          FS2D_STAGE_APPLY_PROJECTION,       FS2D_STAGE_UPDATE_VELOCITY,
+                          FS2D_STAGE_APPLY_ADVECTION};
+const int kPicStages[8] = {FS2D_STAGE_CREATE_WATER_LEVEL_SET, FS2D_STAGE_TRANSFER_VELOCITY_TO_GRID,
+                           FS2D_STAGE_APPLY_GRAVITY,          FS2D_STAGE_CREATE_SOLID_LEVEL_SET,
+                           FS2D_STAGE_APPLY_PROJECTION,       FS2D_STAGE_UPDATE_VELOCITY,
+                           FS2D_STAGE_UPDATE_PARTICLE_VELOCITIES, FS2D_STAGE_APPLY_ADVECTION};
+
+int alloc_particles(Sim* s, size_t cap) {
+    cudaFree(s->pos);
+    cudaFree(s->vel);
+    cudaFree(s->ent_u);
+    cudaFree(s->ent_v);
+    s->pos = nullptr;
+    s->vel = nullptr;
+    s->ent_u = s->ent_v = nullptr;
+    int rc;
+    if ((rc = dalloc(&s->pos, cap))) return rc;
+    if ((rc = dalloc(&s->vel, cap))) return rc;
+    if ((rc = dalloc(&s->ent_u, 4 * cap))) return rc;
+    if ((rc = dalloc(&s->ent_v, 4 * cap))) return rc;
+    s->np_cap = cap;
+    size_t need = std::max(std::max(s->N, std::max(s->NU, s->NV)), cap) / 32 + 4096;
+    if (4 * need > s->partial_cap) {
+        cudaFree(s->partial);
+        s->partial = nullptr;
+        if ((rc = dalloc(&s->partial, 4 * need))) return rc;
+        s->partial_cap = 4 * need;
+    }
+    return 0;
+}
+
+int alloc_all(Sim* s) {
+    int rc;
+    const size_t N = s->N, NU = s->NU, NV = s->NV;
+#define A(ptr, n) \
+    if ((rc = dalloc(&s->ptr, (n)))) return rc
+    A(cell, N);
+    A(phi, N);
+    A(p, N);
+    A(u, NU);
+    A(v, NV);
+    A(nu, NU);
+    A(nv, NV);
+    A(t, N);
+    A(seed_key, N);
+    A(phi_tmp, N);
+    A(u0, NU);
+    A(v0, NV);
+    A(udiv, NU);
+    A(vdiv, NV);
+    A(mask_u, NU);
+    A(mask_v, NV);
+    A(cnt_u, NU + 1);
+    A(cnt_v, NV + 1);
+    A(fill_u, NU);
+    A(fill_v, NV);
+    s->scan_tmp_n = std::max(NU, NV) / 4096 + 4;
+    A(scan_tmp, s->scan_tmp_n);
+    size_t tiles = (size_t)((s->NX + 1 + 31) / 32) * ((s->NY + 31) / 32) + (size_t)((s->NX + 31) / 32) * ((s->NY + 1 + 31) / 32);
+    A(tile_range, tiles);
+    A(max_layer, 16);
+    A(Adiag, N);
+    A(Ax, N);
+    A(Ay, N);
+    A(rhs, N);
+    A(precon, N);
+    A(coef_f, N);
+    A(coef_b, N);
+    A(r, N);
+    A(z, N);
+    A(q, N);
+    A(w, N);
+    A(s0, N);
+    A(s1, N);
+    A(pcg, 1);
+    s->progress_cap = std::max(s->NX, s->NY) / 32 + 2;
+    A(progress, (size_t)s->progress_cap);
+    A(stats, 1);
+    A(err, 1);
+#undef A
+    if ((rc = check_cuda(cudaMallocHost((void**)&s->pcg_host, sizeof(PcgScalars)), "cudaMallocHost"))) return rc;
+    if ((rc = check_cuda(cudaMallocHost((void**)&s->stats_host, sizeof(FrameStats)), "cudaMallocHost"))) return rc;
+    if ((rc = check_cuda(cudaMallocHost((void**)&s->err_host, sizeof(int)), "cudaMallocHost"))) return rc;
+    memset(s->pcg_host, 0, sizeof(PcgScalars));
+    memset(s->stats_host, 0, sizeof(FrameStats));
+    *s->err_host = 0;
+    return 0;
+}
+
+void free_all(Sim* s) {
+    void* ptrs[] = {s->cell, s->phi, s->p, s->u, s->v, s->nu, s->nv, s->pos, s->vel, s->t, s->seed_key,
+                    s->phi_tmp, s->surface, s->u0, s->v0, s->udiv, s->vdiv, s->mask_u, s->mask_v, s->cnt_u,
+                    s->cnt_v, s->fill_u, s->fill_v, s->ent_u, s->ent_v, s->scan_tmp, s->tile_range, s->max_layer,
+                    s->Adiag, s->Ax, s->Ay, s->rhs, s->precon, s->coef_f, s->coef_b, s->r, s->z, s->q, s->w, s->s0,
+                    s->s1, s->partial, s->pcg, s->progress, s->stats, s->err};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (s->pcg_host) cudaFreeHost(s->pcg_host);
+    if (s->stats_host) cudaFreeHost(s->stats_host);
+    if (s->err_host) cudaFreeHost(s->err_host);
+    for (auto& e : s->ev)
+        if (e) cudaEventDestroy(e);
+    if (s->own_stream) cudaStreamDestroy(s->own_stream);
+    free(s->hist);
+}
+
+// libc rand() jitter exactly as src/FluidSim2D.cpp:19-21,52-64.
+double randf(float max) { return ((double)rand() / (double)RAND_MAX) * max; }
+
+int run_stage_impl(Sim* s, int stage, int* status) {
+    switch (stage) {
+        case FS2D_STAGE_CREATE_WATER_LEVEL_SET: return levelset_create(s);
+        case FS2D_STAGE_TRANSFER_VELOCITY_TO_GRID: return p2g(s);
+        case FS2D_STAGE_APPLY_SEMI_LAGRANGIAN_ADVECTION: return sl_advect(s);
+        case FS2D_STAGE_APPLY_GRAVITY: return apply_gravity(s);
+        case FS2D_STAGE_CREATE_SOLID_LEVEL_SET: return 0;  // empty in the reference (:734-736)
+        case FS2D_STAGE_APPLY_PROJECTION: return projection(s, status);
+        case FS2D_STAGE_UPDATE_VELOCITY: return update_velocity(s);
+        case FS2D_STAGE_UPDATE_PARTICLE_VELOCITIES: return g2p(s);
+        case FS2D_STAGE_APPLY_ADVECTION: return advect_particles(s);
+        default:
+            set_error("unknown stage %d", stage);
+            return FS2D_ERR_INVALID;
+    }
+}
+
+// Reads the device error word and the level-set statistics after the stream
+// drained; appends a history entry when the level-set stage ran.
+int finish(Host* h) {
+    Sim* s = &h->sim;
+    FS2D_CUDA(cudaMemcpyAsync(s->err_host, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaMemcpyAsync(s->stats_host, s->stats, sizeof(FrameStats), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    if (h->stats_pending) {
+        if (s->hist_n == s->hist_cap) {
+            size_t cap = s->hist_cap ? 2 * s->hist_cap : 64;
+            double* nh = (double*)realloc(s->hist, cap * 3 * sizeof(double));
+            if (!nh) {
+                set_error("out of host memory");
+                return FS2D_ERR_ALLOC;
+            }
+            s->hist = nh;
+            s->hist_cap = cap;
+        }
+        s->hist[3 * s->hist_n] = s->stats_host->volume;
+        s->hist[3 * s->hist_n + 1] = s->stats_host->energy;
+        s->hist[3 * s->hist_n + 2] = s->stats_host->particle_energy;
+        s->hist_n++;
+        h->stats_pending = false;
+    }
+    int e = *s->err_host;
+    if (e) {
+        FS2D_CUDA(cudaMemsetAsync(s->err, 0, sizeof(int), s->stream));
+        if (e & 1) {
+            set_error("a wavefront sweep timed out waiting for its neighbour strip");
+            return FS2D_ERR_TIMEOUT;
+        }
+        set_error("non-finite or out-of-domain particle position");
+        return FS2D_ERR_NONFINITE;
+    }
+    return 0;
+}
+
+Host* H(fs2d_sim* p) { return reinterpret_cast<Host*>(p); }
+
+}  // namespace
+}  // namespace fs2d
+
+using namespace fs2d;
+
+extern "C" {
+
+void fs2d_default_options(fs2d_options* o) {
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->precision = FS2D_PRECISION_FP64;
+    o->mic_tau = 0.999;
+    o->mic_sigma = 0.25;
+    o->pcg_tol = 1e-12;
+    o->pcg_max_iters = 200;
+    o->ir_inner_tol = 1e-4;
+    o->ir_max_outer = 30;
+    o->p2g_mode = FS2D_P2G_ORDERED;
+    o->extrapolate_band = 0;
+    o->use_seed = 0;
+    o->seed = 0;
+    o->device = 0;
+}
+
+const char* fs2d_last_error(void) { return g_err; }
+
+int fs2d_create(const fs2d_config* cfg, const fs2d_options* opt, fs2d_sim** out) {
+    if (!cfg || !out) {
+        set_error("fs2d_create: null argument");
+        return FS2D_ERR_INVALID;
+    }
+    *out = nullptr;
+    const int NX = cfg->sizeX, NY = cfg->sizeY;
+    if (NX < 3 || NY < 3 || cfg->particlesPerCellSqrt < 1 || !(cfg->dx > 0) || !cfg->initialValues ||
+        (cfg->mode != FS2D_SEMILAGRANGIAN && cfg->mode != FS2D_PICFLIP)) {
+        set_error("fs2d_create: invalid configuration");
+        return FS2D_ERR_INVALID;
+    }
+    if ((long long)NX * NY > (1ll << 28)) {
+        set_error("fs2d_create: grid of %d x %d cells is too large", NX, NY);
+        return FS2D_ERR_INVALID;
+    }
+    for (int j = 0; j < NY; j++)
+        for (int i = 0; i < NX; i++) {
+            bool border = i == 0 || j == 0 || i == NX - 1 || j == NY - 1;
+            uint8_t c = cfg->initialValues[(size_t)j * NX + i];
+            if (c > FS2D_SOLID || (border && c != FS2D_SOLID)) {
+                set_error("fs2d_create: label %d at (%d, %d): labels must be 0..2 and border cells SOLID", c, i, j);
+                return FS2D_ERR_INVALID;
+            }
+        }
+    fs2d_options o;
+    if (opt) o = *opt; else fs2d_default_options(&o);
+    if (o.precision != FS2D_PRECISION_FP64) {
+        set_error("fs2d_create: precision mode %d is not available in this build", o.precision);
+        return FS2D_ERR_INVALID;
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= o.device) {
+        set_error("fs2d_create: no CUDA device %d", o.device);
+        return FS2D_ERR_CUDA;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, o.device) != cudaSuccess || !prop.cooperativeLaunch) {
+        set_error("fs2d_create: device %d does not support cooperative launches", o.device);
+        return FS2D_ERR_CUDA;
+    }
+    if (cudaSetDevice(o.device) != cudaSuccess) {
+        set_error("fs2d_create: cudaSetDevice(%d) failed", o.device);
+        return FS2D_ERR_CUDA;
+    }
+    Host* h = new (std::nothrow) Host();
+    if (!h) {
+        set_error("out of host memory");
+        return FS2D_ERR_ALLOC;
+    }
+    Sim* s = &h->sim;
+    s->device = o.device;
+    s->opt = o;
+    s->NX = NX;
+    s->NY = NY;
+    s->ppc_sqrt = cfg->particlesPerCellSqrt;
+    s->mode = cfg->mode;
+    s->dt = cfg->dt;
+    s->dx = cfg->dx;
+    s->dr = 0.9 * cfg->dx;
+    s->rho = cfg->rho;
+    s->gx = cfg->gravityX;
+    s->gy = cfg->gravityY;
+    s->alpha = cfg->picFlipAlpha;
+    s->N = (size_t)NX * NY;
+    s->NU = (size_t)(NX + 1) * NY;
+    s->NV = (size_t)NX * (NY + 1);
+
+    // particle seeding (src/FluidSim2D.cpp:49-69)
+    if (o.use_seed) srand(o.seed);
+    const int ppc = s->ppc_sqrt * s->ppc_sqrt;
+    std::vector<double> pos;
+    size_t fluid = 0;
+    const float dist = 1.0f / s->ppc_sqrt;
+    for (int j = 0; j < NY; j++)
+        for (int i = 0; i < NX; i++)
+            if (cfg->initialValues[(size_t)j * NX + i] == FS2D_FLUID) {
+                fluid++;
+                for (int k = 0; k < ppc; k++) {
+                    int x = k % s->ppc_sqrt;
+                    int y = k / s->ppc_sqrt;
+                    double px = ((double)i + dist * x + randf(dist)) * s->dx;
+                    double py = ((double)j + dist * y + randf(dist)) * s->dx;
+                    pos.push_back(px);
+                    pos.push_back(py);
+                }
+            }
+    s->np = pos.size() / 2;
+    s->orig_volume = fluid * s->dx * s->dx;
+
+    int rc = check_cuda(cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!rc) {
+        s->stream = s->own_stream;
+        for (auto& e : s->ev)
+            if (!rc) rc = check_cuda(cudaEventCreate(&e), "cudaEventCreate");
+    }
+    if (!rc) rc = alloc_all(s);
+    if (!rc) rc = alloc_particles(s, std::max<size_t>(s->np, 1024));
+    if (!rc) rc = check_cuda(cudaMemcpy(s->cell, cfg->initialValues, s->N, cudaMemcpyHostToDevice), "upload cell");
+    if (!rc && s->np)
+        rc = check_cuda(cudaMemcpy(s->pos, pos.data(), s->np * sizeof(double2), cudaMemcpyHostToDevice), "upload pos");
+    if (rc) {
+        free_all(s);
+        delete h;
+        return rc;
+    }
+    s->stats_host->volume = s->orig_volume;
+    *out = reinterpret_cast<fs2d_sim*>(h);
+    return FS2D_OK;
+}
+
+int fs2d_destroy(fs2d_sim* p) {
+    if (!p) return FS2D_OK;
+    Host* h = H(p);
+    cudaSetDevice(h->sim.device);
+    if (h->sim.stream) cudaStreamSynchronize(h->sim.stream);
+    free_all(&h->sim);
+    delete h;
+    return FS2D_OK;
+}
+
+int fs2d_run_stage(fs2d_sim* p, int stage) {
+    if (!p) return FS2D_ERR_INVALID;
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    int status = 0;
+    int rc = run_stage_impl(s, stage, &status);
+    if (rc) return rc;
+    if (stage == FS2D_STAGE_CREATE_WATER_LEVEL_SET) h->stats_pending = true;
+    rc = finish(h);
+    return rc ? rc : status;
+}
+
+int fs2d_run_frame(fs2d_sim* p) {
+    if (!p) return FS2D_ERR_INVALID;
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    const int n = num_stages(s);
+    const int* st = s->mode == FS2D_SEMILAGRANGIAN ? kSlStages : kPicStages;
+    int status = 0;
+    for (int k = 0; k < n; k++) {
+        FS2D_CUDA(cudaEventRecord(s->ev[2 * k], s->stream));
+        int sst = 0;
+        int rc = run_stage_impl(s, st[k], &sst);
+        if (rc) return rc;
+        if (sst) status = sst;
+        FS2D_CUDA(cudaEventRecord(s->ev[2 * k + 1], s->stream));
+        if (st[k] == FS2D_STAGE_CREATE_WATER_LEVEL_SET) h->stats_pending = true;
+    }
+    int rc = finish(h);
+    for (int k = 0; k < n; k++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, s->ev[2 * k], s->ev[2 * k + 1]);
+        s->stage_ms[k] = ms;
+        h->frame_stage_ms.push_back(ms);
+    }
+    s->n_stage_times = n;
+    s->current_time += s->dt;
+    s->frames++;
+    s->last_status = rc ? rc : status;
+    return s->last_status;
+}
+
+int fs2d_step(fs2d_sim* p, int nframes) {
+    int last = 0;
+    for (int k = 0; k < nframes; k++) {
+        int rc = fs2d_run_frame(p);
+        if (rc && rc != FS2D_ERR_NOT_CONVERGED) return rc;
+        if (rc) last = rc;
+    }
+    return last;
+}
+
+int fs2d_num_particles(fs2d_sim* p, size_t* n) {
+    if (!p || !n) return FS2D_ERR_INVALID;
+    *n = H(p)->sim.np;
+    return FS2D_OK;
+}
+
+int fs2d_upload_state(fs2d_sim* p, const fs2d_state* st) {
+    if (!p || !st) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    auto up = [&](void* d, const void* src, size_t bytes) -> int {
+        if (!src) return 0;
+        return check_cuda(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, s->stream), "upload");
+    };
+    int rc = 0;
+    if (st->cell) {
+        for (int j = 0; j < s->NY && !rc; j++)
+            for (int i = 0; i < s->NX; i++) {
+                bool border = i == 0 || j == 0 || i == s->NX - 1 || j == s->NY - 1;
+                uint8_t c = st->cell[(size_t)j * s->NX + i];
+                if (c > FS2D_SOLID || (border && c != FS2D_SOLID)) {
+                    set_error("fs2d_upload_state: label %d at (%d, %d)", c, i, j);
+                    return FS2D_ERR_INVALID;
+                }
+            }
+    }
+    rc = rc ? rc : up(s->cell, st->cell, s->N);
+    rc = rc ? rc : up(s->phi, st->phi, s->N * sizeof(double));
+    rc = rc ? rc : up(s->p, st->p, s->N * sizeof(double));
+    rc = rc ? rc : up(s->u, st->u, s->NU * sizeof(double));
+    rc = rc ? rc : up(s->v, st->v, s->NV * sizeof(double));
+    rc = rc ? rc : up(s->nu, st->newU, s->NU * sizeof(double));
+    rc = rc ? rc : up(s->nv, st->newV, s->NV * sizeof(double));
+    if (rc) return rc;
+    if (st->particles && st->particleVels) {
+        size_t n = st->numParticles;
+        if (n > s->np_cap) {
+            FS2D_CUDA(cudaStreamSynchronize(s->stream));
+            rc = alloc_particles(s, n + n / 4);
+            if (rc) return rc;
+        }
+        s->np = n;
+        if (n) {
+            rc = up(s->pos, st->particles, n * sizeof(double2));
+            rc = rc ? rc : up(s->vel, st->particleVels, n * sizeof(double2));
+        }
+    } else if (st->particles || st->particleVels) {
+        set_error("fs2d_upload_state: particles and particleVels must be given together");
+        return FS2D_ERR_INVALID;
+    }
+    if (rc) return rc;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    return FS2D_OK;
+}
+
+int fs2d_download_state(fs2d_sim* p, fs2d_state* st) {
+    if (!p || !st) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    if ((st->particles || st->particleVels) && st->numParticles < s->np) {
+        set_error("fs2d_download_state: particle buffers hold %zu, need %zu", st->numParticles, s->np);
+        st->numParticles = s->np;
+        return FS2D_ERR_INVALID;
+    }
+    auto dn = [&](void* dst, const void* d, size_t bytes) -> int {
+        if (!dst || !bytes) return 0;
+        return check_cuda(cudaMemcpyAsync(dst, d, bytes, cudaMemcpyDeviceToHost, s->stream), "download");
+    };
+    int rc = dn(st->cell, s->cell, s->N);
+    rc = rc ? rc : dn(st->phi, s->phi, s->N * sizeof(double));
+    rc = rc ? rc : dn(st->p, s->p, s->N * sizeof(double));
+    rc = rc ? rc : dn(st->u, s->u, s->NU * sizeof(double));
+    rc = rc ? rc : dn(st->v, s->v, s->NV * sizeof(double));
+    rc = rc ? rc : dn(st->newU, s->nu, s->NU * sizeof(double));
+    rc = rc ? rc : dn(st->newV, s->nv, s->NV * sizeof(double));
+    rc = rc ? rc : dn(st->particles, s->pos, s->np * sizeof(double2));
+    rc = rc ? rc : dn(st->particleVels, s->vel, s->np * sizeof(double2));
+    if (rc) return rc;
+    st->numParticles = s->np;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    return FS2D_OK;
+}
+
+int fs2d_set_params(fs2d_sim* p, double gx, double gy, double alpha, double dt) {
+    if (!p) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    s->gx = gx;
+    s->gy = gy;
+    s->alpha = alpha;
+    s->dt = dt;
+    return FS2D_OK;
+}
+
+int fs2d_get_stats(fs2d_sim* p, fs2d_stats* out) {
+    if (!p || !out) return FS2D_ERR_INVALID;
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    out->waterVolume = s->stats_host->volume;
+    out->totalEnergy = s->stats_host->energy;
+    out->particleTotalEnergy = s->stats_host->particle_energy;
+    out->origWaterVolume = s->orig_volume;
+    out->currentTime = s->current_time;
+    out->frames = s->frames;
+    out->pcgIterations = s->last_iters;
+    out->irOuterIterations = s->last_outer;
+    out->pcgRelResidual = s->last_rel_res;
+    out->lastStatus = s->last_status;
+    return FS2D_OK;
+}
+
+int fs2d_get_history(fs2d_sim* p, double* vol, double* en, double* pen, size_t cap, size_t* n) {
+    if (!p) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    size_t m = std::min(cap, s->hist_n);
+    for (size_t k = 0; k < m; k++) {
+        if (vol) vol[k] = s->hist[3 * k];
+        if (en) en[k] = s->hist[3 * k + 1];
+        if (pen) pen[k] = s->hist[3 * k + 2];
+    }
+    if (n) *n = s->hist_n;
+    return FS2D_OK;
+}
+
+static int run_diag(fs2d_sim* p) {
+    if (!p) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    int rc = diagnostics(s);
+    if (rc) return rc;
+    FS2D_CUDA(cudaMemcpyAsync(s->stats_host, s->stats, sizeof(FrameStats), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    return FS2D_OK;
+}
+
+int fs2d_avg_pressure(fs2d_sim* p, double* out) {
+    int rc = run_diag(p);
+    if (!rc && out) *out = H(p)->sim.stats_host->avg_p;
+    return rc;
+}
+int fs2d_avg_pressure_in_fluid(fs2d_sim* p, double* out) {
+    int rc = run_diag(p);
+    if (!rc && out) *out = H(p)->sim.stats_host->avg_p_fluid;
+    return rc;
+}
+int fs2d_max_velocity(fs2d_sim* p, double* out) {
+    int rc = run_diag(p);
+    if (!rc && out) *out = H(p)->sim.stats_host->max_vel;
+    return rc;
+}
+
+int fs2d_get_stage_times(fs2d_sim* p, float* ms, int cap, int* n) {
+    if (!p) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    for (int k = 0; k < std::min(cap, s->n_stage_times); k++) ms[k] = s->stage_ms[k];
+    if (n) *n = s->n_stage_times;
+    return FS2D_OK;
+}
+
+// PerformanceCounter (src/PerformanceCounter.cpp:16-74): a 30-frame ring of
+// stage times, averaged once the ring is full; saveToFile writes one row per
+// frame from frame 30 on, each stage's average followed by ','.  The
+// conservation file follows FluidSim2D::saveStats (src/FluidSim2D.cpp:738-750).
+int fs2d_save_stats(fs2d_sim* p, const char* perf_path, const char* cons_path) {
+    if (!p) return FS2D_ERR_INVALID;
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    if (perf_path) {
+        const int ns = num_stages(s);
+        const int kSamples = 30;
+        std::vector<float> ring((size_t)ns * kSamples, 0.0f), avg(ns, 0.0f);
+        std::string buf;
+        bool finished = false;
+        size_t frames = h->frame_stage_ms.size() / ns;
+        for (size_t f = 0; f < frames; f++) {
+            int slot = (int)(f % kSamples);
+            for (int k = 0; k < ns; k++) ring[(size_t)k * kSamples + slot] = h->frame_stage_ms[f * ns + k];
+            if (finished) {
+                for (int k = 0; k < ns; k++) {
+                    float a = 0.0f;
+                    for (int m = 0; m < kSamples; m++) a += ring[(size_t)k * kSamples + m];
+                    avg[k] = a / kSamples;
+                }
+            }
+            if (slot == kSamples - 1) finished = true;
+            if (f >= (size_t)kSamples) {
+                for (int k = 0; k < ns; k++) {
+                    buf += std::to_string(avg[k]);
+                    buf += ',';
+                }
+                buf += '\n';
+            }
+        }
+        FILE* fp = fopen(perf_path, "w+");
+        if (!fp) {
+            set_error("cannot open %s", perf_path);
+            return FS2D_ERR_INVALID;
+        }
+        fputs(buf.c_str(), fp);
+        fclose(fp);
+    }
+    if (cons_path) {
+        FILE* fp = fopen(cons_path, "w+");
+        if (!fp) {
+            set_error("cannot open %s", cons_path);
+            return FS2D_ERR_INVALID;
+        }
+        fputs("Total Volume, Total Energy, Total Energy (Particle) \n", fp);
+        for (size_t k = 0; k < s->hist_n; k++)
+            fprintf(fp, "%f, %f, %f\n", s->hist[3 * k], s->hist[3 * k + 1], s->hist[3 * k + 2]);
+        fclose(fp);
+    }
+    return FS2D_OK;
+}
+
+int fs2d_set_stream(fs2d_sim* p, void* stream) {
+    if (!p) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+    return FS2D_OK;
+}
+
+int fs2d_launch_count(fs2d_sim* p, unsigned long long* out) {
+    if (!p || !out) return FS2D_ERR_INVALID;
+    *out = H(p)->sim.launches;
+    return FS2D_OK;
+}
+
+}  // extern "C"

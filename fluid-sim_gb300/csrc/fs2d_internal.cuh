@@ -1,0 +1,164 @@
+// fs2d_internal.cuh — device state and shared helpers of the GB300 FluidSim2D step.
+//
+// One simulation handle owns all of its device memory.  Grids are row-major
+// (element (i, j) at j*width + i) exactly as the reference's Array2D
+// (include/Array2D.h:41-49); u faces are (NX+1) x NY, v faces NX x (NY+1)
+// (include/MACGrid2D.h:19-25); particles are interleaved (x, y) pairs.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stddef.h>
+
+#include "../../include/fs2d.h"
+
+namespace fs2d {
+
+constexpr uint8_t kEmpty = FS2D_EMPTY;
+constexpr uint8_t kFluid = FS2D_FLUID;
+constexpr uint8_t kSolid = FS2D_SOLID;
+constexpr uint32_t kUnknown = 0xFFFFFFFFu;   // extrapolation mask of an unknown face
+
+// Scalars of one pressure solve, kept in device memory so that the PCG loop
+// runs without host round trips.  Finalised by the last block of each
+// reduction kernel.
+struct PcgScalars {
+    double sigma;       // z . r
+    double alpha;
+    double beta;
+    double rhs_norm;    // ||b||inf
+    double r_norm;      // ||r||inf after the last update
+    double tol_abs;     // tol * ||b||inf
+    int iter;           // completed iterations (reference's `iter`)
+    int done;           // 1 once the solve stopped
+    int first;          // 1 until the first search direction was formed
+    unsigned int ticket[4];  // last-block-done counters, one per reduction kernel
+};
+
+// Scalars of the per-frame statistics (createWaterLevelSet, src/FluidSim2D.cpp:709-731).
+struct FrameStats {
+    double volume;
+    double energy;
+    double particle_energy;
+    double avg_p;
+    double avg_p_fluid;
+    double max_vel;
+    unsigned int ticket;
+    unsigned int pad;
+};
+
+struct Sim {
+    // configuration
+    int NX = 0, NY = 0, ppc_sqrt = 0, mode = 0;
+    double dt = 0, dx = 0, dr = 0, rho = 0, gx = 0, gy = 0, alpha = 0;
+    fs2d_options opt{};
+    size_t N = 0, NU = 0, NV = 0;
+
+    // state (FluidSim2D public fields)
+    uint8_t* cell = nullptr;
+    double* phi = nullptr;
+    double* p = nullptr;
+    double *u = nullptr, *v = nullptr, *nu = nullptr, *nv = nullptr;
+    double2* pos = nullptr;
+    double2* vel = nullptr;
+    size_t np = 0, np_cap = 0;
+
+    // level-set scratch
+    int* t = nullptr;                 // closest particle of each cell (-1 = none)
+    unsigned long long* seed_key = nullptr;
+    double* phi_tmp = nullptr;
+    uint8_t* surface = nullptr;
+
+    // transfer scratch
+    double *u0 = nullptr, *v0 = nullptr;    // pre-advection copy / uDiff source
+    double *udiv = nullptr, *vdiv = nullptr;
+    uint32_t *mask_u = nullptr, *mask_v = nullptr;
+    uint32_t *cnt_u = nullptr, *cnt_v = nullptr;     // P2G contributions per face (then offsets)
+    uint32_t *fill_u = nullptr, *fill_v = nullptr;
+    uint32_t *ent_u = nullptr, *ent_v = nullptr;     // P2G contribution keys, 4 per particle
+    size_t ent_cap = 0;
+    uint32_t* scan_tmp = nullptr;
+    size_t scan_tmp_n = 0;
+    int2* tile_range = nullptr;                      // extrapolation: per 32x32 tile [min,max] layer
+    unsigned int* max_layer = nullptr;
+
+    // projection scratch
+    double *Adiag = nullptr, *Ax = nullptr, *Ay = nullptr, *rhs = nullptr, *precon = nullptr;
+    double2 *coef_f = nullptr, *coef_b = nullptr;    // MIC(0) forward / backward coefficients
+    double *r = nullptr, *z = nullptr, *q = nullptr, *w = nullptr;
+    double *s0 = nullptr, *s1 = nullptr;             // ping-pong search direction
+    double* partial = nullptr;                       // per-block reduction partials
+    size_t partial_cap = 0;
+    PcgScalars* pcg = nullptr;
+    PcgScalars* pcg_host = nullptr;                  // pinned mirror for polling
+
+    // wavefront progress flags (monotonic, 64-bit, never reset)
+    unsigned long long* progress = nullptr;
+    int progress_cap = 0;
+    unsigned long long wave_launch = 0;
+
+    // frame statistics and errors
+    FrameStats* stats = nullptr;
+    FrameStats* stats_host = nullptr;
+    int* err = nullptr;            // device error word: bit 0 timeout, bit 1 non-finite
+    int* err_host = nullptr;
+
+    // history of per-frame conservation values (host)
+    double* hist = nullptr;        // 3 per frame
+    size_t hist_n = 0, hist_cap = 0;
+
+    // bookkeeping
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[20] = {};
+    float stage_ms[10] = {};
+    int n_stage_times = 0;
+    unsigned long long launches = 0;
+    long long frames = 0;
+    double current_time = 0;
+    double orig_volume = 0;
+    int last_iters = 0;
+    int last_outer = 0;
+    double last_rel_res = 0;
+    int last_status = 0;
+    int device = 0;
+};
+
+// ---- error reporting (thread-local message, see fs2d_last_error) ----
+void set_error(const char* fmt, ...);
+int check_cuda(cudaError_t e, const char* what);
+#define FS2D_CUDA(call)                                   \
+    do {                                                  \
+        int _rc = ::fs2d::check_cuda((call), #call);      \
+        if (_rc) return _rc;                              \
+    } while (0)
+
+// Launch helper: counts the launch and reports launch errors.
+#define FS2D_LAUNCH(sim, kernel, grid, block, smem, ...)                               \
+    do {                                                                              \
+        (sim)->launches++;                                                            \
+        kernel<<<(grid), (block), (smem), (sim)->stream>>>(__VA_ARGS__);             \
+        int _rc = ::fs2d::check_cuda(cudaGetLastError(), #kernel);                   \
+        if (_rc) return _rc;                                                          \
+    } while (0)
+
+inline unsigned int blocks_for(size_t n, int threads) { return (unsigned int)((n + threads - 1) / threads); }
+
+// ---- stage entry points (implemented in the per-stage .cu files) ----
+int levelset_create(Sim* s);              // createWaterLevelSet
+int p2g(Sim* s);                          // transferVelocityToGrid
+int sl_advect(Sim* s);                    // applySemiLagrangianAdvection
+int apply_gravity(Sim* s);                // applyGravity
+int projection(Sim* s, int* status);      // applyProjection
+int update_velocity(Sim* s);              // updateVelocity
+int g2p(Sim* s);                          // updateParticleVelocities
+int advect_particles(Sim* s);             // applyAdvection
+int diagnostics(Sim* s);                  // avgPressure, avgPressureInFluid, maxVelocity
+int extrapolate(Sim* s, double* a, uint32_t* mask, int W, int H, double* b, uint32_t* mask_b, int Wb, int Hb);
+int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n);
+
+// ---- wavefront plumbing ----
+// Reserves `n` progress counters and returns the base value for this launch.
+unsigned long long wave_begin(Sim* s);
+
+}  // namespace fs2d

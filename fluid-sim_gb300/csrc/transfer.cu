@@ -1,0 +1,572 @@
+// transfer.cu — particle/grid transfers and velocity extrapolation (FP64, exact).
+//
+//   FluidSim2D::transferVelocityToGrid   src/FluidSim2D.cpp:144-204   (P2G)
+//   FluidSim2D::updateParticleVelocities src/FluidSim2D.cpp:552-568   (G2P)
+//   Array2D::linearDistribute / linearExtract  include/Array2D.h:361-420
+//   Array2D::extrapolate                 include/Array2D.h:552-591
+// Compiled with --fmad=false.
+//
+// P2G, ordered mode: the reference adds each particle's four bilinear
+// contributions into the face grid in particle order.  Here every
+// contribution becomes a key (4*e + corner) in its face's bucket (counting
+// sort: count, exclusive scan, scatter); each face then sorts its few keys
+// and adds them in key order — the reference's order — so the sums are
+// bit-identical and independent of thread scheduling.  Atomic mode adds
+// with FP64 atomics instead (fast, order not reproducible).
+//
+// Extrapolation: the reference's breadth-first search assigns every unknown
+// face a layer L = its 4-connected (L1) grid distance to the nearest known
+// face and sets it to the mean of its neighbours with layer < L, which are
+// all final before any layer-L face is visited.  So the result depends only
+// on the layers, not on the queue order.  Layers come from an exact
+// separable L1 distance transform; values are then propagated in bands of
+// kBand layers, each 32x32 output tile recomputing its band inside a halo of
+// kBand cells (every dependency of a layer in the band lies within kBand
+// cells), so one launch per band replaces one launch per layer.
+#include <cuda_runtime.h>
+#include <algorithm>
+#include "fs2d_device.cuh"
+
+namespace fs2d {
+namespace {
+
+constexpr int kBand = 16;
+constexpr int kTile = 32;
+constexpr int kReg = kTile + 2 * kBand;
+constexpr int kInf = 1 << 29;
+
+// Bilinear corner k (0: (x1,y1), 1: (x2,y1), 2: (x1,y2), 3: (x2,y2)) of a
+// position, with clamped indices and unclamped weights (include/Array2D.h:361-376).
+struct Bilinear {
+    int x1, x2, y1, y2;
+    double dxp, dyp;
+    __device__ Bilinear(double px, double py, int W, int H) {
+        int ui = (int)px, uj = (int)py;
+        dxp = px - ui;
+        dyp = py - uj;
+        x1 = iclamp(ui, 0, W - 1);
+        x2 = iclamp(ui + 1, 0, W - 1);
+        y1 = iclamp(uj, 0, H - 1);
+        y2 = iclamp(uj + 1, 0, H - 1);
+    }
+    __device__ int face(int k, int W) const {
+        int x = (k & 1) ? x2 : x1, y = (k & 2) ? y2 : y1;
+        return y * W + x;
+    }
+    // linearDistribute's contribution: weight * value, evaluated as the
+    // reference does ((wx * wy) * value).
+    __device__ double contrib(int k, double value) const {
+        double wx = (k & 1) ? dxp : (1 - dxp);
+        double wy = (k & 2) ? dyp : (1 - dyp);
+        return wx * wy * value;
+    }
+};
+
+__device__ __forceinline__ void upos(double2 p, double dx, double& x, double& y) { x = p.x / dx; y = p.y / dx - 0.5; }
+__device__ __forceinline__ void vpos(double2 p, double dx, double& x, double& y) { x = p.x / dx - 0.5; y = p.y / dx; }
+
+__global__ void k_p2g_count(const double2* __restrict__ pos, size_t np, double dx, int NX, int NY, uint32_t* cnt_u,
+                            uint32_t* cnt_v) {
+    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    double2 p = pos[e];
+    double x, y;
+    upos(p, dx, x, y);
+    Bilinear bu(x, y, NX + 1, NY);
+    vpos(p, dx, x, y);
+    Bilinear bv(x, y, NX, NY + 1);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        atomicAdd(cnt_u + bu.face(k, NX + 1), 1u);
+        atomicAdd(cnt_v + bv.face(k, NX), 1u);
+    }
+}
+
+__global__ void k_p2g_fill(const double2* __restrict__ pos, size_t np, double dx, int NX, int NY,
+                           const uint32_t* __restrict__ off_u, const uint32_t* __restrict__ off_v, uint32_t* fill_u,
+                           uint32_t* fill_v, uint32_t* ent_u, uint32_t* ent_v) {
+    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    double2 p = pos[e];
+    double x, y;
+    upos(p, dx, x, y);
+    Bilinear bu(x, y, NX + 1, NY);
+    vpos(p, dx, x, y);
+    Bilinear bv(x, y, NX, NY + 1);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        int fu = bu.face(k, NX + 1);
+        ent_u[off_u[fu] + atomicAdd(fill_u + fu, 1u)] = (uint32_t)(4 * e + k);
+        int fv = bv.face(k, NX);
+        ent_v[off_v[fv] + atomicAdd(fill_v + fv, 1u)] = (uint32_t)(4 * e + k);
+    }
+}
+
+// Per face: sort the bucket's keys, then accumulate value and weight in key
+// order from 0.0, divide where the weight is positive, and mark faces whose
+// value is exactly 0.0 unknown (src/FluidSim2D.cpp:175-201).
+template <int COMP>
+__global__ void k_p2g_sum(const double2* __restrict__ pos, const double2* __restrict__ vel, double dx, int NX, int NY,
+                          int W, int H, const uint32_t* __restrict__ off, uint32_t* ent, size_t nfaces, double* out,
+                          uint32_t* mask) {
+    size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (f >= nfaces) return;
+    uint32_t b = off[f], e_ = off[f + 1];
+    // insertion sort of the bucket (buckets hold a few keys per particle nearby)
+    for (uint32_t a = b + 1; a < e_; a++) {
+        uint32_t key = ent[a];
+        uint32_t c = a;
+        while (c > b && ent[c - 1] > key) {
+            ent[c] = ent[c - 1];
+            c--;
+        }
+        ent[c] = key;
+    }
+    double sum = 0.0, wsum = 0.0;
+    for (uint32_t a = b; a < e_; a++) {
+        uint32_t key = ent[a];
+        size_t e = key >> 2;
+        int k = key & 3;
+        double2 p = pos[e];
+        double x, y;
+        if (COMP == 0) upos(p, dx, x, y); else vpos(p, dx, x, y);
+        Bilinear bl(x, y, W, H);
+        double value = COMP == 0 ? vel[e].x : vel[e].y;
+        sum += bl.contrib(k, value);
+        wsum += bl.contrib(k, 1.0);
+    }
+    if (wsum > 0) sum /= wsum;
+    out[f] = sum;
+    mask[f] = (sum == 0.0) ? kUnknown : 0u;
+}
+
+__global__ void k_p2g_atomic(const double2* __restrict__ pos, const double2* __restrict__ vel, size_t np, double dx,
+                             int NX, int NY, double* u, double* udiv, double* v, double* vdiv) {
+    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    double2 p = pos[e], w = vel[e];
+    double x, y;
+    upos(p, dx, x, y);
+    Bilinear bu(x, y, NX + 1, NY);
+    vpos(p, dx, x, y);
+    Bilinear bv(x, y, NX, NY + 1);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        int fu = bu.face(k, NX + 1), fv = bv.face(k, NX);
+        atomicAdd(u + fu, bu.contrib(k, w.x));
+        atomicAdd(udiv + fu, bu.contrib(k, 1.0));
+        atomicAdd(v + fv, bv.contrib(k, w.y));
+        atomicAdd(vdiv + fv, bv.contrib(k, 1.0));
+    }
+}
+
+__global__ void k_p2g_normalize(double* a, const double* __restrict__ div, uint32_t* mask, size_t n) {
+    size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (f >= n) return;
+    double s = a[f], w = div[f];
+    if (w > 0) s /= w;
+    a[f] = s;
+    mask[f] = (s == 0.0) ? kUnknown : 0u;
+}
+
+// ---- G2P (src/FluidSim2D.cpp:552-568) ----
+
+// linearExtract (include/Array2D.h:402-420) of a face grid, or of the
+// difference of two face grids (uDiff = newMac.u - mac.u, rounded per face).
+__device__ __forceinline__ double extract(const double* __restrict__ a, const double* __restrict__ b, double px,
+                                          double py, int W, int H) {
+    Bilinear bl(px, py, W, H);
+    int f0 = bl.y1 * W + bl.x1, f1 = bl.y1 * W + bl.x2, f2 = bl.y2 * W + bl.x1, f3 = bl.y2 * W + bl.x2;
+    double a0 = a[f0], a1 = a[f1], a2 = a[f2], a3 = a[f3];
+    if (b != nullptr) {
+        a0 = a0 - b[f0];
+        a1 = a1 - b[f1];
+        a2 = a2 - b[f2];
+        a3 = a3 - b[f3];
+    }
+    double value = 0.0;
+    value += a0 * (1 - bl.dxp) * (1 - bl.dyp);
+    value += a1 * bl.dxp * (1 - bl.dyp);
+    value += a2 * (1 - bl.dxp) * bl.dyp;
+    value += a3 * bl.dxp * bl.dyp;
+    return value;
+}
+
+__global__ void k_g2p(const double2* __restrict__ pos, double2* vel, size_t np, const double* __restrict__ nu,
+                      const double* __restrict__ nv, const double* __restrict__ u, const double* __restrict__ v,
+                      double dx, int NX, int NY, double alpha) {
+    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    double2 p = pos[e];
+    double ux, uy, vx, vy;
+    upos(p, dx, ux, uy);
+    vpos(p, dx, vx, vy);
+    double picx = extract(nu, nullptr, ux, uy, NX + 1, NY);
+    double picy = extract(nv, nullptr, vx, vy, NX, NY + 1);
+    double2 w = vel[e];
+    double flipx = w.x + extract(nu, u, ux, uy, NX + 1, NY);
+    double flipy = w.y + extract(nv, v, vx, vy, NX, NY + 1);
+    vel[e] = make_double2(alpha * picx + (1 - alpha) * flipx, alpha * picy + (1 - alpha) * flipy);
+}
+
+// ---- extrapolation ----
+
+// Column pass of the L1 distance transform: vertical distance to the nearest
+// known face (mask 0) of the same column, kInf if none.  Written into d.
+__global__ void k_dt_cols(const uint32_t* __restrict__ mask, int* d, int W, int H) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= W) return;
+    int g = kInf;
+    for (int y = 0; y < H; y++) {
+        size_t c = (size_t)y * W + x;
+        g = (mask[c] == 0) ? 0 : (g >= kInf ? kInf : g + 1);
+        d[c] = g;
+    }
+    g = kInf;
+    for (int y = H - 1; y >= 0; y--) {
+        size_t c = (size_t)y * W + x;
+        int v = d[c];
+        g = (g >= kInf) ? v : min(v, g + 1);
+        d[c] = g;
+    }
+}
+
+// Row pass: D(x) = min_x' (col(x') + |x - x'|) via a block-wide prefix-min of
+// col(x') - x' (forward) and suffix-min of col(x') + x' (backward).  Writes
+// layers into mask (0 known, >= 1 unknown, kUnknown unreachable) and
+// per-32x32-tile layer ranges of the unknown faces.
+__global__ void __launch_bounds__(1024) k_dt_rows(const int* __restrict__ d, uint32_t* mask, int W, int H,
+                                                  int2* tile_range, int tiles_x) {
+    __shared__ int fwd_carry[32], bwd_carry[32];
+    int y = blockIdx.x;
+    int T = blockDim.x;
+    int chunk = (W + T - 1) / T;
+    int x0 = threadIdx.x * chunk, x1 = min(W, x0 + chunk);
+    const int* row = d + (size_t)y * W;
+    // local scans
+    int fm = kInf * 2, bm = kInf * 2;
+    for (int x = x0; x < x1; x++) fm = min(fm, row[x] - x);
+    for (int x = x0; x < x1; x++) bm = min(bm, row[x] + x);
+    // exclusive prefix-min over threads (fm) and suffix-min (bm)
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (T + 31) >> 5;
+    int f_inc = fm, b_inc = bm;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, f_inc, o);
+        if (lane >= o) f_inc = min(f_inc, t);
+        int u = __shfl_down_sync(0xffffffffu, b_inc, o);
+        if (lane + o < 32) b_inc = min(b_inc, u);
+    }
+    if (lane == 31) fwd_carry[wid] = f_inc;
+    if (lane == 0) bwd_carry[wid] = b_inc;
+    __syncthreads();
+    if (wid == 0) {
+        int fv = lane < nw ? fwd_carry[lane] : kInf * 2;
+        int bv = lane < nw ? bwd_carry[lane] : kInf * 2;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int t = __shfl_up_sync(0xffffffffu, fv, o);
+            if (lane >= o) fv = min(fv, t);
+            int u = __shfl_down_sync(0xffffffffu, bv, o);
+            if (lane + o < 32) bv = min(bv, u);
+        }
+        __syncwarp();
+        if (lane < nw) {
+            fwd_carry[lane] = fv;
+            bwd_carry[lane] = bv;
+        }
+    }
+    __syncthreads();
+    int f_prev = __shfl_up_sync(0xffffffffu, f_inc, 1);
+    if (lane == 0) f_prev = kInf * 2;
+    if (wid > 0) f_prev = min(f_prev, fwd_carry[wid - 1]);
+    int b_next = __shfl_down_sync(0xffffffffu, b_inc, 1);
+    if (lane == 31) b_next = kInf * 2;
+    if (wid + 1 < nw) b_next = min(b_next, bwd_carry[wid + 1]);
+    // apply: forward running min from the left, backward from the right
+    int run = f_prev;
+    int tmin = kInf * 2, tmax = -1;
+    int tx_cur = -1;
+    for (int x = x0; x < x1; x++) {
+        run = min(run, row[x] - x);
+        mask[(size_t)y * W + x] = (uint32_t)(run + x);  // provisional forward value
+    }
+    run = b_next;
+    for (int x = x1 - 1; x >= x0; x--) {
+        run = min(run, row[x] + x);
+        int L = min((int)mask[(size_t)y * W + x], run - x);
+        uint32_t out = (L >= kInf) ? kUnknown : (uint32_t)L;
+        mask[(size_t)y * W + x] = out;
+        int tx = x / kTile;
+        if (tx != tx_cur) {
+            if (tx_cur >= 0 && tmax >= 0) {
+                int2* tr = tile_range + (size_t)(y / kTile) * tiles_x + tx_cur;
+                atomicMin(&tr->x, tmin);
+                atomicMax(&tr->y, tmax);
+            }
+            tx_cur = tx;
+            tmin = kInf * 2;
+            tmax = -1;
+        }
+        if (out != 0 && out != kUnknown) {
+            tmin = min(tmin, (int)out);
+            tmax = max(tmax, (int)out);
+        }
+    }
+    if (tx_cur >= 0 && tmax >= 0) {
+        int2* tr = tile_range + (size_t)(y / kTile) * tiles_x + tx_cur;
+        atomicMin(&tr->x, tmin);
+        atomicMax(&tr->y, tmax);
+    }
+}
+
+__global__ void k_tile_init(int2* tr, size_t n) {
+    size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (k < n) tr[k] = make_int2(kInf * 2, -1);
+}
+
+__global__ void k_tile_max(const int2* __restrict__ tr, size_t n, unsigned int* max_layer) {
+    size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (k < n && tr[k].y >= 0) atomicMax(max_layer, (unsigned int)tr[k].y);
+}
+
+// Layers [lo, hi] of one 32x32 tile, recomputed in shared memory inside a
+// halo of kBand cells.  Neighbours outside the region or the grid count as
+// absent; only region cells farther than kBand from the tile can be affected
+// by that, and none of them feeds a tile cell within the band.
+__global__ void __launch_bounds__(256) k_extrap_band(double* a, const uint32_t* __restrict__ layer, int W, int H,
+                                                     const int2* __restrict__ tile_range, int tiles_x, int lo, int hi) {
+    __shared__ double val[kReg * kReg];
+    __shared__ uint32_t lay[kReg * kReg];
+    int tx = blockIdx.x, ty = blockIdx.y;
+    int2 tr = tile_range[(size_t)ty * tiles_x + tx];
+    if (tr.y < lo || tr.x > hi) return;
+    int ox = tx * kTile - kBand, oy = ty * kTile - kBand;
+    for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
+        int rx = k % kReg, ry = k / kReg;
+        int gx = ox + rx, gy = oy + ry;
+        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+            size_t c = (size_t)gy * W + gx;
+            lay[k] = layer[c];
+            val[k] = a[c];
+        } else {
+            lay[k] = kUnknown;
+            val[k] = 0.0;
+        }
+    }
+    for (int L = lo; L <= hi; L++) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
+            if (lay[k] != (uint32_t)L) continue;
+            int rx = k % kReg, ry = k / kReg;
+            double sum = 0.0;
+            int count = 0;
+            if (rx > 0 && lay[k - 1] < (uint32_t)L) { sum += val[k - 1]; count++; }
+            if (rx < kReg - 1 && lay[k + 1] < (uint32_t)L) { sum += val[k + 1]; count++; }
+            if (ry > 0 && lay[k - kReg] < (uint32_t)L) { sum += val[k - kReg]; count++; }
+            if (ry < kReg - 1 && lay[k + kReg] < (uint32_t)L) { sum += val[k + kReg]; count++; }
+            val[k] = count == 0 ? 0 : sum / count;
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kTile * kTile; k += blockDim.x) {
+        int rx = kBand + k % kTile, ry = kBand + k / kTile;
+        int gx = ox + rx, gy = oy + ry;
+        if (gx >= W || gy >= H) continue;
+        uint32_t l = lay[ry * kReg + rx];
+        if (l >= (uint32_t)lo && l <= (uint32_t)hi) a[(size_t)gy * W + gx] = val[ry * kReg + rx];
+    }
+}
+
+// ---- exclusive scan of uint32 (counts -> offsets), n+1 outputs ----
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_blocks(const uint32_t* __restrict__ in, uint32_t* out, size_t n, uint32_t* block_sums) {
+    __shared__ uint32_t sh[32];
+    size_t base = (size_t)blockIdx.x * kScanBlock * 4;
+    uint32_t v[4];
+    uint32_t local = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        size_t idx = base + threadIdx.x * 4 + k;
+        v[k] = idx < n ? in[idx] : 0u;
+        local += v[k];
+    }
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t inc = local;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) sh[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t s = sh[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += t;
+        }
+        sh[lane] = s;
+    }
+    __syncthreads();
+    uint32_t excl = inc - local + (wid > 0 ? sh[wid - 1] : 0u);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        size_t idx = base + threadIdx.x * 4 + k;
+        if (idx < n) out[idx] = excl;
+        excl += v[k];
+    }
+    if (threadIdx.x == blockDim.x - 1) block_sums[blockIdx.x] = sh[31];
+}
+
+__global__ void k_scan_sums(uint32_t* block_sums, int nb, uint32_t* total_out) {
+    // single block: sequential over chunks, parallel within
+    __shared__ uint32_t sh[32];
+    uint32_t carry = 0;
+    for (int base = 0; base < nb; base += blockDim.x) {
+        int k = base + threadIdx.x;
+        uint32_t v = k < nb ? block_sums[k] : 0u;
+        int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        uint32_t inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += t;
+        }
+        __syncthreads();
+        if (lane == 31) sh[wid] = inc;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t s = sh[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t t = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += t;
+            }
+            sh[lane] = s;
+        }
+        __syncthreads();
+        uint32_t excl = inc - v + (wid > 0 ? sh[wid - 1] : 0u) + carry;
+        if (k < nb) block_sums[k] = excl;
+        carry += sh[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *total_out = carry;
+}
+
+__global__ void k_scan_add(uint32_t* out, size_t n, const uint32_t* __restrict__ block_sums) {
+    size_t base = (size_t)blockIdx.x * kScanBlock * 4;
+    uint32_t add = block_sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        size_t idx = base + threadIdx.x * 4 + k;
+        if (idx < n) out[idx] += add;
+    }
+}
+
+}  // namespace
+
+// In-place exclusive scan of data[0..n); data[n] receives the total.
+int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n) {
+    size_t nb = (n + kScanBlock * 4 - 1) / (kScanBlock * 4);
+    if (nb + 1 > s->scan_tmp_n) {
+        set_error("scan: %zu elements exceed scratch", n);
+        return FS2D_ERR_INVALID;
+    }
+    FS2D_LAUNCH(s, k_scan_blocks, (unsigned)nb, kScanBlock, 0, data, data, n, s->scan_tmp);
+    FS2D_LAUNCH(s, k_scan_sums, 1, 1024, 0, s->scan_tmp, (int)nb, data + n);
+    FS2D_LAUNCH(s, k_scan_add, (unsigned)nb, kScanBlock, 0, data, n, s->scan_tmp);
+    return 0;
+}
+
+// Array2D::extrapolate on one or two face grids (b may be null).
+int extrapolate(Sim* s, double* a, uint32_t* mask_a, int Wa, int Ha, double* b, uint32_t* mask_b, int Wb, int Hb) {
+    struct G {
+        double* a;
+        uint32_t* m;
+        int W, H;
+    } grids[2] = {{a, mask_a, Wa, Ha}, {b, mask_b, Wb, Hb}};
+    int ng = b ? 2 : 1;
+    int band_limit = s->opt.extrapolate_band > 0 ? s->opt.extrapolate_band : (1 << 28);
+    unsigned int* maxl = s->max_layer;
+    FS2D_CUDA(cudaMemsetAsync(maxl, 0, 2 * sizeof(unsigned int), s->stream));
+    int* dtmp = (int*)s->udiv;  // scratch: the P2G weight arrays are free here
+    int tiles_x[2], tiles_y[2];
+    size_t tile_off[2] = {0, 0};
+    for (int gi = 0; gi < ng; gi++) {
+        G& g = grids[gi];
+        tiles_x[gi] = (g.W + kTile - 1) / kTile;
+        tiles_y[gi] = (g.H + kTile - 1) / kTile;
+        if (gi == 1) tile_off[1] = (size_t)tiles_x[0] * tiles_y[0];
+        size_t nt = (size_t)tiles_x[gi] * tiles_y[gi];
+        int2* tr = s->tile_range + tile_off[gi];
+        int* d = gi == 0 ? dtmp : (int*)s->vdiv;
+        FS2D_LAUNCH(s, k_tile_init, blocks_for(nt, 256), 256, 0, tr, nt);
+        FS2D_LAUNCH(s, k_dt_cols, blocks_for(g.W, 128), 128, 0, g.m, d, g.W, g.H);
+        FS2D_LAUNCH(s, k_dt_rows, g.H, 1024, 0, d, g.m, g.W, g.H, tr, tiles_x[gi]);
+        FS2D_LAUNCH(s, k_tile_max, blocks_for(nt, 256), 256, 0, tr, nt, maxl + gi);
+    }
+    unsigned int hmax[2] = {0, 0};
+    FS2D_CUDA(cudaMemcpyAsync(hmax, maxl, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    for (int gi = 0; gi < ng; gi++) {
+        G& g = grids[gi];
+        int maxL = (int)std::min<unsigned int>(hmax[gi], (unsigned int)band_limit);
+        for (int lo = 1; lo <= maxL; lo += kBand) {
+            int hi = std::min(lo + kBand - 1, maxL);
+            dim3 grid(tiles_x[gi], tiles_y[gi]);
+            FS2D_LAUNCH(s, k_extrap_band, grid, 256, 0, g.a, g.m, g.W, g.H, s->tile_range + tile_off[gi], tiles_x[gi],
+                        lo, hi);
+        }
+    }
+    return 0;
+}
+
+int p2g(Sim* s) {
+    const int NX = s->NX, NY = s->NY, T = 256;
+    const size_t NU = s->NU, NV = s->NV;
+    if (s->opt.p2g_mode == FS2D_P2G_ATOMIC) {
+        FS2D_CUDA(cudaMemsetAsync(s->u, 0, NU * sizeof(double), s->stream));
+        FS2D_CUDA(cudaMemsetAsync(s->v, 0, NV * sizeof(double), s->stream));
+        FS2D_CUDA(cudaMemsetAsync(s->udiv, 0, NU * sizeof(double), s->stream));
+        FS2D_CUDA(cudaMemsetAsync(s->vdiv, 0, NV * sizeof(double), s->stream));
+        if (s->np > 0)
+            FS2D_LAUNCH(s, k_p2g_atomic, blocks_for(s->np, T), T, 0, s->pos, s->vel, s->np, s->dx, NX, NY, s->u, s->udiv,
+                        s->v, s->vdiv);
+        FS2D_LAUNCH(s, k_p2g_normalize, blocks_for(NU, T), T, 0, s->u, s->udiv, s->mask_u, NU);
+        FS2D_LAUNCH(s, k_p2g_normalize, blocks_for(NV, T), T, 0, s->v, s->vdiv, s->mask_v, NV);
+    } else {
+        FS2D_CUDA(cudaMemsetAsync(s->cnt_u, 0, (NU + 1) * sizeof(uint32_t), s->stream));
+        FS2D_CUDA(cudaMemsetAsync(s->cnt_v, 0, (NV + 1) * sizeof(uint32_t), s->stream));
+        FS2D_CUDA(cudaMemsetAsync(s->fill_u, 0, NU * sizeof(uint32_t), s->stream));
+        FS2D_CUDA(cudaMemsetAsync(s->fill_v, 0, NV * sizeof(uint32_t), s->stream));
+        if (s->np > 0)
+            FS2D_LAUNCH(s, k_p2g_count, blocks_for(s->np, T), T, 0, s->pos, s->np, s->dx, NX, NY, s->cnt_u, s->cnt_v);
+        int rc = exclusive_scan_u32(s, s->cnt_u, NU);
+        if (rc) return rc;
+        rc = exclusive_scan_u32(s, s->cnt_v, NV);
+        if (rc) return rc;
+        if (s->np > 0)
+            FS2D_LAUNCH(s, k_p2g_fill, blocks_for(s->np, T), T, 0, s->pos, s->np, s->dx, NX, NY, s->cnt_u, s->cnt_v,
+                        s->fill_u, s->fill_v, s->ent_u, s->ent_v);
+        FS2D_LAUNCH(s, k_p2g_sum<0>, blocks_for(NU, T), T, 0, s->pos, s->vel, s->dx, NX, NY, NX + 1, NY, s->cnt_u,
+                    s->ent_u, NU, s->u, s->mask_u);
+        FS2D_LAUNCH(s, k_p2g_sum<1>, blocks_for(NV, T), T, 0, s->pos, s->vel, s->dx, NX, NY, NX, NY + 1, s->cnt_v,
+                    s->ent_v, NV, s->v, s->mask_v);
+    }
+    return extrapolate(s, s->u, s->mask_u, NX + 1, NY, s->v, s->mask_v, NX, NY + 1);
+}
+
+int g2p(Sim* s) {
+    const int T = 256;
+    if (s->np > 0)
+        FS2D_LAUNCH(s, k_g2p, blocks_for(s->np, T), T, 0, s->pos, s->vel, s->np, s->nu, s->nv, s->u, s->v, s->dx, s->NX,
+                    s->NY, s->alpha);
+    FS2D_CUDA(cudaMemcpyAsync(s->u, s->nu, s->NU * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+    FS2D_CUDA(cudaMemcpyAsync(s->v, s->nv, s->NV * sizeof(double), cudaMemcpyDeviceToDevice, s->stream));
+    return 0;
+}
+
+}  // namespace fs2d

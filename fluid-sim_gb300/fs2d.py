@@ -1,0 +1,281 @@
+"""Python binding of the GB300 FluidSim2D library (ctypes over include/fs2d.h).
+
+The class mirrors the reference's C++ API (include/FluidSim2D.h:116-150):
+``FluidSim2D.create(config)``, ``runFrame()``, ``update()``, the stage
+methods (``createWaterLevelSet()``, ``transferVelocityToGrid()``, ...) and
+the diagnostics (``avgPressure()``, ``avgPressureInFluid()``,
+``maxVelocity()``, ``saveStats()``).  State fields are read and written
+through ``get_state()`` / ``set_state()`` as numpy arrays in the
+reference's layouts.
+
+There is no CPU fallback: if libfs2d.so is missing or no CUDA device is
+usable, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfs2d.so")
+
+PRECISION = {"fp64": 0, "mixed": 1}
+P2G = {"ordered": 0, "atomic": 1}
+STAGES = {
+    "createWaterLevelSet": 1,
+    "transferVelocityToGrid": 2,
+    "applySemiLagrangianAdvection": 3,
+    "applyGravity": 4,
+    "createSolidLevelSet": 5,
+    "applyProjection": 6,
+    "updateVelocity": 7,
+    "updateParticleVelocities": 8,
+    "applyAdvection": 9,
+}
+ERRORS = {0: "OK", 1: "INVALID", 2: "ALLOC", 3: "CUDA", 4: "NOT_CONVERGED", 5: "NONFINITE", 6: "TIMEOUT"}
+
+
+class Config(C.Structure):
+    _fields_ = [("sizeX", C.c_int), ("sizeY", C.c_int), ("particlesPerCellSqrt", C.c_int),
+                ("dt", C.c_double), ("dx", C.c_double), ("rho", C.c_double),
+                ("gravityX", C.c_double), ("gravityY", C.c_double),
+                ("mode", C.c_int), ("picFlipAlpha", C.c_double),
+                ("initialValues", C.POINTER(C.c_uint8))]
+
+
+class Options(C.Structure):
+    _fields_ = [("precision", C.c_int), ("mic_tau", C.c_double), ("mic_sigma", C.c_double),
+                ("pcg_tol", C.c_double), ("pcg_max_iters", C.c_int), ("ir_inner_tol", C.c_double),
+                ("ir_max_outer", C.c_int), ("p2g_mode", C.c_int), ("extrapolate_band", C.c_int),
+                ("use_seed", C.c_int), ("seed", C.c_uint), ("device", C.c_int)]
+
+
+class State(C.Structure):
+    _fields_ = [("cell", C.POINTER(C.c_uint8)), ("phi", C.POINTER(C.c_double)),
+                ("p", C.POINTER(C.c_double)), ("u", C.POINTER(C.c_double)),
+                ("v", C.POINTER(C.c_double)), ("newU", C.POINTER(C.c_double)),
+                ("newV", C.POINTER(C.c_double)), ("particles", C.POINTER(C.c_double)),
+                ("particleVels", C.POINTER(C.c_double)), ("numParticles", C.c_size_t)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("waterVolume", C.c_double), ("totalEnergy", C.c_double),
+                ("particleTotalEnergy", C.c_double), ("origWaterVolume", C.c_double),
+                ("currentTime", C.c_double), ("frames", C.c_longlong), ("pcgIterations", C.c_int),
+                ("irOuterIterations", C.c_int), ("pcgRelResidual", C.c_double), ("lastStatus", C.c_int)]
+
+
+# Every entry point declared in include/fs2d.h, with its ctypes signature.
+SIGNATURES = {
+    "fs2d_default_options": (None, [C.POINTER(Options)]),
+    "fs2d_create": (C.c_int, [C.POINTER(Config), C.POINTER(Options), C.POINTER(C.c_void_p)]),
+    "fs2d_destroy": (C.c_int, [C.c_void_p]),
+    "fs2d_run_frame": (C.c_int, [C.c_void_p]),
+    "fs2d_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "fs2d_run_stage": (C.c_int, [C.c_void_p, C.c_int]),
+    "fs2d_upload_state": (C.c_int, [C.c_void_p, C.POINTER(State)]),
+    "fs2d_download_state": (C.c_int, [C.c_void_p, C.POINTER(State)]),
+    "fs2d_num_particles": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "fs2d_set_params": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_double, C.c_double]),
+    "fs2d_get_stats": (C.c_int, [C.c_void_p, C.POINTER(Stats)]),
+    "fs2d_get_history": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                   C.POINTER(C.c_double), C.c_size_t, C.POINTER(C.c_size_t)]),
+    "fs2d_avg_pressure": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "fs2d_avg_pressure_in_fluid": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "fs2d_max_velocity": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
+    "fs2d_save_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "fs2d_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fs2d_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
+    "fs2d_last_error": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+class FS2DError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"fs2d error {code} ({ERRORS.get(code, '?')}): {msg}")
+        self.code = code
+
+
+def load(path=LIB_PATH):
+    """Load libfs2d.so (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(path):
+            raise RuntimeError(f"CUDA library {path} is missing: run fluid-sim_gb300/build.py "
+                               "(there is no CPU fallback)")
+        lib = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(rc, allow=()):
+    if rc != 0 and rc not in allow:
+        raise FS2DError(rc, load().fs2d_last_error().decode())
+    return rc
+
+
+def default_options(**kw):
+    o = Options()
+    load().fs2d_default_options(C.byref(o))
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = PRECISION[v]
+        if k == "p2g_mode" and isinstance(v, str):
+            v = P2G[v]
+        setattr(o, k, v)
+    return o
+
+
+def make_config(scene):
+    cells = np.ascontiguousarray(scene["cells"], dtype=np.uint8)
+    cfg = Config(scene["sizeX"], scene["sizeY"], scene["ppcSqrt"], scene["dt"], scene["dx"], scene["rho"],
+                 scene["gravityX"], scene["gravityY"], scene["mode"], scene["picFlipAlpha"],
+                 cells.ctypes.data_as(C.POINTER(C.c_uint8)))
+    cfg._keep = cells
+    return cfg
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double)) if a is not None else None
+
+
+def state_view(arrs):
+    st = State()
+    for name in ("phi", "p", "u", "v", "newU", "newV", "particles", "particleVels"):
+        a = arrs.get(name)
+        setattr(st, name, _dptr(a))
+    c = arrs.get("cell")
+    st.cell = c.ctypes.data_as(C.POINTER(C.c_uint8)) if c is not None else None
+    parts = arrs.get("particles")
+    st.numParticles = 0 if parts is None else len(parts) // 2
+    return st
+
+
+class FluidSim2D:
+    """One simulation on the GPU.  ``scene`` is a dict as made by scenes.py
+    (the fields of FluidSim2DConfig plus the label array)."""
+
+    def __init__(self, scene, seed=None, **options):
+        lib = load()
+        self.nx, self.ny = scene["sizeX"], scene["sizeY"]
+        self.mode = scene["mode"]
+        self.cfg = make_config(scene)
+        if seed is not None:
+            options.setdefault("use_seed", 1)
+            options.setdefault("seed", seed)
+        self.opt = default_options(**options)
+        h = C.c_void_p()
+        _check(lib.fs2d_create(C.byref(self.cfg), C.byref(self.opt), C.byref(h)))
+        self.h = h
+
+    create = classmethod(lambda cls, scene, **kw: cls(scene, **kw))
+
+    # ---- frame and stages (FluidSim2D::runFrame / update / stage methods) ----
+    def runFrame(self):
+        return _check(load().fs2d_run_frame(self.h), allow=(4,))
+
+    update = runFrame
+
+    def step(self, n):
+        return _check(load().fs2d_step(self.h, n), allow=(4,))
+
+    def stage(self, name):
+        return _check(load().fs2d_run_stage(self.h, STAGES[name] if isinstance(name, str) else name), allow=(4,))
+
+    def __getattr__(self, name):
+        if name in STAGES:
+            return lambda: self.stage(name)
+        raise AttributeError(name)
+
+    # ---- state ----
+    def num_particles(self):
+        n = C.c_size_t()
+        _check(load().fs2d_num_particles(self.h, C.byref(n)))
+        return n.value
+
+    def get_state(self, fields=None):
+        n = self.num_particles()
+        nx, ny = self.nx, self.ny
+        shapes = {"cell": (nx * ny, np.uint8), "phi": (nx * ny, np.float64), "p": (nx * ny, np.float64),
+                  "u": ((nx + 1) * ny, np.float64), "v": (nx * (ny + 1), np.float64),
+                  "newU": ((nx + 1) * ny, np.float64), "newV": (nx * (ny + 1), np.float64),
+                  "particles": (2 * n, np.float64), "particleVels": (2 * n, np.float64)}
+        names = fields or list(shapes)
+        arrs = {k: np.zeros(shapes[k][0], shapes[k][1]) for k in names}
+        st = state_view(arrs)
+        st.numParticles = n
+        _check(load().fs2d_download_state(self.h, C.byref(st)))
+        return arrs
+
+    def set_state(self, arrs):
+        arrs = {k: np.ascontiguousarray(v) for k, v in arrs.items() if v is not None}
+        st = state_view(arrs)
+        _check(load().fs2d_upload_state(self.h, C.byref(st)))
+
+    def set_params(self, gravityX, gravityY, picFlipAlpha, dt):
+        _check(load().fs2d_set_params(self.h, gravityX, gravityY, picFlipAlpha, dt))
+
+    # ---- statistics and diagnostics ----
+    def stats(self):
+        s = Stats()
+        _check(load().fs2d_get_stats(self.h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def history(self):
+        n = C.c_size_t()
+        _check(load().fs2d_get_history(self.h, None, None, None, 0, C.byref(n)))
+        a, b, c = (np.zeros(n.value) for _ in range(3))
+        _check(load().fs2d_get_history(self.h, _dptr(a), _dptr(b), _dptr(c), n.value, C.byref(n)))
+        return a, b, c
+
+    def _diag(self, fn):
+        out = C.c_double()
+        _check(fn(self.h, C.byref(out)))
+        return out.value
+
+    def avgPressure(self):
+        return self._diag(load().fs2d_avg_pressure)
+
+    def avgPressureInFluid(self):
+        return self._diag(load().fs2d_avg_pressure_in_fluid)
+
+    def maxVelocity(self):
+        return self._diag(load().fs2d_max_velocity)
+
+    def saveStats(self, perf="perf.csv", conservation="conservation.csv"):
+        _check(load().fs2d_save_stats(self.h, perf.encode() if perf else None,
+                                      conservation.encode() if conservation else None))
+
+    def stage_times(self):
+        buf = (C.c_float * 16)()
+        n = C.c_int()
+        _check(load().fs2d_get_stage_times(self.h, buf, 16, C.byref(n)))
+        return list(buf[:n.value])
+
+    def launch_count(self):
+        n = C.c_ulonglong()
+        _check(load().fs2d_launch_count(self.h, C.byref(n)))
+        return n.value
+
+    def set_stream(self, stream_ptr):
+        _check(load().fs2d_set_stream(self.h, C.c_void_p(stream_ptr)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().fs2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

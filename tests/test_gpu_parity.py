@@ -1,0 +1,150 @@
+"""GPU parity: every stage of the FP64 device path against the reference.
+
+Each stage is fed the reference's own pre-stage state (golden vectors made
+by the unmodified reference, tests/golden/) and its output is compared with
+the reference's post-stage state:
+
+* bit-exact: particle seeding, level set + labels, P2G (ordered mode),
+  gravity, velocity update + extrapolation, G2P, particle advection;
+* semi-Lagrangian advection: bit-exact against the oracle's double-buffered
+  variant (the GPU's semantics) and within SL_INPLACE_RTOL of the
+  reference's in-place loop (which reads faces it already overwrote);
+* pressure: within PRESSURE_RTOL of max|p| (tree-ordered dot products and
+  norms instead of the reference's serial sums).
+"""
+import numpy as np
+import pytest
+
+import golden_util as G
+import oracle_py as O
+
+fs2d = pytest.importorskip("fs2d")
+pytestmark = pytest.mark.gpu
+
+PRESSURE_RTOL = 1e-8     # |p_gpu - p_ref|_inf / |p_ref|_inf after a 1e-12 solve
+SL_INPLACE_RTOL = 0.25   # double-buffered vs in-place advection, |du|_inf / |u|_inf
+
+
+def same(a, b):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def first_diff(a, b):
+    d = np.nonzero(a != b)[0]
+    return d[:5], a[d[:5]], b[d[:5]]
+
+
+def gpu_sim(g, **kw):
+    return fs2d.FluidSim2D(G.scene(g), seed=7, **kw)
+
+
+@pytest.mark.parametrize("name", G.NAMES)
+def test_create_matches_reference(name):
+    g = G.load(name)
+    sim = gpu_sim(g)
+    st = sim.get_state()
+    for f in ("cell", "particles", "particleVels"):
+        assert same(st[f], g["init_" + f]), f
+
+
+EXACT_FIELDS = {
+    "createWaterLevelSet": ("cell", "phi"),
+    "transferVelocityToGrid": ("u", "v"),
+    "applyGravity": ("u", "v"),
+    "createSolidLevelSet": ("cell", "phi", "u", "v"),
+    "updateVelocity": ("newU", "newV", "u", "v"),
+    "updateParticleVelocities": ("particleVels", "u", "v"),
+    "applyAdvection": ("particles",),
+}
+
+
+@pytest.mark.parametrize("name", G.NAMES)
+def test_stages_against_reference(name):
+    g = G.load(name)
+    sc = G.scene(g)
+    sim = gpu_sim(g)
+    for k, stage in enumerate(G.stage_order(sc)):
+        pre = G.pre_stage(g, k)
+        sim.set_state(pre)
+        sim.stage(stage)
+        st = sim.get_state()
+        post = G.snapshot(g, f"s{k}_post_")
+        if stage in EXACT_FIELDS:
+            for f in EXACT_FIELDS[stage]:
+                assert same(st[f], post[f]), (stage, f, first_diff(st[f], post[f]))
+        elif stage == "applyProjection":
+            scale = np.abs(post["p"]).max()
+            err = np.abs(st["p"] - post["p"]).max()
+            assert err <= PRESSURE_RTOL * scale, (stage, err, scale)
+        elif stage == "applySemiLagrangianAdvection":
+            orc = O.OracleSim(sc, seed=7, sl_inplace=0)
+            orc.set_state(pre)
+            orc.stage(stage)
+            ost = orc.get_state()
+            for f in ("u", "v"):
+                assert same(st[f], ost[f]), (stage, f, first_diff(st[f], ost[f]))
+                scale = np.abs(post[f]).max() + 1e-30
+                assert np.abs(st[f] - post[f]).max() <= SL_INPLACE_RTOL * scale, (stage, f)
+
+
+@pytest.mark.parametrize("name", ["pic_disk_32", "sl_dam_32"])
+def test_frames_against_oracle(name):
+    """Whole frames, double-buffered oracle: labels identical while the
+    pressure agrees to rounding; fields within tolerance over 10 frames."""
+    g = G.load(name)
+    sc = G.scene(g)
+    sim = gpu_sim(g)
+    orc = O.OracleSim(sc, seed=7, sl_inplace=0)
+    for frame in range(10):
+        sim.runFrame()
+        orc.frame()
+        a, b = sim.get_state(), orc.get_state()
+        assert same(a["cell"], b["cell"]), frame
+        for f in ("p", "u", "v", "particles", "particleVels"):
+            scale = np.abs(b[f]).max() + 1e-30
+            assert np.abs(a[f] - b[f]).max() <= 1e-6 * scale, (frame, f)
+    st = sim.stats()
+    ref = orc.stats()
+    assert abs(st["waterVolume"] - ref["waterVolume"]) <= 1e-12
+    assert abs(st["totalEnergy"] - ref["totalEnergy"]) <= 1e-9 * abs(ref["totalEnergy"])
+    assert abs(st["particleTotalEnergy"] - ref["particleTotalEnergy"]) <= 1e-9 * abs(ref["particleTotalEnergy"])
+    assert abs(sim.avgPressure() - ref["avgPressure"]) <= 1e-6 * abs(ref["avgPressure"]) + 1e-9
+    assert abs(sim.maxVelocity() - ref["maxVelocity"]) <= 1e-6 * abs(ref["maxVelocity"]) + 1e-12
+
+
+def test_p2g_atomic_mode_close():
+    g = G.load("pic_disk_32")
+    sc = G.scene(g)
+    sim = gpu_sim(g, p2g_mode="atomic")
+    k = G.stage_order(sc).index("transferVelocityToGrid")
+    sim.set_state(G.pre_stage(g, k))
+    sim.stage("transferVelocityToGrid")
+    st = sim.get_state()
+    post = G.snapshot(g, f"s{k}_post_")
+    for f in ("u", "v"):
+        scale = np.abs(post[f]).max() + 1e-30
+        assert np.abs(st[f] - post[f]).max() <= 1e-12 * scale, f
+
+
+def test_no_fluid_scene():
+    """No fluid at all: zero particles, empty level set, zero pressure."""
+    import scenes
+    sc = scenes.dam_break(24, mode=scenes.PICFLIP, extent=(0.0, 0.0))
+    sim = fs2d.FluidSim2D(sc, seed=1)
+    assert sim.num_particles() == 0
+    for _ in range(2):
+        sim.runFrame()
+    st = sim.get_state()
+    assert not (st["cell"] == 1).any()
+    assert np.all(st["p"] == 0)
+
+
+def test_invalid_border_rejected():
+    import scenes
+    sc = scenes.sl_dam_break(16)
+    sc["cells"] = sc["cells"].copy()
+    sc["cells"][0] = 0
+    with pytest.raises(fs2d.FS2DError) as e:
+        fs2d.FluidSim2D(sc, seed=1)
+    assert e.value.code == 1
