@@ -1,0 +1,335 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 FluidSim2D time step.
+
+Workload: the PIC/FLIP dam break (x < 0.4, y < 0.6) united with a disk of
+radius 0.1 at (0.7, 0.7), 1024 x 1024 cells, dx = 1/1024, 4 particles per
+fluid cell (~1.1 M particles), FLIP ratio 0.95 (picFlipAlpha = 0.05),
+dt = 1/960, pressure solve MIC(0)-PCG to a relative residual of 1e-6
+(infinity norm, the reference's convention), at most 200 iterations.
+Seeded synthetic input (the reference ships no datasets).
+
+A step is one FluidSim2D::runFrame (all eight stages).  Metric: grid-cell
+steps/s = NX * NY * steps / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py --impl reference ...   # the reference's CPU path (oracle port)
+
+One JSON line is printed by rank 0.  Multi-GPU runs are independent
+replicas (the step does not shard); value = total cell-steps / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "fluid-sim_gb300"))
+
+METRIC = "grid-cell steps/s at 1024^2 (PIC/FLIP step, MIC(0)-PCG to 1e-6 rel res)"
+UNIT = "grid-cell steps/s"
+SEED = 12345
+FLUSH_BYTES = 256 << 20          # > 129 MB L2
+DOMINANT = ("wave_MicForwardOp", "wave_MicBackwardOp")
+# algorithmic bytes per cell of one MIC(0) triangular solve: read r (or q),
+# two coefficients and precon, write q (or z): 5 values of b bytes
+MIC_VALUES_PER_CELL = 5
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(size):
+    import scenes
+    return scenes.pic_dam_break_disk(size)
+
+
+def config_dict(args, n_particles, extra=None):
+    d = {
+        "workload": f"PIC/FLIP dam break + disk r=0.1, {args.size}x{args.size}, dt=1/{int(round(960 * args.size / 1024))}, "
+                    f"4 ppc, FLIP 0.95, MIC(0)-PCG tol {args.tol:g} rel (inf-norm), <=200 iters",
+        "grid": [args.size, args.size],
+        "particles": n_particles,
+        "precision": args.precision,
+        "l2": "flushed between timed steps (256 MiB write)",
+        "parallelism": f"replicas x{args.gpus}",
+    }
+    if extra:
+        d.update(extra)
+    return d
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        self.gpu = gpu_index
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_baseline(args, budget_s, max_frames):
+    """The oracle port (OpenMP build, all host threads) on the same workload:
+    frames after one warm-up frame until `budget_s` seconds or `max_frames`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    sc = workload(args.size)
+    sim = oracle_py.OracleSim(sc, seed=SEED, omp=True, sl_inplace=0, pcg_tol=args.tol, pcg_max_iters=200)
+    sim.frame()
+    frames, t0 = 0, time.perf_counter()
+    while frames < max_frames:
+        sim.frame()
+        frames += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    value = args.size * args.size * frames / dt
+    info = sim.solver_info()
+    sim.close()
+    return {"value": value, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", threads)), "kind": "port",
+            "sample": f"{frames} frame(s) of the same {args.size}^2 workload after 1 warm-up frame, "
+                      f"{dt:.1f} s; oracle restatement (C, -O3 -fopenmp, the reference's race-free "
+                      f"OpenMP loops), PCG tol {args.tol:g} (last solve {info['iterations']} iterations)"}
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    budget = 150.0
+    t_start = time.perf_counter()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(threads))
+    sc = workload(args.size)
+    sim = oracle_py.OracleSim(sc, seed=SEED, omp=True, sl_inplace=0, pcg_tol=args.tol, pcg_max_iters=200)
+    n_particles = sim.num_particles()
+    warm = min(args.warmup, 2)
+    for _ in range(warm):
+        sim.frame()
+    frames, t0 = 0, time.perf_counter()
+    while frames < args.steps:
+        sim.frame()
+        frames += 1
+        if time.perf_counter() - t_start > budget:
+            break
+    dt = time.perf_counter() - t0
+    value = args.size * args.size * frames / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": frames, "warmup": warm, "ms_per_step": 1000 * dt / frames, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dam break + disk)",
+        "config": config_dict(args, n_particles, {"precision": "fp64 (reference CPU path)",
+                                                  "cpu_threads": int(os.environ["OMP_NUM_THREADS"])}),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
+                         "sample": f"{frames} of {args.steps} requested frames after {warm} warm-up frame(s), "
+                                   f"capped at {budget:.0f} s; oracle restatement of the reference step "
+                                   f"(OpenMP on its race-free loops); the reference checkout does not exist "
+                                   f"on this machine, so its own build cannot run here"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------- GPU arm
+def state_bytes(st):
+    return sum(a.nbytes for a in st.values())
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    rank, world, local = dist_env()
+    import numpy as np
+    import torch
+    import fs2d
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    sc = workload(args.size)
+    opts = dict(precision=args.precision, pcg_tol=args.tol, pcg_max_iters=200, device=local)
+    sim = fs2d.FluidSim2D(sc, seed=SEED, **opts)
+    stream = torch.cuda.Stream()
+    sim.set_stream(stream.cuda_stream)
+    n_particles = sim.num_particles()
+    for _ in range(args.warmup):
+        sim.runFrame()
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+
+    # ---- timed region: device-resident state, per-step CUDA events ----
+    sim.set_kernel_timing(",".join(DOMINANT))
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.3)
+    l0 = sim.launch_count()
+    iters = []
+    barrier()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.runFrame()
+        e1.record(stream)
+        evs.append((e0, e1))
+        iters.append(sim.stats()["pcgIterations"])
+    torch.cuda.synchronize()
+    barrier()
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    launches = sim.launch_count() - l0
+    ktimes = sim.kernel_times()
+    sim.set_kernel_timing("")
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    cells = args.size * args.size
+    value = cells * args.steps * world / (total_ms / 1000.0)
+
+    # ---- roofline of the dominant kernel ----
+    b = 8 if args.precision == "fp64" else 4
+    dom = max((k for k in ktimes if k in DOMINANT), key=lambda k: ktimes[k][1], default=None)
+    roofline = None
+    if dom is not None:
+        n_launch, ms = ktimes[dom]
+        alg_bytes = MIC_VALUES_PER_CELL * b * cells
+        achieved = alg_bytes / (ms / n_launch / 1000.0) / 1e9
+        peak, peak_src = 6800.0, "fallback"
+        try:
+            peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+            peak_src = "measured"
+        except Exception:
+            pass
+        traffic = None
+        tf = os.path.join(ROOT, "profiles", "traffic.txt")
+        if os.path.exists(tf):
+            for line in open(tf):
+                parts = line.split()
+                if len(parts) >= 3 and parts[0] == dom and parts[1] == args.precision:
+                    traffic = float(parts[2])
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                    "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                    "traffic": traffic, "launches": n_launch, "avg_launch_us": round(1000 * ms / n_launch, 2),
+                    "algorithmic_bytes_per_launch": alg_bytes,
+                    "share_of_step": round(sum(v[1] for k, v in ktimes.items() if k in DOMINANT) / total_ms, 3)}
+
+    # ---- e2e: through the C ABI with host buffers (upload + frame + download) ----
+    st = sim.get_state()
+    host_in = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in st.items()}
+    host_out = {k: torch.from_numpy(v.copy()).pin_memory().numpy() for k, v in st.items()}
+    h2d = state_bytes(host_in)
+    d2h = state_bytes(host_out)
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        sim.set_state(host_in)
+        sim.runFrame()
+        sim.get_state(out=host_out)
+        host_in, host_out = host_out, host_in
+    e2e_s = time.perf_counter() - t0
+    e2e_value = cells * args.e2e_steps * world / e2e_s
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32+f64",
+        "data": "synthetic (seeded dam break + disk, libc rand() particle jitter)",
+        "config": config_dict(args, n_particles, {"pcg_iterations_per_step": iters}),
+        "gpu_launches": launches,
+        "clocks": clk,
+        "roofline": roofline,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": args.e2e_steps, "path": "fs2d_upload_state + fs2d_run_frame + fs2d_download_state, "
+                                                 "full state, pinned host buffers"},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args, args.cpu_budget, 10)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    sim.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -34,6 +34,58 @@ int check_cuda(cudaError_t e, const char* what) {
     return e == cudaErrorMemoryAllocation ? FS2D_ERR_ALLOC : FS2D_ERR_CUDA;
 }
 
+long long ktimer_begin(Sim* s, const char* name) {
+    if (s->kt_patterns.empty()) return -1;
+    auto it = s->kt_match.find(name);
+    bool hit;
+    if (it == s->kt_match.end()) {
+        hit = false;
+        size_t a = 0;
+        const std::string& pat = s->kt_patterns;
+        while (a <= pat.size()) {
+            size_t b = pat.find(',', a);
+            if (b == std::string::npos) b = pat.size();
+            std::string tok = pat.substr(a, b - a);
+            if (!tok.empty() && strstr(name, tok.c_str())) hit = true;
+            a = b + 1;
+        }
+        s->kt_match[name] = hit;
+    } else {
+        hit = it->second;
+    }
+    if (!hit) return -1;
+    if (s->kt_used + 2 > s->kt_pool.size()) {
+        for (int k = 0; k < 64; k++) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return -1;
+            s->kt_pool.push_back(e);
+        }
+    }
+    size_t slot = s->kt_used;
+    s->kt_used += 2;
+    cudaEventRecord(s->kt_pool[slot], s->stream);
+    s->kt_pending.push_back(std::make_pair(name, slot));
+    return (long long)slot;
+}
+
+void ktimer_end(Sim* s, long long slot) {
+    if (slot < 0) return;
+    cudaEventRecord(s->kt_pool[(size_t)slot + 1], s->stream);
+}
+
+void ktimer_collect(Sim* s) {
+    for (auto& pr : s->kt_pending) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, s->kt_pool[pr.second], s->kt_pool[pr.second + 1]) == cudaSuccess) {
+            auto& acc = s->kt_acc[pr.first];
+            acc.first += 1;
+            acc.second += ms;
+        }
+    }
+    s->kt_pending.clear();
+    s->kt_used = 0;
+}
+
 unsigned long long wave_begin(Sim* s) {
     // progress values are base + (columns done); columns < 2^24
     s->wave_launch++;
@@ -167,6 +219,7 @@ void free_all(Sim* s) {
     if (s->err_host) cudaFreeHost(s->err_host);
     for (auto& e : s->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : s->kt_pool) cudaEventDestroy(e);
     if (s->own_stream) cudaStreamDestroy(s->own_stream);
     free(s->hist);
 }
@@ -198,6 +251,7 @@ int finish(Host* h) {
     FS2D_CUDA(cudaMemcpyAsync(s->err_host, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     FS2D_CUDA(cudaMemcpyAsync(s->stats_host, s->stats, sizeof(FrameStats), cudaMemcpyDeviceToHost, s->stream));
     FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    ktimer_collect(s);
     if (h->stats_pending) {
         if (s->hist_n == s->hist_cap) {
             size_t cap = s->hist_cap ? 2 * s->hist_cap : 64;
@@ -653,6 +707,37 @@ int fs2d_set_stream(fs2d_sim* p, void* stream) {
 int fs2d_launch_count(fs2d_sim* p, unsigned long long* out) {
     if (!p || !out) return FS2D_ERR_INVALID;
     *out = H(p)->sim.launches;
+    return FS2D_OK;
+}
+
+int fs2d_set_kernel_timing(fs2d_sim* p, const char* patterns) {
+    if (!p) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    ktimer_collect(s);
+    s->kt_patterns = patterns ? patterns : "";
+    s->kt_match.clear();
+    s->kt_acc.clear();
+    return FS2D_OK;
+}
+
+int fs2d_get_kernel_times(fs2d_sim* p, char* buf, size_t cap) {
+    if (!p || !buf || cap == 0) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    ktimer_collect(s);
+    std::string out;
+    for (auto& kv : s->kt_acc) {
+        char line[256];
+        snprintf(line, sizeof(line), "%s %lld %.6f\n", kv.first.c_str(), kv.second.first, kv.second.second);
+        out += line;
+    }
+    s->kt_acc.clear();
+    if (out.size() + 1 > cap) {
+        set_error("fs2d_get_kernel_times: buffer of %zu bytes too small", cap);
+        return FS2D_ERR_INVALID;
+    }
+    memcpy(buf, out.c_str(), out.size() + 1);
     return FS2D_OK;
 }
 

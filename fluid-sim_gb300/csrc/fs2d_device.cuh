@@ -236,9 +236,12 @@ int launch_wave(Sim* s, const Op& op, WaveGeom g, const int* skip) {
     unsigned long long base = wave_begin(s);
     void* args[] = {(void*)&op, (void*)&g, (void*)&s->progress, (void*)&base, (void*)&s->err, (void*)&skip};
     s->launches++;
-    return check_cuda(cudaLaunchCooperativeKernel((const void*)wave_kernel<Op>, dim3(nstrips), dim3(32), args, 0,
-                                                  s->stream),
-                      "wave_kernel");
+    long long kt = ktimer_begin(s, Op::kName);
+    int rc = check_cuda(cudaLaunchCooperativeKernel((const void*)wave_kernel<Op>, dim3(nstrips), dim3(32), args, 0,
+                                                    s->stream),
+                        Op::kName);
+    ktimer_end(s, kt);
+    return rc;
 }
 
 }  // namespace fs2d

@@ -9,6 +9,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
+#include <map>
+#include <string>
+#include <utility>
+#include <vector>
 
 #include "../../include/fs2d.h"
 
@@ -122,6 +126,14 @@ struct Sim {
     double last_rel_res = 0;
     int last_status = 0;
     int device = 0;
+
+    // opt-in per-kernel event timing (fs2d_set_kernel_timing)
+    std::string kt_patterns;
+    std::map<const char*, bool> kt_match;
+    std::vector<cudaEvent_t> kt_pool;
+    size_t kt_used = 0;
+    std::vector<std::pair<const char*, size_t>> kt_pending;  // name, index of the start event
+    std::map<std::string, std::pair<long long, double>> kt_acc;
 };
 
 // ---- error reporting (thread-local message, see fs2d_last_error) ----
@@ -133,11 +145,19 @@ int check_cuda(cudaError_t e, const char* what);
         if (_rc) return _rc;                              \
     } while (0)
 
-// Launch helper: counts the launch and reports launch errors.
+// Kernel timing hooks: returns the start-event index, or -1 when `name` is
+// not being timed.
+long long ktimer_begin(Sim* s, const char* name);
+void ktimer_end(Sim* s, long long slot);
+void ktimer_collect(Sim* s);  // after the stream drained
+
+// Launch helper: counts the launch, optionally times it, reports launch errors.
 #define FS2D_LAUNCH(sim, kernel, grid, block, smem, ...)                               \
     do {                                                                              \
         (sim)->launches++;                                                            \
+        long long _kt = ::fs2d::ktimer_begin((sim), #kernel);                         \
         kernel<<<(grid), (block), (smem), (sim)->stream>>>(__VA_ARGS__);             \
+        ::fs2d::ktimer_end((sim), _kt);                                              \
         int _rc = ::fs2d::check_cuda(cudaGetLastError(), #kernel);                   \
         if (_rc) return _rc;                                                          \
     } while (0)
@@ -155,6 +175,16 @@ int g2p(Sim* s);                          // updateParticleVelocities
 int advect_particles(Sim* s);             // applyAdvection
 int diagnostics(Sim* s);                  // avgPressure, avgPressureInFluid, maxVelocity
 int extrapolate(Sim* s, double* a, uint32_t* mask, int W, int H, double* b, uint32_t* mask_b, int Wb, int Hb);
+
+// Scratch of one extrapolation call over up to two face grids.
+struct ExtrapScratch {
+    int* dist[2];              // W*H ints per grid (distance transform)
+    int2* tile_range;          // per 32x32 tile [min, max] layer, grid 1 after grid 0
+    unsigned int* max_layer;   // 2 counters
+};
+size_t extrap_tiles(int W, int H);
+int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double* const a[2], uint32_t* const m[2],
+                     const int W[2], const int H[2], int band);
 int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n);
 
 // ---- wavefront plumbing ----

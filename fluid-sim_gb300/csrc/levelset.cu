@@ -101,6 +101,7 @@ __device__ __forceinline__ void cp_candidate(int e, const double2* __restrict__ 
 }
 
 struct ClosestPointOp {
+    static constexpr const char* kName = "wave_ClosestPointOp";
     typedef CPCarry Carry;
     double* phi;
     int* t;
@@ -186,6 +187,7 @@ __device__ __forceinline__ double eikonal(double own, double a, double b, double
 }
 
 struct EikonalOp {
+    static constexpr const char* kName = "wave_EikonalOp";
     typedef double Carry;
     double* phi;
     int NX;

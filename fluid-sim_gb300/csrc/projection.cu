@@ -92,6 +92,7 @@ __global__ void k_build(const uint8_t* __restrict__ cell, const double* __restri
 // The reference's SQUARE(x) is (x)*(x) without outer parentheses, so
 // a*b*SQUARE(p) associates as ((a*b)*p)*p.
 struct MicFactorOp {
+    static constexpr const char* kName = "wave_MicFactorOp";
     typedef double Carry;
     const uint8_t* cell;
     const double *Adiag, *Ax, *Ay;
@@ -134,6 +135,7 @@ __global__ void k_coef(const double* __restrict__ Ax, const double* __restrict__
 
 // applyPreconditioner, forward substitution (:400-409): q = L^-1 r.
 struct MicForwardOp {
+    static constexpr const char* kName = "wave_MicForwardOp";
     typedef double Carry;
     const uint8_t* cell;
     const double *r, *pc;
@@ -160,6 +162,7 @@ struct MicForwardOp {
 
 // applyPreconditioner, backward substitution (:410-419): z = L^-T q.
 struct MicBackwardOp {
+    static constexpr const char* kName = "wave_MicBackwardOp";
     typedef double Carry;
     const uint8_t* cell;
     const double *q, *pc;

@@ -481,47 +481,69 @@ int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n) {
     return 0;
 }
 
-// Array2D::extrapolate on one or two face grids (b may be null).
-int extrapolate(Sim* s, double* a, uint32_t* mask_a, int Wa, int Ha, double* b, uint32_t* mask_b, int Wb, int Hb) {
-    struct G {
-        double* a;
-        uint32_t* m;
-        int W, H;
-    } grids[2] = {{a, mask_a, Wa, Ha}, {b, mask_b, Wb, Hb}};
-    int ng = b ? 2 : 1;
-    int band_limit = s->opt.extrapolate_band > 0 ? s->opt.extrapolate_band : (1 << 28);
-    unsigned int* maxl = s->max_layer;
-    FS2D_CUDA(cudaMemsetAsync(maxl, 0, 2 * sizeof(unsigned int), s->stream));
-    int* dtmp = (int*)s->udiv;  // scratch: the P2G weight arrays are free here
+// Launch inside the extrapolation core: counted and timed when a handle is given.
+#define XLAUNCH(kernel, grid, block, ...)                                           \
+    do {                                                                          \
+        long long _kt = -1;                                                       \
+        if (s) {                                                                  \
+            s->launches++;                                                        \
+            _kt = ktimer_begin(s, #kernel);                                       \
+        }                                                                         \
+        kernel<<<(grid), (block), 0, stream>>>(__VA_ARGS__);                      \
+        if (s) ktimer_end(s, _kt);                                                \
+        int _rc = check_cuda(cudaGetLastError(), #kernel);                        \
+        if (_rc) return _rc;                                                      \
+    } while (0)
+
+
+size_t extrap_tiles(int W, int H) { return (size_t)((W + kTile - 1) / kTile) * ((H + kTile - 1) / kTile); }
+
+// Array2D::extrapolate on one or two face grids (grid 1 may be absent,
+// a[1] == nullptr).  Scratch: dist[g] holds W*H ints per grid, tile_range
+// extrap_tiles(W,H) entries per grid (grid 1's after grid 0's), max_layer 2
+// counters.  Synchronises `stream` once (to read the deepest layer).
+int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double* const a[2], uint32_t* const m[2],
+                     const int W[2], const int H[2], int band) {
+    int ng = a[1] ? 2 : 1;
+    int band_limit = band > 0 ? band : (1 << 28);
+    FS2D_CUDA(cudaMemsetAsync(x.max_layer, 0, 2 * sizeof(unsigned int), stream));
     int tiles_x[2], tiles_y[2];
     size_t tile_off[2] = {0, 0};
     for (int gi = 0; gi < ng; gi++) {
-        G& g = grids[gi];
-        tiles_x[gi] = (g.W + kTile - 1) / kTile;
-        tiles_y[gi] = (g.H + kTile - 1) / kTile;
-        if (gi == 1) tile_off[1] = (size_t)tiles_x[0] * tiles_y[0];
+        tiles_x[gi] = (W[gi] + kTile - 1) / kTile;
+        tiles_y[gi] = (H[gi] + kTile - 1) / kTile;
+        if (gi == 1) tile_off[1] = extrap_tiles(W[0], H[0]);
         size_t nt = (size_t)tiles_x[gi] * tiles_y[gi];
-        int2* tr = s->tile_range + tile_off[gi];
-        int* d = gi == 0 ? dtmp : (int*)s->vdiv;
-        FS2D_LAUNCH(s, k_tile_init, blocks_for(nt, 256), 256, 0, tr, nt);
-        FS2D_LAUNCH(s, k_dt_cols, blocks_for(g.W, 128), 128, 0, g.m, d, g.W, g.H);
-        FS2D_LAUNCH(s, k_dt_rows, g.H, 1024, 0, d, g.m, g.W, g.H, tr, tiles_x[gi]);
-        FS2D_LAUNCH(s, k_tile_max, blocks_for(nt, 256), 256, 0, tr, nt, maxl + gi);
+        int2* tr = x.tile_range + tile_off[gi];
+        XLAUNCH(k_tile_init, blocks_for(nt, 256), 256, tr, nt);
+        XLAUNCH(k_dt_cols, blocks_for(W[gi], 128), 128, m[gi], x.dist[gi], W[gi], H[gi]);
+        XLAUNCH(k_dt_rows, H[gi], 1024, x.dist[gi], m[gi], W[gi], H[gi], tr, tiles_x[gi]);
+        XLAUNCH(k_tile_max, blocks_for(nt, 256), 256, tr, nt, x.max_layer + gi);
     }
     unsigned int hmax[2] = {0, 0};
-    FS2D_CUDA(cudaMemcpyAsync(hmax, maxl, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, s->stream));
-    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    FS2D_CUDA(cudaMemcpyAsync(hmax, x.max_layer, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
+    FS2D_CUDA(cudaStreamSynchronize(stream));
     for (int gi = 0; gi < ng; gi++) {
-        G& g = grids[gi];
         int maxL = (int)std::min<unsigned int>(hmax[gi], (unsigned int)band_limit);
         for (int lo = 1; lo <= maxL; lo += kBand) {
             int hi = std::min(lo + kBand - 1, maxL);
             dim3 grid(tiles_x[gi], tiles_y[gi]);
-            FS2D_LAUNCH(s, k_extrap_band, grid, 256, 0, g.a, g.m, g.W, g.H, s->tile_range + tile_off[gi], tiles_x[gi],
-                        lo, hi);
+            XLAUNCH(k_extrap_band, grid, 256, a[gi], m[gi], W[gi], H[gi], x.tile_range + tile_off[gi], tiles_x[gi],
+                    lo, hi);
         }
     }
     return 0;
+}
+#undef XLAUNCH
+
+// Array2D::extrapolate on one or two face grids of the handle (b may be null).
+int extrapolate(Sim* s, double* a, uint32_t* mask_a, int Wa, int Ha, double* b, uint32_t* mask_b, int Wb, int Hb) {
+    // scratch: the P2G weight arrays are free whenever extrapolation runs
+    ExtrapScratch x{{(int*)s->udiv, (int*)s->vdiv}, s->tile_range, s->max_layer};
+    double* const aa[2] = {a, b};
+    uint32_t* const mm[2] = {mask_a, mask_b};
+    const int W[2] = {Wa, Wb}, H[2] = {Ha, Hb};
+    return extrapolate_core(s, s->stream, x, aa, mm, W, H, s->opt.extrapolate_band);
 }
 
 int p2g(Sim* s) {
@@ -570,3 +592,30 @@ int g2p(Sim* s) {
 }
 
 }  // namespace fs2d
+
+using namespace fs2d;
+
+// Array2D::extrapolate (include/Array2D.h:552-591) on caller-owned device
+// buffers; scratch is allocated with cudaMalloc for the duration of the call.
+extern "C" int fs2d_extrapolate(double* values, uint32_t* mask, int width, int height, int band, void* stream) {
+    if (!values || !mask || width < 1 || height < 1) {
+        set_error("fs2d_extrapolate: invalid arguments");
+        return FS2D_ERR_INVALID;
+    }
+    const size_t n = (size_t)width * height;
+    const size_t dist_bytes = (n * sizeof(int) + 255) / 256 * 256;
+    const size_t tile_bytes = (extrap_tiles(width, height) * sizeof(int2) + 255) / 256 * 256;
+    char* buf = nullptr;
+    int rc = check_cuda(cudaMalloc((void**)&buf, dist_bytes + tile_bytes + 256), "cudaMalloc");
+    if (rc) return rc;
+    ExtrapScratch x{{(int*)buf, nullptr}, (int2*)(buf + dist_bytes), (unsigned int*)(buf + dist_bytes + tile_bytes)};
+    double* const aa[2] = {values, nullptr};
+    uint32_t* const mm[2] = {mask, nullptr};
+    const int W[2] = {width, 0}, H[2] = {height, 0};
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = extrapolate_core(nullptr, st, x, aa, mm, W, H, band);
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(buf);
+    if (rc) return rc;
+    return check_cuda(e, "fs2d_extrapolate");
+}

@@ -90,6 +90,9 @@ SIGNATURES = {
     "fs2d_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fs2d_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
     "fs2d_last_error": (C.c_char_p, []),
+    "fs2d_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "fs2d_extrapolate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "fs2d_get_kernel_times": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
 }
 
 _lib = None
@@ -202,15 +205,20 @@ class FluidSim2D:
         _check(load().fs2d_num_particles(self.h, C.byref(n)))
         return n.value
 
-    def get_state(self, fields=None):
+    def get_state(self, fields=None, out=None):
+        """Download the state; `out` may supply the destination arrays
+        (e.g. pinned host memory), which are filled in place."""
         n = self.num_particles()
         nx, ny = self.nx, self.ny
         shapes = {"cell": (nx * ny, np.uint8), "phi": (nx * ny, np.float64), "p": (nx * ny, np.float64),
                   "u": ((nx + 1) * ny, np.float64), "v": (nx * (ny + 1), np.float64),
                   "newU": ((nx + 1) * ny, np.float64), "newV": (nx * (ny + 1), np.float64),
                   "particles": (2 * n, np.float64), "particleVels": (2 * n, np.float64)}
-        names = fields or list(shapes)
-        arrs = {k: np.zeros(shapes[k][0], shapes[k][1]) for k in names}
+        names = fields or (list(out) if out is not None else list(shapes))
+        arrs = out if out is not None else {k: np.zeros(shapes[k][0], shapes[k][1]) for k in names}
+        for k in names:
+            if arrs[k].shape != (shapes[k][0],) or arrs[k].dtype != shapes[k][1]:
+                raise ValueError(f"get_state: buffer {k} has the wrong shape or dtype")
         st = state_view(arrs)
         st.numParticles = n
         _check(load().fs2d_download_state(self.h, C.byref(st)))
@@ -265,6 +273,21 @@ class FluidSim2D:
         n = C.c_ulonglong()
         _check(load().fs2d_launch_count(self.h, C.byref(n)))
         return n.value
+
+    def set_kernel_timing(self, patterns):
+        """Time (CUDA events) every launch whose kernel name contains one of
+        the comma-separated patterns; "" turns timing off."""
+        _check(load().fs2d_set_kernel_timing(self.h, patterns.encode() if patterns else None))
+
+    def kernel_times(self):
+        """{kernel name: (launches, total ms)} since the previous call."""
+        buf = C.create_string_buffer(1 << 16)
+        _check(load().fs2d_get_kernel_times(self.h, buf, len(buf)))
+        out = {}
+        for line in buf.value.decode().splitlines():
+            name, n, ms = line.split()
+            out[name] = (int(n), float(ms))
+        return out
 
     def set_stream(self, stream_ptr):
         _check(load().fs2d_set_stream(self.h, C.c_void_p(stream_ptr)))

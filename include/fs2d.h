@@ -173,6 +173,17 @@ int fs2d_step(fs2d_sim* sim, int nframes);
  * include/FluidSim2D.h:124-140) on the current device state. */
 int fs2d_run_stage(fs2d_sim* sim, int stage);
 
+/* Array2D::extrapolate (include/Array2D.h:552-591) on caller-owned DEVICE
+ * buffers: `values` holds width*height doubles, `mask` width*height uint32
+ * (0 = known, nonzero = unknown).  Every unknown face at breadth-first layer
+ * L (its 4-connected grid distance to the nearest known face) becomes the
+ * mean of its neighbours of lower layer, as in the reference; `mask` is left
+ * holding the layers, as the reference leaves its intMask.  band > 0 stops
+ * after that many layers.  Runs on `stream` (NULL: the default stream) and
+ * returns after the work completed.  Allocates 4 bytes of scratch per face
+ * with cudaMalloc for the duration of the call. */
+int fs2d_extrapolate(double* values, uint32_t* mask, int width, int height, int band, void* stream);
+
 /* Host <-> device state transfer (the reference's public fields). */
 int fs2d_upload_state(fs2d_sim* sim, const fs2d_state* st);
 int fs2d_download_state(fs2d_sim* sim, fs2d_state* st);
@@ -211,6 +222,16 @@ int fs2d_set_stream(fs2d_sim* sim, void* stream);
 
 /* Number of kernels this handle has launched so far. */
 int fs2d_launch_count(fs2d_sim* sim, unsigned long long* out);
+
+/* Per-kernel device timing, the kernel-level analogue of the reference's
+ * PerformanceCounter stage timers (src/PerformanceCounter.cpp:16-50): CUDA
+ * events are recorded on the handle's stream around every launch whose
+ * kernel name contains one of the comma-separated `patterns` ("" or NULL
+ * turns timing off).  fs2d_get_kernel_times writes one line per timed
+ * kernel, "name launches total_ms\n", covering the launches since the
+ * previous call, and resets the counts. */
+int fs2d_set_kernel_timing(fs2d_sim* sim, const char* patterns);
+int fs2d_get_kernel_times(fs2d_sim* sim, char* buf, size_t cap);
 
 /* Message of the last error on the calling thread ("" if none). */
 const char* fs2d_last_error(void);
