@@ -25,6 +25,7 @@
 // cells), so one launch per band replaces one launch per layer.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <mutex>
 #include "fs2d_device.cuh"
 
 namespace fs2d {
@@ -618,4 +619,82 @@ extern "C" int fs2d_extrapolate(double* values, uint32_t* mask, int width, int h
     cudaFree(buf);
     if (rc) return rc;
     return check_cuda(e, "fs2d_extrapolate");
+}
+
+// ---------------------------------------------------------------------------
+// fs2d_extrapolate_noalloc: the same extrapolation for callers that cannot
+// allocate device memory (for example code running under a memory pool or
+// allocator it does not own, or a plugin that may only use the buffers it is
+// handed).  Its scratch lives in this file-scope device array, sized for at
+// most kNoAllocMaxFaces faces with each side at most kNoAllocMaxSide; every
+// GPU that loads the library holds these bytes until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoAllocMaxFaces = (size_t)1 << 21;  // 2,097,152 faces
+constexpr int kNoAllocMaxSide = 8192;
+constexpr size_t kNoAllocMaxTiles = kNoAllocMaxFaces / 1024 + 2 * (kNoAllocMaxSide / 32) + 1;
+constexpr size_t kNoAllocDistBytes = kNoAllocMaxFaces * sizeof(int);
+constexpr size_t kNoAllocTileBytes = (kNoAllocMaxTiles * sizeof(int2) + 255) / 256 * 256;
+constexpr size_t kNoAllocBytes = kNoAllocDistBytes + kNoAllocTileBytes + 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+// Device address of g_noalloc_scratch, looked up once per device (with that
+// device current) on the first call made on it.
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+int noalloc_scratch(void** out) {
+    int dev = 0;
+    int rc = check_cuda(cudaGetDevice(&dev), "cudaGetDevice");
+    if (rc) return rc;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) {
+        set_error("fs2d_extrapolate_noalloc: device %d out of range", dev);
+        return FS2D_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        rc = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), "cudaGetSymbolAddress");
+        if (rc) return rc;
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return 0;
+}
+
+}  // namespace
+
+// Same contract as fs2d_extrapolate, without allocating: see include/fs2d.h.
+extern "C" int fs2d_extrapolate_noalloc(double* values, uint32_t* mask, int width, int height, int band,
+                                        void* stream) {
+    if (!values || !mask || width < 1 || height < 1) {
+        set_error("fs2d_extrapolate_noalloc: invalid arguments");
+        return FS2D_ERR_INVALID;
+    }
+    if (width > kNoAllocMaxSide || height > kNoAllocMaxSide || (size_t)width * height > kNoAllocMaxFaces) {
+        set_error("fs2d_extrapolate_noalloc: %d x %d faces exceed the static scratch (at most %zu faces, "
+                  "each side at most %d); use fs2d_extrapolate",
+                  width, height, kNoAllocMaxFaces, kNoAllocMaxSide);
+        return FS2D_ERR_INVALID;
+    }
+    void* base = nullptr;
+    int rc = noalloc_scratch(&base);
+    if (rc) return rc;
+    char* buf = (char*)base;
+    // every part of the scratch is (re)initialised by the kernels of this call:
+    // the distance map and tile ranges are written before they are read and
+    // the layer counters are cleared by extrapolate_core
+    ExtrapScratch x{{(int*)buf, nullptr}, (int2*)(buf + kNoAllocDistBytes),
+                    (unsigned int*)(buf + kNoAllocDistBytes + kNoAllocTileBytes)};
+    double* const aa[2] = {values, nullptr};
+    uint32_t* const mm[2] = {mask, nullptr};
+    const int W[2] = {width, 0}, H[2] = {height, 0};
+    cudaStream_t st = (cudaStream_t)stream;
+    rc = extrapolate_core(nullptr, st, x, aa, mm, W, H, band);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (rc) return rc;
+    return check_cuda(e, "fs2d_extrapolate_noalloc");
 }

@@ -92,6 +92,7 @@ SIGNATURES = {
     "fs2d_last_error": (C.c_char_p, []),
     "fs2d_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_char_p]),
     "fs2d_extrapolate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
+    "fs2d_extrapolate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "fs2d_get_kernel_times": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
 }
 

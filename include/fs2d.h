@@ -184,6 +184,24 @@ int fs2d_run_stage(fs2d_sim* sim, int stage);
  * with cudaMalloc for the duration of the call. */
 int fs2d_extrapolate(double* values, uint32_t* mask, int width, int height, int band, void* stream);
 
+/* fs2d_extrapolate for callers that cannot allocate device memory — code
+ * that must run on the buffers it is handed, such as a plugin living inside
+ * a host application's own memory pool.  No reference counterpart: the
+ * reference allocates its BFS queue on the host per call.  Same arguments
+ * and results as fs2d_extrapolate, but no cudaMalloc, cudaFree or other
+ * allocating call: the scratch is one static device array of 8 MiB + 24 KiB
+ * (FS2D_NOALLOC_MAX_FACES faces, each side at most FS2D_NOALLOC_MAX_SIDE),
+ * which every GPU that loads the library holds until the process exits.
+ * Larger grids are rejected with FS2D_ERR_INVALID.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.
+ * Every call shares the one array, so calls that overlap on the GPU (other
+ * streams, other host threads) race; each call initialises what it reads
+ * and returns after its work completed. */
+#define FS2D_NOALLOC_MAX_FACES 2097152
+#define FS2D_NOALLOC_MAX_SIDE 8192
+int fs2d_extrapolate_noalloc(double* values, uint32_t* mask, int width, int height, int band, void* stream);
+
 /* Host <-> device state transfer (the reference's public fields). */
 int fs2d_upload_state(fs2d_sim* sim, const fs2d_state* st);
 int fs2d_download_state(fs2d_sim* sim, fs2d_state* st);
