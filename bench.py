@@ -35,7 +35,7 @@ METRIC = "grid-cell steps/s at 1024^2 (PIC/FLIP step, MIC(0)-PCG to 1e-6 rel res
 UNIT = "grid-cell steps/s"
 SEED = 12345
 FLUSH_BYTES = 256 << 20          # > 129 MB L2
-DOMINANT = ("wave_MicForwardOp", "wave_MicBackwardOp")
+DOMINANT = ("wave2_MicForward64", "wave2_MicBackward64", "wave2_MicForward32", "wave2_MicBackward32")
 # algorithmic bytes per cell of one MIC(0) triangular solve: read r (or q),
 # two coefficients and precon, write q (or z): 5 values of b bytes
 MIC_VALUES_PER_CELL = 5

@@ -30,6 +30,7 @@ UNITS = {
     "transfer.cu": ["--fmad=false"],
     "advect.cu": ["--fmad=false"],
     "projection.cu": ["--fmad=false"],
+    "projection_mixed.cu": [],
 }
 
 

@@ -183,8 +183,10 @@ int alloc_all(Sim* s) {
     A(Ay, N);
     A(rhs, N);
     A(precon, N);
-    A(coef_f, N);
-    A(coef_b, N);
+    A(cfx, N);
+    A(cfy, N);
+    A(cbx, N);
+    A(cby, N);
     A(r, N);
     A(z, N);
     A(q, N);
@@ -196,10 +198,33 @@ int alloc_all(Sim* s) {
     A(progress, (size_t)s->progress_cap);
     A(stats, 1);
     A(err, 1);
+    if (s->opt.precision == FS2D_PRECISION_MIXED) {
+        Mixed32& m = s->m32;
+        A(m32.a0, N);
+        A(m32.ax, N);
+        A(m32.ay, N);
+        A(m32.pc, N);
+        A(m32.fa, N);
+        A(m32.fb, N);
+        A(m32.fc, N);
+        A(m32.fd, N);
+        A(m32.r, N);
+        A(m32.rp, N);
+        A(m32.q, N);
+        A(m32.z, N);
+        A(m32.w, N);
+        A(m32.s0, N);
+        A(m32.s1, N);
+        A(m32.e, N);
+        A(pcg32, 1);
+        (void)m;
+    }
 #undef A
     if ((rc = check_cuda(cudaMallocHost((void**)&s->pcg_host, sizeof(PcgScalars)), "cudaMallocHost"))) return rc;
     if ((rc = check_cuda(cudaMallocHost((void**)&s->stats_host, sizeof(FrameStats)), "cudaMallocHost"))) return rc;
     if ((rc = check_cuda(cudaMallocHost((void**)&s->err_host, sizeof(int)), "cudaMallocHost"))) return rc;
+    if ((rc = check_cuda(cudaMallocHost((void**)&s->pcg32_host, sizeof(PcgScalars)), "cudaMallocHost"))) return rc;
+    memset(s->pcg32_host, 0, sizeof(PcgScalars));
     memset(s->pcg_host, 0, sizeof(PcgScalars));
     memset(s->stats_host, 0, sizeof(FrameStats));
     *s->err_host = 0;
@@ -210,11 +235,14 @@ void free_all(Sim* s) {
     void* ptrs[] = {s->cell, s->phi, s->p, s->u, s->v, s->nu, s->nv, s->pos, s->vel, s->t, s->seed_key,
                     s->phi_tmp, s->surface, s->u0, s->v0, s->udiv, s->vdiv, s->mask_u, s->mask_v, s->cnt_u,
                     s->cnt_v, s->fill_u, s->fill_v, s->ent_u, s->ent_v, s->scan_tmp, s->tile_range, s->max_layer,
-                    s->Adiag, s->Ax, s->Ay, s->rhs, s->precon, s->coef_f, s->coef_b, s->r, s->z, s->q, s->w, s->s0,
-                    s->s1, s->partial, s->pcg, s->progress, s->stats, s->err};
+                    s->Adiag, s->Ax, s->Ay, s->rhs, s->precon, s->cfx, s->cfy, s->cbx, s->cby, s->r, s->z, s->q, s->w, s->s0,
+                    s->s1, s->partial, s->pcg, s->progress, s->stats, s->err, s->m32.a0, s->m32.ax, s->m32.ay,
+                    s->m32.pc, s->m32.fa, s->m32.fb, s->m32.fc, s->m32.fd, s->m32.r, s->m32.rp, s->m32.q,
+                    s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->pcg_host) cudaFreeHost(s->pcg_host);
+    if (s->pcg32_host) cudaFreeHost(s->pcg32_host);
     if (s->stats_host) cudaFreeHost(s->stats_host);
     if (s->err_host) cudaFreeHost(s->err_host);
     for (auto& e : s->ev)
@@ -234,7 +262,8 @@ int run_stage_impl(Sim* s, int stage, int* status) {
         case FS2D_STAGE_APPLY_SEMI_LAGRANGIAN_ADVECTION: return sl_advect(s);
         case FS2D_STAGE_APPLY_GRAVITY: return apply_gravity(s);
         case FS2D_STAGE_CREATE_SOLID_LEVEL_SET: return 0;  // empty in the reference (:734-736)
-        case FS2D_STAGE_APPLY_PROJECTION: return projection(s, status);
+        case FS2D_STAGE_APPLY_PROJECTION:
+            return s->opt.precision == FS2D_PRECISION_MIXED ? projection_mixed(s, status) : projection(s, status);
         case FS2D_STAGE_UPDATE_VELOCITY: return update_velocity(s);
         case FS2D_STAGE_UPDATE_PARTICLE_VELOCITIES: return g2p(s);
         case FS2D_STAGE_APPLY_ADVECTION: return advect_particles(s);
@@ -337,8 +366,12 @@ int fs2d_create(const fs2d_config* cfg, const fs2d_options* opt, fs2d_sim** out)
         }
     fs2d_options o;
     if (opt) o = *opt; else fs2d_default_options(&o);
-    if (o.precision != FS2D_PRECISION_FP64) {
-        set_error("fs2d_create: precision mode %d is not available in this build", o.precision);
+    if (o.precision != FS2D_PRECISION_FP64 && o.precision != FS2D_PRECISION_MIXED) {
+        set_error("fs2d_create: unknown precision mode %d", o.precision);
+        return FS2D_ERR_INVALID;
+    }
+    if (!(o.pcg_tol >= 0) || o.pcg_max_iters < 0 || !(o.ir_inner_tol > 0) || o.ir_max_outer < 1) {
+        set_error("fs2d_create: invalid solver options");
         return FS2D_ERR_INVALID;
     }
     int ndev = 0;

@@ -51,6 +51,14 @@ struct FrameStats {
     unsigned int pad;
 };
 
+// FP32 arrays of the mixed-precision inner solver (projection_mixed.cu).
+struct Mixed32 {
+    float *a0 = nullptr, *ax = nullptr, *ay = nullptr;             // matrix
+    float *pc = nullptr, *fa = nullptr, *fb = nullptr, *fc = nullptr, *fd = nullptr;  // MIC(0), folded
+    float *r = nullptr, *rp = nullptr, *q = nullptr, *z = nullptr, *w = nullptr;
+    float *s0 = nullptr, *s1 = nullptr, *e = nullptr;
+};
+
 struct Sim {
     // configuration
     int NX = 0, NY = 0, ppc_sqrt = 0, mode = 0;
@@ -88,13 +96,18 @@ struct Sim {
 
     // projection scratch
     double *Adiag = nullptr, *Ax = nullptr, *Ay = nullptr, *rhs = nullptr, *precon = nullptr;
-    double2 *coef_f = nullptr, *coef_b = nullptr;    // MIC(0) forward / backward coefficients
+    // MIC(0) triangular-solve coefficients: forward Ax(i-1,j)*pc(i-1,j), Ay(i,j-1)*pc(i,j-1);
+    // backward Ax(i,j)*pc(i,j), Ay(i,j)*pc(i,j)
+    double *cfx = nullptr, *cfy = nullptr, *cbx = nullptr, *cby = nullptr;
     double *r = nullptr, *z = nullptr, *q = nullptr, *w = nullptr;
     double *s0 = nullptr, *s1 = nullptr;             // ping-pong search direction
     double* partial = nullptr;                       // per-block reduction partials
     size_t partial_cap = 0;
     PcgScalars* pcg = nullptr;
     PcgScalars* pcg_host = nullptr;                  // pinned mirror for polling
+    Mixed32 m32;                                     // MIXED precision only
+    PcgScalars* pcg32 = nullptr;                     // inner FP32 solve scalars
+    PcgScalars* pcg32_host = nullptr;
 
     // wavefront progress flags (monotonic, 64-bit, never reset)
     unsigned long long* progress = nullptr;
@@ -169,7 +182,9 @@ int levelset_create(Sim* s);              // createWaterLevelSet
 int p2g(Sim* s);                          // transferVelocityToGrid
 int sl_advect(Sim* s);                    // applySemiLagrangianAdvection
 int apply_gravity(Sim* s);                // applyGravity
-int projection(Sim* s, int* status);      // applyProjection
+int projection(Sim* s, int* status);      // applyProjection, FP64
+int projection_mixed(Sim* s, int* status);  // applyProjection, FP32 PCG in FP64 refinement
+int projection_build(Sim* s);             // FP64 matrix, rhs, p = 0, r = rhs, ||rhs||
 int update_velocity(Sim* s);              // updateVelocity
 int g2p(Sim* s);                          // updateParticleVelocities
 int advect_particles(Sim* s);             // applyAdvection

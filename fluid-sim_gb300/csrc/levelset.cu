@@ -21,6 +21,7 @@
 #include <math.h>
 #include <limits.h>
 #include "fs2d_device.cuh"
+#include "wave2.cuh"
 
 namespace fs2d {
 namespace {
@@ -109,6 +110,12 @@ struct ClosestPointOp {
     int NX, NY, sx, sy;
     double dx, dr;
 
+    __device__ void prefetch(int i, int j) const {
+        size_t c = (size_t)j * NX + i;
+        prefetch_l1(phi + c);
+        prefetch_l1(t + c);
+        if (j + sy >= 0 && j + sy < NY) prefetch_l1(t + (size_t)(j + sy) * NX + i);
+    }
     __device__ Carry fetch(int i, int j, bool l2) const {
         if (i < 0 || i >= NX || j < 0 || j >= NY) return Carry{-1};
         const int* a = t + (size_t)j * NX + i;
@@ -186,24 +193,19 @@ __device__ __forceinline__ double eikonal(double own, double a, double b, double
     return (d < -own) ? -d : own;
 }
 
-struct EikonalOp {
-    static constexpr const char* kName = "wave_EikonalOp";
-    typedef double Carry;
-    double* phi;
-    int NX;
+struct Eikonal64 {
+    static constexpr const char* kName = "wave2_Eikonal64";
+    typedef double T;
+    static constexpr int NA = 1;
+    const double* in[1];  // phi before the sweep (the output array itself)
+    double* out;
+    int pitch;
     double dx;
-    __device__ Carry fetch(int i, int j, bool l2) const {
-        const double* a = phi + (size_t)j * NX + i;
-        return l2 ? __ldcg(a) : *a;
+    __device__ double stored(const double*, double r) const { return r; }
+    __device__ double border(int i, int j) const { return out[(size_t)j * pitch + i]; }
+    __device__ double compute(const double* v, double left, double below, int, int) const {
+        return eikonal(v[0], left, below, dx);
     }
-    __device__ Carry update(int i, int j, Carry left, Carry below) const {
-        size_t c = (size_t)j * NX + i;
-        double own = phi[c];
-        double nv = eikonal(own, left, below, dx);
-        if (nv != own) phi[c] = nv;
-        return nv;
-    }
-    static __device__ Carry shfl_up(Carry v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 };
 
 __global__ void k_eik_check(const double* __restrict__ phi, int NX, int i_lo, int i_hi, int j_lo, int j_hi, int sx,
@@ -345,9 +347,9 @@ int levelset_create(Sim* s) {
             FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));
             dim3 gc(blocks_for(i_hi - i_lo + 1, 128), j_hi - j_lo + 1);
             FS2D_LAUNCH(s, k_eik_check, gc, 128, 0, s->phi_tmp, NX, i_lo, i_hi, j_lo, j_hi, sx, sy, s->dx, noop);
-            EikonalOp op{s->phi_tmp, NX, s->dx};
+            Eikonal64 op{{s->phi_tmp}, s->phi_tmp, NX, s->dx};
             WaveGeom g{sx, sy, i_lo, i_hi, j_lo, j_hi};
-            int rc = launch_wave(s, op, g, noop);
+            int rc = launch_wave2<Eikonal64, 2, 8>(s, op, g, noop);
             if (rc) return rc;
         }
     }

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include "fs2d_device.cuh"
+#include "wave2.cuh"
 
 namespace fs2d {
 namespace {
@@ -60,7 +61,9 @@ __global__ void k_build(const uint8_t* __restrict__ cell, const double* __restri
             if (d == kSolid) b -= scale * (v0 - 0);
             if (up == kSolid) b += scale * (v1 - 0);
         }
-        Adiag[c] = ad;
+        // non-fluid cells carry -0.0: a marker the MIC(0) factor reads from its
+        // staged operands (fluid cells hold the reference's value, >= +0.0)
+        Adiag[c] = (cell[c] == kFluid) ? ad : -0.0;
         Ax[c] = ax;
         Ay[c] = ay;
         rhs[c] = b;
@@ -88,103 +91,78 @@ __global__ void k_build(const uint8_t* __restrict__ cell, const double* __restri
     }
 }
 
-// MIC(0) factor (:364-387): precon(i,j) from precon(i-1,j) and precon(i,j-1).
+// MIC(0) factor (:364-387): precon(i,j) from precon(i-1,j) and precon(i,j-1),
+// staged operands Adiag(i,j), Ax(i-1,j), Ay(i-1,j), Ay(i,j-1), Ax(i,j-1).
 // The reference's SQUARE(x) is (x)*(x) without outer parentheses, so
 // a*b*SQUARE(p) associates as ((a*b)*p)*p.
-struct MicFactorOp {
-    static constexpr const char* kName = "wave_MicFactorOp";
-    typedef double Carry;
-    const uint8_t* cell;
-    const double *Adiag, *Ax, *Ay;
-    double* precon;
-    int NX;
+struct MicFactor64 {
+    static constexpr const char* kName = "wave2_MicFactor64";
+    typedef double T;
+    static constexpr int NA = 5;
+    const double* in[5];
+    double* out;
+    int pitch;
     double tau, sigma;
-    __device__ Carry fetch(int i, int j, bool l2) const {
-        const double* a = precon + (size_t)j * NX + i;
-        return l2 ? __ldcg(a) : *a;
+    __device__ double stored(const double*, double r) const { return r; }
+    __device__ double border(int i, int j) const { return out[(size_t)j * pitch + i]; }
+    __device__ double compute(const double* v, double pl, double pd, int, int) const {
+        const double ad = v[0];
+        if (signbit(ad)) return 0.0;  // not a fluid cell
+        const double axl = v[1], ayl = v[2], ayd = v[3], axd = v[4];
+        double e = ad - (axl * pl) * (axl * pl) - (ayd * pd) * (ayd * pd) -
+                   tau * (axl * ayl * pl * pl + ayd * axd * pd * pd);
+        if (e < sigma * ad) e = ad;
+        return 1 / sqrt(e);
     }
-    __device__ Carry update(int i, int j, Carry pl, Carry pd) const {
-        size_t c = (size_t)j * NX + i;
-        double pc = 0.0;
-        if (cell[c] == kFluid) {
-            double axl = Ax[c - 1], ayl = Ay[c - 1], ayd = Ay[c - NX], axd = Ax[c - NX], ad = Adiag[c];
-            double e = ad - (axl * pl) * (axl * pl) - (ayd * pd) * (ayd * pd) -
-                       tau * (axl * ayl * pl * pl + ayd * axd * pd * pd);
-            if (e < sigma * ad) e = ad;
-            pc = 1 / sqrt(e);
-        }
-        precon[c] = pc;
-        return pc;
-    }
-    static __device__ Carry shfl_up(Carry v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 };
 
 // Triangular-solve coefficients: forward uses Ax(i-1,j)*precon(i-1,j) and
 // Ay(i,j-1)*precon(i,j-1), backward Ax(i,j)*precon(i,j) and Ay(i,j)*precon(i,j)
 // (:403-405,413-415), each product rounded exactly as the reference rounds it.
 __global__ void k_coef(const double* __restrict__ Ax, const double* __restrict__ Ay, const double* __restrict__ pc,
-                       double2* cf, double2* cb, int NX, int NY) {
+                       double* cfx, double* cfy, double* cbx, double* cby, int NX, int NY) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (c >= (size_t)NX * NY) return;
     int i = (int)(c % NX), j = (int)(c / NX);
-    double fx = i > 0 ? Ax[c - 1] * pc[c - 1] : 0.0;
-    double fy = j > 0 ? Ay[c - NX] * pc[c - NX] : 0.0;
-    cf[c] = make_double2(fx, fy);
-    cb[c] = make_double2(Ax[c] * pc[c], Ay[c] * pc[c]);
+    cfx[c] = i > 0 ? Ax[c - 1] * pc[c - 1] : 0.0;
+    cfy[c] = j > 0 ? Ay[c - NX] * pc[c - NX] : 0.0;
+    cbx[c] = Ax[c] * pc[c];
+    cby[c] = Ay[c] * pc[c];
 }
 
-// applyPreconditioner, forward substitution (:400-409): q = L^-1 r.
-struct MicForwardOp {
-    static constexpr const char* kName = "wave_MicForwardOp";
-    typedef double Carry;
-    const uint8_t* cell;
-    const double *r, *pc;
-    const double2* cf;
-    double* q;
-    int NX;
-    __device__ Carry fetch(int i, int j, bool l2) const {
-        const double* a = q + (size_t)j * NX + i;
-        return l2 ? __ldcg(a) : *a;
+// applyPreconditioner, forward substitution (:400-409): q = L^-1 r.  Fluid
+// cells are exactly those with precon != 0 (precon = 1/sqrt(e) with e finite).
+struct MicForward64 {
+    static constexpr const char* kName = "wave2_MicForward64";
+    typedef double T;
+    static constexpr int NA = 4;
+    const double* in[4];  // r, cfx, cfy, precon
+    double* out;          // q
+    int pitch;
+    __device__ double stored(const double*, double r) const { return r; }
+    __device__ double border(int i, int j) const { return out[(size_t)j * pitch + i]; }
+    __device__ double compute(const double* v, double ql, double qd, int, int) const {
+        if (__double_as_longlong(v[3]) == 0) return 0.0;
+        double t = v[0] - v[1] * ql - v[2] * qd;
+        return t * v[3];
     }
-    __device__ Carry update(int i, int j, Carry ql, Carry qd) const {
-        size_t c = (size_t)j * NX + i;
-        double out = 0.0;
-        if (cell[c] == kFluid) {
-            double2 f = cf[c];
-            double t = r[c] - f.x * ql - f.y * qd;
-            out = t * pc[c];
-        }
-        q[c] = out;
-        return out;
-    }
-    static __device__ Carry shfl_up(Carry v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 };
 
 // applyPreconditioner, backward substitution (:410-419): z = L^-T q.
-struct MicBackwardOp {
-    static constexpr const char* kName = "wave_MicBackwardOp";
-    typedef double Carry;
-    const uint8_t* cell;
-    const double *q, *pc;
-    const double2* cb;
-    double* z;
-    int NX;
-    __device__ Carry fetch(int i, int j, bool l2) const {
-        const double* a = z + (size_t)j * NX + i;
-        return l2 ? __ldcg(a) : *a;
+struct MicBackward64 {
+    static constexpr const char* kName = "wave2_MicBackward64";
+    typedef double T;
+    static constexpr int NA = 4;
+    const double* in[4];  // q, cbx, cby, precon
+    double* out;          // z
+    int pitch;
+    __device__ double stored(const double*, double r) const { return r; }
+    __device__ double border(int i, int j) const { return out[(size_t)j * pitch + i]; }
+    __device__ double compute(const double* v, double zr, double zu, int, int) const {
+        if (__double_as_longlong(v[3]) == 0) return 0.0;
+        double t = v[0] - v[1] * zr - v[2] * zu;
+        return t * v[3];
     }
-    __device__ Carry update(int i, int j, Carry zr, Carry zu) const {
-        size_t c = (size_t)j * NX + i;
-        double out = 0.0;
-        if (cell[c] == kFluid) {
-            double2 b = cb[c];
-            double t = q[c] - b.x * zr - b.y * zu;
-            out = t * pc[c];
-        }
-        z[c] = out;
-        return out;
-    }
-    static __device__ Carry shfl_up(Carry v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 };
 
 // sigma = z.r (:428 before the loop; :457-460 in it).  In the loop the last
@@ -407,27 +385,36 @@ __global__ void k_diag(const uint8_t* __restrict__ cell, const double* __restric
 
 }  // namespace
 
+int projection_build(Sim* s) {
+    const double scaleA = s->dt / (s->rho * s->dx * s->dx);
+    FS2D_LAUNCH(s, k_build, blocks_for(s->N, kT), kT, 0, s->cell, s->phi, s->u, s->v, s->NX, s->NY, scaleA,
+                1.0 / s->dx, s->Adiag, s->Ax, s->Ay, s->rhs, s->r, s->p, s->partial, s->pcg, s->opt.pcg_tol);
+    return 0;
+}
+
 int projection(Sim* s, int* status) {
     const int NX = s->NX, NY = s->NY;
     const size_t N = s->N;
     const unsigned nb = blocks_for(N, kT);
-    const double scaleA = s->dt / (s->rho * s->dx * s->dx);
-    FS2D_LAUNCH(s, k_build, nb, kT, 0, s->cell, s->phi, s->u, s->v, NX, NY, scaleA, 1.0 / s->dx, s->Adiag, s->Ax,
-                s->Ay, s->rhs, s->r, s->p, s->partial, s->pcg, s->opt.pcg_tol);
     {
-        MicFactorOp op{s->cell, s->Adiag, s->Ax, s->Ay, s->precon, NX, s->opt.mic_tau, s->opt.mic_sigma};
-        int rc = launch_wave(s, op, WaveGeom{1, 1, 1, NX - 1, 1, NY - 1}, nullptr);
+        int rc0 = projection_build(s);
+        if (rc0) return rc0;
+    }
+    {
+        MicFactor64 op{{s->Adiag, s->Ax - 1, s->Ay - 1, s->Ay - NX, s->Ax - NX}, s->precon, NX, s->opt.mic_tau,
+                       s->opt.mic_sigma};
+        int rc = launch_wave2<MicFactor64, 1, 8>(s, op, WaveGeom{1, 1, 1, NX - 1, 1, NY - 1}, nullptr);
         if (rc) return rc;
     }
-    FS2D_LAUNCH(s, k_coef, nb, kT, 0, s->Ax, s->Ay, s->precon, s->coef_f, s->coef_b, NX, NY);
+    FS2D_LAUNCH(s, k_coef, nb, kT, 0, s->Ax, s->Ay, s->precon, s->cfx, s->cfy, s->cbx, s->cby, NX, NY);
     const int* done = &s->pcg->done;
-    MicForwardOp fwd{s->cell, s->r, s->precon, s->coef_f, s->q, NX};
-    MicBackwardOp bwd{s->cell, s->q, s->precon, s->coef_b, s->z, NX};
+    MicForward64 fwd{{s->r, s->cfx, s->cfy, s->precon}, s->q, NX};
+    MicBackward64 bwd{{s->q, s->cbx, s->cby, s->precon}, s->z, NX};
     const WaveGeom gf{1, 1, 1, NX - 1, 1, NY - 1};
     const WaveGeom gb{-1, -1, 0, NX - 2, 0, NY - 2};
-    int rc = launch_wave(s, fwd, gf, done);
+    int rc = launch_wave2<MicForward64, 2, 8>(s, fwd, gf, done);
     if (rc) return rc;
-    rc = launch_wave(s, bwd, gb, done);
+    rc = launch_wave2<MicBackward64, 2, 8>(s, bwd, gb, done);
     if (rc) return rc;
     FS2D_LAUNCH(s, k_dot_zr, nb, kT, 0, s->z, s->r, N, s->partial, s->pcg, 1, s->opt.pcg_max_iters);
 
@@ -441,9 +428,9 @@ int projection(Sim* s, int* status) {
         FS2D_LAUNCH(s, k_spmv, nb, kT, 0, s->cell, s->Adiag, s->Ax, s->Ay, s->z, s_old, s_new, s->w, NX, N, s->partial,
                     s->pcg);
         FS2D_LAUNCH(s, k_axpy, nb, kT, 0, s->p, s->r, s_new, s->w, N, s->partial, s->pcg);
-        rc = launch_wave(s, fwd, gf, done);
+        rc = launch_wave2<MicForward64, 2, 8>(s, fwd, gf, done);
         if (rc) return rc;
-        rc = launch_wave(s, bwd, gb, done);
+        rc = launch_wave2<MicBackward64, 2, 8>(s, bwd, gb, done);
         if (rc) return rc;
         FS2D_LAUNCH(s, k_dot_zr, nb, kT, 0, s->z, s->r, N, s->partial, s->pcg, 0, max_iters);
         if ((it + 1) % batch == 0 || it + 1 == max_iters) {

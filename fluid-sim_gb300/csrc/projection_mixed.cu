@@ -1,0 +1,375 @@
+// projection_mixed.cu — mixed-precision pressure solve (FS2D_PRECISION_MIXED).
+//
+// The reference's MIC(0)-PCG (src/FluidSim2D.cpp:252-467) with the inner
+// iteration in FP32 and the accuracy owned by FP64:
+//   * iterative refinement: the FP64 residual r = b - A p is recomputed from
+//     the FP64 matrix (built exactly as the reference builds it, projection.cu)
+//     after each inner solve, and the stop test is the reference's
+//     ||r||inf <= tol * ||b||inf on that FP64 residual;
+//   * each inner solve runs MIC(0)-PCG on A e = r / ||r||inf in FP32: matrix,
+//     preconditioner factor and both triangular solves (strip wavefronts in the
+//     reference's dependency order, precon folded into the coefficients so a
+//     cell costs two FMAs), SpMV and vector updates;
+//   * inner dot products use exact FP32 products (p + e, e from an FMA),
+//     double-float (FP32 pair) accumulation inside a warp and FP64 across
+//     warps and blocks; norms are maxima (exact in any precision); the
+//     scalars alpha, beta, sigma are FP64.
+// Compiled with the default FMA contraction.
+#include <cuda_runtime.h>
+#include <math.h>
+#include "fs2d_device.cuh"
+#include "wave2.cuh"
+
+namespace fs2d {
+namespace {
+
+constexpr int kT = 256;
+
+// ---- double-float accumulation of exact products ----
+struct DF {
+    float hi, lo;
+};
+__device__ __forceinline__ void df_add(DF& a, float b) {  // TwoSum
+    float s = a.hi + b;
+    float bb = s - a.hi;
+    float err = (a.hi - (s - bb)) + (b - bb);
+    a.hi = s;
+    a.lo += err;
+}
+__device__ __forceinline__ DF df_prod(float x, float y) {  // exact: x*y = hi + lo
+    float p = x * y;
+    return DF{p, fmaf(x, y, -p)};
+}
+__device__ __forceinline__ void df_add(DF& a, DF b) {
+    df_add(a, b.hi);
+    a.lo += b.lo;
+}
+__device__ __forceinline__ DF df_warp_sum(DF v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        DF t{__shfl_down_sync(0xffffffffu, v.hi, o), __shfl_down_sync(0xffffffffu, v.lo, o)};
+        df_add(v, t);
+    }
+    return v;
+}
+// Block sum of per-thread products as FP64 (valid in thread 0).
+__device__ __forceinline__ double block_dot(DF v, double* sh) {
+    v = df_warp_sum(v);
+    double d = (double)v.hi + (double)v.lo;
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = d;
+    __syncthreads();
+    int nw = (blockDim.x + 31) >> 5;
+    d = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
+    if (wid == 0) d = warp_sum(d);
+    return d;
+}
+
+// FP32 copies of the FP64 matrix (Adiag keeps its -0.0 non-fluid marker).
+__global__ void k_mixed_matrix(const double* __restrict__ A0, const double* __restrict__ Ax,
+                               const double* __restrict__ Ay, float* a0, float* ax, float* ay, size_t N) {
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    a0[c] = (float)A0[c];
+    ax[c] = (float)Ax[c];
+    ay[c] = (float)Ay[c];
+}
+
+struct MicFactor32 {
+    static constexpr const char* kName = "wave2_MicFactor32";
+    typedef float T;
+    static constexpr int NA = 5;
+    const float* in[5];  // Adiag(i,j), Ax(i-1,j), Ay(i-1,j), Ay(i,j-1), Ax(i,j-1)
+    float* out;          // precon
+    int pitch;
+    float tau, sigma;
+    __device__ float border(int i, int j) const { return out[(size_t)j * pitch + i]; }
+    __device__ float stored(const float*, float r) const { return r; }
+    __device__ float compute(const float* v, float pl, float pd, int, int) const {
+        const float ad = v[0];
+        if (signbit(ad)) return 0.0f;
+        const float axl = v[1], ayl = v[2], ayd = v[3], axd = v[4];
+        float e = ad - (axl * pl) * (axl * pl) - (ayd * pd) * (ayd * pd) -
+                  tau * (axl * ayl * pl * pl + ayd * axd * pd * pd);
+        if (e < sigma * ad) e = ad;
+        return 1.0f / sqrtf(e);
+    }
+};
+
+// Folded coefficients: forward q = r*pc - fa*q(i-1,j) - fb*q(i,j-1),
+// backward z = q*pc - fc*z(i+1,j) - fd*z(i,j+1).
+__global__ void k_mixed_coef(const float* __restrict__ ax, const float* __restrict__ ay,
+                             const float* __restrict__ pc, float* fa, float* fb, float* fc, float* fd, int NX,
+                             int NY) {
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= (size_t)NX * NY) return;
+    int i = (int)(c % NX), j = (int)(c / NX);
+    float p = pc[c];
+    fa[c] = i > 0 ? ax[c - 1] * pc[c - 1] * p : 0.0f;
+    fb[c] = j > 0 ? ay[c - NX] * pc[c - NX] * p : 0.0f;
+    fc[c] = ax[c] * p * p;
+    fd[c] = ay[c] * p * p;
+}
+
+struct MicForward32 {
+    static constexpr const char* kName = "wave2_MicForward32";
+    typedef float T;
+    static constexpr int NA = 3;
+    const float* in[3];  // r*pc, fa, fb
+    float* out;          // q
+    int pitch;
+    __device__ float border(int i, int j) const { return out[(size_t)j * pitch + i]; }
+    __device__ float stored(const float*, float r) const { return r; }
+    __device__ float compute(const float* v, float ql, float qd, int, int) const {
+        return fmaf(-v[2], qd, fmaf(-v[1], ql, v[0]));
+    }
+};
+
+struct MicBackward32 {
+    static constexpr const char* kName = "wave2_MicBackward32";
+    typedef float T;
+    static constexpr int NA = 4;
+    const float* in[4];  // q, pc, fc, fd
+    float* out;          // z
+    int pitch;
+    __device__ float border(int i, int j) const { return out[(size_t)j * pitch + i]; }
+    __device__ float stored(const float*, float r) const { return r; }
+    __device__ float compute(const float* v, float zr, float zu, int, int) const {
+        return fmaf(-v[3], zu, fmaf(-v[2], zr, v[0] * v[1]));
+    }
+};
+
+// FP64 residual r = b - A p on fluid cells (the SpMV of :433-444 in FP64),
+// ||r||inf into the outer scalars.
+__global__ void k_resid64(const uint8_t* __restrict__ cell, const double* __restrict__ A0,
+                          const double* __restrict__ Ax, const double* __restrict__ Ay, const double* __restrict__ rhs,
+                          const double* __restrict__ p, double* r, int NX, size_t N, double* partial,
+                          PcgScalars* outer) {
+    __shared__ double sh[32];
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    double m = 0;
+    if (c < N) {
+        double v = 0.0;
+        if (cell[c] == kFluid) {
+            double ap = A0[c] * p[c] + Ax[c - 1] * p[c - 1] + Ax[c] * p[c + 1] + Ay[c - NX] * p[c - NX] +
+                        Ay[c] * p[c + NX];
+            v = rhs[c] - ap;
+        }
+        r[c] = v;
+        m = fabs(v);
+    }
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+    if (last_block(&outer->ticket[0])) {
+        double mm = 0;
+        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) mm = fmax(mm, partial[k]);
+        mm = block_max(mm, sh);
+        if (threadIdx.x == 0) outer->r_norm = mm;
+    }
+}
+
+// Start of an inner solve: r32 = r64 / ||r64||inf, r*pc, e = 0, scalars reset.
+__global__ void k_inner_init(const double* __restrict__ r64, const PcgScalars* __restrict__ outer,
+                             const float* __restrict__ pc, float* r32, float* rp32, float* e32, size_t N,
+                             PcgScalars* inner) {
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const double rn = outer->r_norm;
+    const double scale = rn > 0 ? 1.0 / rn : 0.0;
+    if (c < N) {
+        float rv = (float)(r64[c] * scale);
+        r32[c] = rv;
+        rp32[c] = rv * pc[c];
+        e32[c] = 0.0f;
+    }
+    if (c == 0) {
+        inner->iter = 0;
+        inner->done = (rn > 0) ? 0 : 1;
+        inner->first = 1;
+        inner->sigma = inner->alpha = inner->beta = 0;
+        inner->rhs_norm = 1.0;
+        inner->r_norm = 1.0;
+    }
+}
+
+__global__ void k_dot32(const float* __restrict__ z, const float* __restrict__ r, size_t N, double* partial,
+                        PcgScalars* pcg, int init, int max_iters) {
+    __shared__ double sh[32];
+    if (pcg->done) return;
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    DF a = c < N ? df_prod(z[c], r[c]) : DF{0.f, 0.f};
+    double d = block_dot(a, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = d;
+    if (last_block(&pcg->ticket[1])) {
+        double s = 0;
+        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) s += partial[k];
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) {
+            if (init) {
+                pcg->sigma = s;
+            } else {
+                pcg->beta = s / pcg->sigma;
+                pcg->sigma = s;
+                pcg->iter += 1;
+                pcg->first = 0;
+                if (pcg->iter >= max_iters) pcg->done = 2;
+            }
+        }
+    }
+}
+
+__global__ void k_spmv32(const uint8_t* __restrict__ cell, const float* __restrict__ a0,
+                         const float* __restrict__ ax, const float* __restrict__ ay, const float* __restrict__ z,
+                         const float* __restrict__ s_old, float* s_new, float* w, int NX, size_t N, double* partial,
+                         PcgScalars* pcg) {
+    __shared__ double sh[32];
+    if (pcg->done) return;
+    const bool first = pcg->first != 0;
+    const float beta = (float)pcg->beta;
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    DF a{0.f, 0.f};
+    if (c < N) {
+        float sc = first ? z[c] : fmaf(beta, s_old[c], z[c]);
+        s_new[c] = sc;
+        float out = 0.0f;
+        if (cell[c] == kFluid) {
+            float sl = first ? z[c - 1] : fmaf(beta, s_old[c - 1], z[c - 1]);
+            float sr = first ? z[c + 1] : fmaf(beta, s_old[c + 1], z[c + 1]);
+            float sd = first ? z[c - NX] : fmaf(beta, s_old[c - NX], z[c - NX]);
+            float su = first ? z[c + NX] : fmaf(beta, s_old[c + NX], z[c + NX]);
+            out = a0[c] * sc + ax[c - 1] * sl + ax[c] * sr + ay[c - NX] * sd + ay[c] * su;
+        }
+        w[c] = out;
+        a = df_prod(out, sc);
+    }
+    double d = block_dot(a, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = d;
+    if (last_block(&pcg->ticket[2])) {
+        double s = 0;
+        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) s += partial[k];
+        s = block_sum(s, sh);
+        if (threadIdx.x == 0) {
+            if (s == 0.0) pcg->done = 1;
+            else pcg->alpha = pcg->sigma / s;
+        }
+    }
+}
+
+__global__ void k_axpy32(float* e, float* r, float* rp, const float* __restrict__ pc, const float* __restrict__ s,
+                         const float* __restrict__ w, size_t N, double* partial, PcgScalars* pcg, double inner_tol) {
+    __shared__ double sh[32];
+    if (pcg->done) return;
+    const float alpha = (float)pcg->alpha;
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    double m = 0;
+    if (c < N) {
+        e[c] = fmaf(alpha, s[c], e[c]);
+        float rv = fmaf(-alpha, w[c], r[c]);
+        r[c] = rv;
+        rp[c] = rv * pc[c];
+        m = fabsf(rv);
+    }
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+    if (last_block(&pcg->ticket[3])) {
+        double mm = 0;
+        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) mm = fmax(mm, partial[k]);
+        mm = block_max(mm, sh);
+        if (threadIdx.x == 0) {
+            pcg->r_norm = mm;
+            if (mm <= inner_tol) pcg->done = 1;
+        }
+    }
+}
+
+// p += e * ||r||inf (undo the inner scaling) in FP64.
+__global__ void k_update64(double* p, const float* __restrict__ e, const PcgScalars* __restrict__ outer, size_t N) {
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c < N) p[c] = p[c] + (double)e[c] * outer->r_norm;
+}
+
+}  // namespace
+
+int projection_mixed(Sim* s, int* status) {
+    const int NX = s->NX, NY = s->NY;
+    const size_t N = s->N;
+    const unsigned nb = blocks_for(N, kT);
+    Mixed32& m = s->m32;
+    // the FP64 matrix, rhs, ||b||inf, p = 0, r = b (exactly the reference's)
+    int rc = projection_build(s);
+    if (rc) return rc;
+    FS2D_LAUNCH(s, k_mixed_matrix, nb, kT, 0, s->Adiag, s->Ax, s->Ay, m.a0, m.ax, m.ay, N);
+    {
+        MicFactor32 op{{m.a0, m.ax - 1, m.ay - 1, m.ay - NX, m.ax - NX}, m.pc, NX, (float)s->opt.mic_tau,
+                       (float)s->opt.mic_sigma};
+        rc = launch_wave2<MicFactor32, 2, 16>(s, op, WaveGeom{1, 1, 1, NX - 1, 1, NY - 1}, nullptr);
+        if (rc) return rc;
+    }
+    FS2D_LAUNCH(s, k_mixed_coef, nb, kT, 0, m.ax, m.ay, m.pc, m.fa, m.fb, m.fc, m.fd, NX, NY);
+
+    PcgScalars* outer = s->pcg;     // rhs_norm, tol_abs from projection_build; r_norm = ||r64||
+    PcgScalars* inner = s->pcg32;
+    const int* done = &inner->done;
+    MicForward32 fwd{{m.rp, m.fa, m.fb}, m.q, NX};
+    MicBackward32 bwd{{m.q, m.pc, m.fc, m.fd}, m.z, NX};
+    const WaveGeom gf{1, 1, 1, NX - 1, 1, NY - 1};
+    const WaveGeom gb{-1, -1, 0, NX - 2, 0, NY - 2};
+    const int max_iters = s->opt.pcg_max_iters;
+    const int batch = 4;
+    int total_iters = 0, outer_iters = 0, status_out = 0;
+
+    FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, outer, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    const double rhs_norm = s->pcg_host->rhs_norm;
+    const double tol_abs = s->pcg_host->tol_abs;
+    double r_norm = rhs_norm;
+    if (rhs_norm > 1e-12) {
+        for (outer_iters = 0; outer_iters < s->opt.ir_max_outer; outer_iters++) {
+            if (r_norm <= tol_abs) break;
+            FS2D_LAUNCH(s, k_inner_init, nb, kT, 0, s->r, outer, m.pc, m.r, m.rp, m.e, N, inner);
+            rc = launch_wave2<MicForward32, 4, 16>(s, fwd, gf, done);
+            if (rc) return rc;
+            rc = launch_wave2<MicBackward32, 4, 16>(s, bwd, gb, done);
+            if (rc) return rc;
+            FS2D_LAUNCH(s, k_dot32, nb, kT, 0, m.z, m.r, N, s->partial, inner, 1, max_iters);
+            float* sbuf[2] = {m.s0, m.s1};
+            for (int it = 0; it < max_iters; it++) {
+                float* s_old = sbuf[it & 1];
+                float* s_new = sbuf[(it + 1) & 1];
+                FS2D_LAUNCH(s, k_spmv32, nb, kT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, N,
+                            s->partial, inner);
+                FS2D_LAUNCH(s, k_axpy32, nb, kT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, N, s->partial, inner,
+                            s->opt.ir_inner_tol);
+                rc = launch_wave2<MicForward32, 4, 16>(s, fwd, gf, done);
+                if (rc) return rc;
+                rc = launch_wave2<MicBackward32, 4, 16>(s, bwd, gb, done);
+                if (rc) return rc;
+                FS2D_LAUNCH(s, k_dot32, nb, kT, 0, m.z, m.r, N, s->partial, inner, 0, max_iters);
+                if ((it + 1) % batch == 0 || it + 1 == max_iters) {
+                    FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                              s->stream));
+                    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+                    if (s->pcg32_host->done) break;
+                }
+            }
+            FS2D_LAUNCH(s, k_update64, nb, kT, 0, s->p, m.e, outer, N);
+            FS2D_LAUNCH(s, k_resid64, nb, kT, 0, s->cell, s->Adiag, s->Ax, s->Ay, s->rhs, s->p, s->r, NX, N,
+                        s->partial, outer);
+            FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
+            FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, outer, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
+            FS2D_CUDA(cudaStreamSynchronize(s->stream));
+            total_iters += s->pcg32_host->iter;
+            r_norm = s->pcg_host->r_norm;
+        }
+        if (r_norm > tol_abs) status_out = FS2D_ERR_NOT_CONVERGED;
+    } else {
+        r_norm = rhs_norm;
+    }
+    s->last_iters = total_iters;
+    s->last_outer = outer_iters;
+    s->last_rel_res = rhs_norm > 0 ? r_norm / rhs_norm : 0.0;
+    if (status) *status = status_out;
+    return 0;
+}
+
+}  // namespace fs2d

@@ -1,0 +1,75 @@
+"""Mixed-precision projection (FP32 MIC(0)-PCG inside FP64 iterative
+refinement) against the reference.
+
+The stop test is the reference's, ||r||inf <= tol * ||b||inf, evaluated on
+the FP64 residual b - A p, so at the reference's tol = 1e-12 the mixed
+pressure agrees with the reference's FP64 solve to PRESSURE_RTOL, the same
+tolerance the FP64 path is held to."""
+import numpy as np
+import pytest
+
+import golden_util as G
+import oracle_py as O
+
+fs2d = pytest.importorskip("fs2d")
+pytestmark = pytest.mark.gpu
+
+PRESSURE_RTOL = 1e-8
+
+
+@pytest.mark.parametrize("name", G.NAMES)
+def test_mixed_projection_matches_reference(name):
+    g = G.load(name)
+    sc = G.scene(g)
+    k = G.stage_order(sc).index("applyProjection")
+    sim = fs2d.FluidSim2D(sc, seed=7, precision="mixed")
+    sim.set_state(G.pre_stage(g, k))
+    sim.stage("applyProjection")
+    p = sim.get_state(["p"])["p"]
+    ref = g[f"s{k}_post_p"]
+    scale = np.abs(ref).max()
+    assert np.abs(p - ref).max() <= PRESSURE_RTOL * scale
+    st = sim.stats()
+    assert st["pcgRelResidual"] <= 1e-12
+    assert st["irOuterIterations"] >= 1
+
+
+@pytest.mark.parametrize("tol", [1e-6, 1e-10])
+def test_mixed_meets_tolerance_on_fp64_residual(tol):
+    import scenes
+    sc = scenes.pic_dam_break_disk(96)
+    sim = fs2d.FluidSim2D(sc, seed=3, precision="mixed", pcg_tol=tol)
+    ref = fs2d.FluidSim2D(sc, seed=3, precision="fp64", pcg_tol=1e-13, pcg_max_iters=2000)
+    for _ in range(3):
+        sim.runFrame()
+        ref.runFrame()
+    st = sim.stats()
+    assert st["pcgRelResidual"] <= tol
+    # same pre-projection state for both: compare one projection stage
+    pre = ref.get_state()
+    sim.set_state(pre)
+    ref.set_state(pre)
+    for s in ("createWaterLevelSet", "transferVelocityToGrid", "applyGravity"):
+        sim.stage(s)
+        ref.stage(s)
+    sim.stage("applyProjection")
+    ref.stage("applyProjection")
+    p, pr = sim.get_state(["p"])["p"], ref.get_state(["p"])["p"]
+    # ||p - p*|| is bounded by cond(A) * tol; check a loose multiple
+    assert np.abs(p - pr).max() <= 1e4 * tol * np.abs(pr).max()
+
+
+@pytest.mark.parametrize("name", ["pic_disk_32", "sl_dam_32"])
+def test_mixed_frames_against_oracle(name):
+    g = G.load(name)
+    sc = G.scene(g)
+    sim = fs2d.FluidSim2D(sc, seed=7, precision="mixed")
+    orc = O.OracleSim(sc, seed=7, sl_inplace=0)
+    for frame in range(10):
+        sim.runFrame()
+        orc.frame()
+        a, b = sim.get_state(), orc.get_state()
+        assert np.array_equal(a["cell"], b["cell"]), frame
+        for f in ("p", "u", "v", "particles", "particleVels"):
+            scale = np.abs(b[f]).max() + 1e-30
+            assert np.abs(a[f] - b[f]).max() <= 1e-6 * scale, (frame, f)
