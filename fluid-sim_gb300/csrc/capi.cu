@@ -200,6 +200,8 @@ int alloc_all(Sim* s) {
     A(err, 1);
     if (s->opt.precision == FS2D_PRECISION_MIXED) {
         Mixed32& m = s->m32;
+        s->P = (s->NX + 31) / 32 * 32;
+        const size_t N = (size_t)s->P * s->NY;  // pitched FP32 arrays
         A(m32.a0, N);
         A(m32.ax, N);
         A(m32.ay, N);
@@ -218,6 +220,12 @@ int alloc_all(Sim* s) {
         A(m32.e, N);
         A(pcg32, 1);
         (void)m;
+        s->m32maps = new (std::nothrow) Mic32MapsHost();
+        if (!s->m32maps) {
+            set_error("out of host memory");
+            return FS2D_ERR_ALLOC;
+        }
+        if ((rc = mixed_setup_maps(s))) return rc;
     }
 #undef A
     if ((rc = check_cuda(cudaMallocHost((void**)&s->pcg_host, sizeof(PcgScalars)), "cudaMallocHost"))) return rc;
@@ -243,6 +251,7 @@ void free_all(Sim* s) {
         if (p) cudaFree(p);
     if (s->pcg_host) cudaFreeHost(s->pcg_host);
     if (s->pcg32_host) cudaFreeHost(s->pcg32_host);
+    delete s->m32maps;
     if (s->stats_host) cudaFreeHost(s->stats_host);
     if (s->err_host) cudaFreeHost(s->err_host);
     for (auto& e : s->ev)

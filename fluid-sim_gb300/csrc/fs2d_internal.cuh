@@ -6,6 +6,7 @@
 // (include/MACGrid2D.h:19-25); particles are interleaved (x, y) pairs.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
@@ -51,12 +52,19 @@ struct FrameStats {
     unsigned int pad;
 };
 
-// FP32 arrays of the mixed-precision inner solver (projection_mixed.cu).
+// FP32 arrays of the mixed-precision inner solver (projection_mixed.cu),
+// each P x NY with a row pitch of P = NX rounded up to 32 floats (tiles of
+// the TMA wavefront start on 128-byte boundaries); padding holds zeros.
 struct Mixed32 {
     float *a0 = nullptr, *ax = nullptr, *ay = nullptr;             // matrix
     float *pc = nullptr, *fa = nullptr, *fb = nullptr, *fc = nullptr, *fd = nullptr;  // MIC(0), folded
     float *r = nullptr, *rp = nullptr, *q = nullptr, *z = nullptr, *w = nullptr;
     float *s0 = nullptr, *s1 = nullptr, *e = nullptr;
+};
+// TMA descriptors of the two FP32 MIC(0) sweeps (see mic32_tma.cuh).
+struct Mic32MapsHost {
+    alignas(64) unsigned char fwd[4 * 128 + 128];
+    alignas(64) unsigned char bwd[4 * 128 + 128];
 };
 
 struct Sim {
@@ -106,6 +114,8 @@ struct Sim {
     PcgScalars* pcg = nullptr;
     PcgScalars* pcg_host = nullptr;                  // pinned mirror for polling
     Mixed32 m32;                                     // MIXED precision only
+    int P = 0;                                       // row pitch of the FP32 arrays
+    Mic32MapsHost* m32maps = nullptr;
     PcgScalars* pcg32 = nullptr;                     // inner FP32 solve scalars
     PcgScalars* pcg32_host = nullptr;
 
@@ -185,6 +195,7 @@ int apply_gravity(Sim* s);                // applyGravity
 int projection(Sim* s, int* status);      // applyProjection, FP64
 int projection_mixed(Sim* s, int* status);  // applyProjection, FP32 PCG in FP64 refinement
 int projection_build(Sim* s);             // FP64 matrix, rhs, p = 0, r = rhs, ||rhs||
+int mixed_setup_maps(Sim* s);             // TMA descriptors of the FP32 MIC(0) sweeps
 int update_velocity(Sim* s);              // updateVelocity
 int g2p(Sim* s);                          // updateParticleVelocities
 int advect_particles(Sim* s);             // applyAdvection

@@ -8,8 +8,9 @@
 //     ||r||inf <= tol * ||b||inf on that FP64 residual;
 //   * each inner solve runs MIC(0)-PCG on A e = r / ||r||inf in FP32: matrix,
 //     preconditioner factor and both triangular solves (strip wavefronts in the
-//     reference's dependency order, precon folded into the coefficients so a
-//     cell costs two FMAs), SpMV and vector updates;
+//     reference's dependency order; the forward solve runs on q~ = q*precon,
+//     so both solves have the form out = v0 - v1*left - v2*below with three
+//     operand arrays, TMA-staged, see mic32_tma.cuh), SpMV and vector updates;
 //   * inner dot products use exact FP32 products (p + e, e from an FMA),
 //     double-float (FP32 pair) accumulation inside a warp and FP64 across
 //     warps and blocks; norms are maxima (exact in any precision); the
@@ -17,8 +18,11 @@
 // Compiled with the default FMA contraction.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <string.h>
+#include <cudaTypedefs.h>
 #include "fs2d_device.cuh"
 #include "wave2.cuh"
+#include "mic32_tma.cuh"
 
 namespace fs2d {
 namespace {
@@ -66,14 +70,17 @@ __device__ __forceinline__ double block_dot(DF v, double* sh) {
     return d;
 }
 
-// FP32 copies of the FP64 matrix (Adiag keeps its -0.0 non-fluid marker).
+// FP32 copies of the FP64 matrix in the pitched layout (Adiag keeps its
+// -0.0 non-fluid marker).
 __global__ void k_mixed_matrix(const double* __restrict__ A0, const double* __restrict__ Ax,
-                               const double* __restrict__ Ay, float* a0, float* ax, float* ay, size_t N) {
+                               const double* __restrict__ Ay, float* a0, float* ax, float* ay, int NX, int P,
+                               size_t N) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (c >= N) return;
-    a0[c] = (float)A0[c];
-    ax[c] = (float)Ax[c];
-    ay[c] = (float)Ay[c];
+    size_t k = (c / NX) * (size_t)P + (c % NX);
+    a0[k] = (float)A0[c];
+    ax[k] = (float)Ax[c];
+    ay[k] = (float)Ay[c];
 }
 
 struct MicFactor32 {
@@ -97,48 +104,26 @@ struct MicFactor32 {
     }
 };
 
-// Folded coefficients: forward q = r*pc - fa*q(i-1,j) - fb*q(i,j-1),
-// backward z = q*pc - fc*z(i+1,j) - fd*z(i,j+1).
+// Folded MIC(0) coefficients.  With q~ = q*pc the reference's forward
+// substitution q = (r - Ax(i-1,j)pc(i-1,j)q(i-1,j) - Ay(i,j-1)pc(i,j-1)q(i,j-1))*pc
+// becomes q~ = r*pc^2 - fa*q~(i-1,j) - fb*q~(i,j-1) with fa = Ax(i-1,j)*pc^2,
+// fb = Ay(i,j-1)*pc^2, and the backward substitution
+// z = (q - Ax pc z(i+1,j) - Ay pc z(i,j+1))*pc becomes z = q~ - fc*z(i+1,j) - fd*z(i,j+1)
+// with fc = Ax*pc^2, fd = Ay*pc^2 (pc taken at (i,j)).
 __global__ void k_mixed_coef(const float* __restrict__ ax, const float* __restrict__ ay,
-                             const float* __restrict__ pc, float* fa, float* fb, float* fc, float* fd, int NX,
-                             int NY) {
+                             const float* __restrict__ pc, float* fa, float* fb, float* fc, float* fd, int NX, int NY,
+                             int P) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (c >= (size_t)NX * NY) return;
     int i = (int)(c % NX), j = (int)(c / NX);
-    float p = pc[c];
-    fa[c] = i > 0 ? ax[c - 1] * pc[c - 1] * p : 0.0f;
-    fb[c] = j > 0 ? ay[c - NX] * pc[c - NX] * p : 0.0f;
-    fc[c] = ax[c] * p * p;
-    fd[c] = ay[c] * p * p;
+    size_t k = (size_t)j * P + i;
+    float p = pc[k];
+    float p2 = p * p;
+    fa[k] = i > 0 ? ax[k - 1] * p2 : 0.0f;
+    fb[k] = j > 0 ? ay[k - P] * p2 : 0.0f;
+    fc[k] = ax[k] * p2;
+    fd[k] = ay[k] * p2;
 }
-
-struct MicForward32 {
-    static constexpr const char* kName = "wave2_MicForward32";
-    typedef float T;
-    static constexpr int NA = 3;
-    const float* in[3];  // r*pc, fa, fb
-    float* out;          // q
-    int pitch;
-    __device__ float border(int i, int j) const { return out[(size_t)j * pitch + i]; }
-    __device__ float stored(const float*, float r) const { return r; }
-    __device__ float compute(const float* v, float ql, float qd, int, int) const {
-        return fmaf(-v[2], qd, fmaf(-v[1], ql, v[0]));
-    }
-};
-
-struct MicBackward32 {
-    static constexpr const char* kName = "wave2_MicBackward32";
-    typedef float T;
-    static constexpr int NA = 4;
-    const float* in[4];  // q, pc, fc, fd
-    float* out;          // z
-    int pitch;
-    __device__ float border(int i, int j) const { return out[(size_t)j * pitch + i]; }
-    __device__ float stored(const float*, float r) const { return r; }
-    __device__ float compute(const float* v, float zr, float zu, int, int) const {
-        return fmaf(-v[3], zu, fmaf(-v[2], zr, v[0] * v[1]));
-    }
-};
 
 // FP64 residual r = b - A p on fluid cells (the SpMV of :433-444 in FP64),
 // ||r||inf into the outer scalars.
@@ -169,18 +154,20 @@ __global__ void k_resid64(const uint8_t* __restrict__ cell, const double* __rest
     }
 }
 
-// Start of an inner solve: r32 = r64 / ||r64||inf, r*pc, e = 0, scalars reset.
+// Start of an inner solve: r32 = r64 / ||r64||inf, r*pc^2, e = 0, scalars reset.
 __global__ void k_inner_init(const double* __restrict__ r64, const PcgScalars* __restrict__ outer,
-                             const float* __restrict__ pc, float* r32, float* rp32, float* e32, size_t N,
-                             PcgScalars* inner) {
+                             const float* __restrict__ pc, float* r32, float* rp32, float* e32, int NX, int P,
+                             size_t N, PcgScalars* inner) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const double rn = outer->r_norm;
     const double scale = rn > 0 ? 1.0 / rn : 0.0;
     if (c < N) {
+        size_t k = (c / NX) * (size_t)P + (c % NX);
         float rv = (float)(r64[c] * scale);
-        r32[c] = rv;
-        rp32[c] = rv * pc[c];
-        e32[c] = 0.0f;
+        float p = pc[k];
+        r32[k] = rv;
+        rp32[k] = rv * (p * p);
+        e32[k] = 0.0f;
     }
     if (c == 0) {
         inner->iter = 0;
@@ -192,12 +179,16 @@ __global__ void k_inner_init(const double* __restrict__ r64, const PcgScalars* _
     }
 }
 
-__global__ void k_dot32(const float* __restrict__ z, const float* __restrict__ r, size_t N, double* partial,
-                        PcgScalars* pcg, int init, int max_iters) {
+__global__ void k_dot32(const float* __restrict__ z, const float* __restrict__ r, int NX, int P, size_t N,
+                        double* partial, PcgScalars* pcg, int init, int max_iters) {
     __shared__ double sh[32];
     if (pcg->done) return;
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    DF a = c < N ? df_prod(z[c], r[c]) : DF{0.f, 0.f};
+    DF a{0.f, 0.f};
+    if (c < N) {
+        size_t k = (c / NX) * (size_t)P + (c % NX);
+        a = df_prod(z[k], r[k]);
+    }
     double d = block_dot(a, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = d;
     if (last_block(&pcg->ticket[1])) {
@@ -220,8 +211,8 @@ __global__ void k_dot32(const float* __restrict__ z, const float* __restrict__ r
 
 __global__ void k_spmv32(const uint8_t* __restrict__ cell, const float* __restrict__ a0,
                          const float* __restrict__ ax, const float* __restrict__ ay, const float* __restrict__ z,
-                         const float* __restrict__ s_old, float* s_new, float* w, int NX, size_t N, double* partial,
-                         PcgScalars* pcg) {
+                         const float* __restrict__ s_old, float* s_new, float* w, int NX, int P, size_t N,
+                         double* partial, PcgScalars* pcg) {
     __shared__ double sh[32];
     if (pcg->done) return;
     const bool first = pcg->first != 0;
@@ -229,17 +220,18 @@ __global__ void k_spmv32(const uint8_t* __restrict__ cell, const float* __restri
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     DF a{0.f, 0.f};
     if (c < N) {
-        float sc = first ? z[c] : fmaf(beta, s_old[c], z[c]);
-        s_new[c] = sc;
+        size_t k = (c / NX) * (size_t)P + (c % NX);
+        float sc = first ? z[k] : fmaf(beta, s_old[k], z[k]);
+        s_new[k] = sc;
         float out = 0.0f;
         if (cell[c] == kFluid) {
-            float sl = first ? z[c - 1] : fmaf(beta, s_old[c - 1], z[c - 1]);
-            float sr = first ? z[c + 1] : fmaf(beta, s_old[c + 1], z[c + 1]);
-            float sd = first ? z[c - NX] : fmaf(beta, s_old[c - NX], z[c - NX]);
-            float su = first ? z[c + NX] : fmaf(beta, s_old[c + NX], z[c + NX]);
-            out = a0[c] * sc + ax[c - 1] * sl + ax[c] * sr + ay[c - NX] * sd + ay[c] * su;
+            float sl = first ? z[k - 1] : fmaf(beta, s_old[k - 1], z[k - 1]);
+            float sr = first ? z[k + 1] : fmaf(beta, s_old[k + 1], z[k + 1]);
+            float sd = first ? z[k - P] : fmaf(beta, s_old[k - P], z[k - P]);
+            float su = first ? z[k + P] : fmaf(beta, s_old[k + P], z[k + P]);
+            out = a0[k] * sc + ax[k - 1] * sl + ax[k] * sr + ay[k - P] * sd + ay[k] * su;
         }
-        w[c] = out;
+        w[k] = out;
         a = df_prod(out, sc);
     }
     double d = block_dot(a, sh);
@@ -256,17 +248,20 @@ __global__ void k_spmv32(const uint8_t* __restrict__ cell, const float* __restri
 }
 
 __global__ void k_axpy32(float* e, float* r, float* rp, const float* __restrict__ pc, const float* __restrict__ s,
-                         const float* __restrict__ w, size_t N, double* partial, PcgScalars* pcg, double inner_tol) {
+                         const float* __restrict__ w, int NX, int P, size_t N, double* partial, PcgScalars* pcg,
+                         double inner_tol) {
     __shared__ double sh[32];
     if (pcg->done) return;
     const float alpha = (float)pcg->alpha;
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     double m = 0;
     if (c < N) {
-        e[c] = fmaf(alpha, s[c], e[c]);
-        float rv = fmaf(-alpha, w[c], r[c]);
-        r[c] = rv;
-        rp[c] = rv * pc[c];
+        size_t k = (c / NX) * (size_t)P + (c % NX);
+        e[k] = fmaf(alpha, s[k], e[k]);
+        float rv = fmaf(-alpha, w[k], r[k]);
+        r[k] = rv;
+        float p = pc[k];
+        rp[k] = rv * (p * p);
         m = fabsf(rv);
     }
     m = block_max(m, sh);
@@ -283,37 +278,91 @@ __global__ void k_axpy32(float* e, float* r, float* rp, const float* __restrict_
 }
 
 // p += e * ||r||inf (undo the inner scaling) in FP64.
-__global__ void k_update64(double* p, const float* __restrict__ e, const PcgScalars* __restrict__ outer, size_t N) {
+__global__ void k_update64(double* p, const float* __restrict__ e, const PcgScalars* __restrict__ outer, int NX, int P,
+                           size_t N) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (c < N) p[c] = p[c] + (double)e[c] * outer->r_norm;
+    if (c < N) p[c] = p[c] + (double)e[(c / NX) * (size_t)P + (c % NX)] * outer->r_norm;
 }
 
 }  // namespace
 
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+int mic32_make_map(CUtensorMap* map, float* base, int P, int NY, int box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return FS2D_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)P, (cuuint64_t)NY};
+    cuuint64_t strides[1] = {(cuuint64_t)P * sizeof(float)};
+    cuuint32_t box[2] = {(cuuint32_t)kM32Cols, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return FS2D_ERR_CUDA;
+    }
+    return 0;
+}
+
+static_assert(sizeof(Mic32Maps) <= sizeof(Mic32MapsHost::fwd), "tensor map storage");
+
+// Tensor maps of the FP32 MIC(0) sweeps, built once per handle.
+int mixed_setup_maps(Sim* s) {
+    Mixed32& m = s->m32;
+    Mic32Maps f{}, b{};
+    const int tail = s->NY % kM32Rows;
+    int rc = 0;
+    float* fin[3] = {m.rp, m.fa, m.fb};
+    float* bin[3] = {m.q, m.fc, m.fd};
+    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&f.in[a], fin[a], s->P, s->NY, kM32Rows);
+    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&b.in[a], bin[a], s->P, s->NY, kM32Rows);
+    if (!rc) rc = mic32_make_map(&f.out, m.q, s->P, s->NY, kM32Rows);
+    if (!rc) rc = mic32_make_map(&b.out, m.z, s->P, s->NY, kM32Rows);
+    if (!rc) rc = mic32_make_map(&f.out_tail, m.q, s->P, s->NY, tail > 0 ? tail : kM32Rows);
+    if (!rc) rc = mic32_make_map(&b.out_tail, m.z, s->P, s->NY, tail > 0 ? tail : kM32Rows);
+    if (rc) return rc;
+    memcpy(s->m32maps->fwd, &f, sizeof(f));
+    memcpy(s->m32maps->bwd, &b, sizeof(b));
+    return 0;
+}
+
 int projection_mixed(Sim* s, int* status) {
-    const int NX = s->NX, NY = s->NY;
+    const int NX = s->NX, NY = s->NY, P = s->P;
     const size_t N = s->N;
     const unsigned nb = blocks_for(N, kT);
     Mixed32& m = s->m32;
     // the FP64 matrix, rhs, ||b||inf, p = 0, r = b (exactly the reference's)
     int rc = projection_build(s);
     if (rc) return rc;
-    FS2D_LAUNCH(s, k_mixed_matrix, nb, kT, 0, s->Adiag, s->Ax, s->Ay, m.a0, m.ax, m.ay, N);
+    FS2D_LAUNCH(s, k_mixed_matrix, nb, kT, 0, s->Adiag, s->Ax, s->Ay, m.a0, m.ax, m.ay, NX, P, N);
     {
-        MicFactor32 op{{m.a0, m.ax - 1, m.ay - 1, m.ay - NX, m.ax - NX}, m.pc, NX, (float)s->opt.mic_tau,
+        MicFactor32 op{{m.a0, m.ax - 1, m.ay - 1, m.ay - P, m.ax - P}, m.pc, P, (float)s->opt.mic_tau,
                        (float)s->opt.mic_sigma};
         rc = launch_wave2<MicFactor32, 2, 16>(s, op, WaveGeom{1, 1, 1, NX - 1, 1, NY - 1}, nullptr);
         if (rc) return rc;
     }
-    FS2D_LAUNCH(s, k_mixed_coef, nb, kT, 0, m.ax, m.ay, m.pc, m.fa, m.fb, m.fc, m.fd, NX, NY);
+    FS2D_LAUNCH(s, k_mixed_coef, nb, kT, 0, m.ax, m.ay, m.pc, m.fa, m.fb, m.fc, m.fd, NX, NY, P);
 
     PcgScalars* outer = s->pcg;     // rhs_norm, tol_abs from projection_build; r_norm = ||r64||
     PcgScalars* inner = s->pcg32;
     const int* done = &inner->done;
-    MicForward32 fwd{{m.rp, m.fa, m.fb}, m.q, NX};
-    MicBackward32 bwd{{m.q, m.pc, m.fc, m.fd}, m.z, NX};
-    const WaveGeom gf{1, 1, 1, NX - 1, 1, NY - 1};
-    const WaveGeom gb{-1, -1, 0, NX - 2, 0, NY - 2};
+    const Mic32Maps& fmaps = *reinterpret_cast<const Mic32Maps*>(s->m32maps->fwd);
+    const Mic32Maps& bmaps = *reinterpret_cast<const Mic32Maps*>(s->m32maps->bwd);
     const int max_iters = s->opt.pcg_max_iters;
     const int batch = 4;
     int total_iters = 0, outer_iters = 0, status_out = 0;
@@ -326,25 +375,25 @@ int projection_mixed(Sim* s, int* status) {
     if (rhs_norm > 1e-12) {
         for (outer_iters = 0; outer_iters < s->opt.ir_max_outer; outer_iters++) {
             if (r_norm <= tol_abs) break;
-            FS2D_LAUNCH(s, k_inner_init, nb, kT, 0, s->r, outer, m.pc, m.r, m.rp, m.e, N, inner);
-            rc = launch_wave2<MicForward32, 4, 16>(s, fwd, gf, done);
+            FS2D_LAUNCH(s, k_inner_init, nb, kT, 0, s->r, outer, m.pc, m.r, m.rp, m.e, NX, P, N, inner);
+            rc = launch_mic32<true>(s, fmaps, m.q, done);
             if (rc) return rc;
-            rc = launch_wave2<MicBackward32, 4, 16>(s, bwd, gb, done);
+            rc = launch_mic32<false>(s, bmaps, m.z, done);
             if (rc) return rc;
-            FS2D_LAUNCH(s, k_dot32, nb, kT, 0, m.z, m.r, N, s->partial, inner, 1, max_iters);
+            FS2D_LAUNCH(s, k_dot32, nb, kT, 0, m.z, m.r, NX, P, N, s->partial, inner, 1, max_iters);
             float* sbuf[2] = {m.s0, m.s1};
             for (int it = 0; it < max_iters; it++) {
                 float* s_old = sbuf[it & 1];
                 float* s_new = sbuf[(it + 1) & 1];
-                FS2D_LAUNCH(s, k_spmv32, nb, kT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, N,
+                FS2D_LAUNCH(s, k_spmv32, nb, kT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, P, N,
                             s->partial, inner);
-                FS2D_LAUNCH(s, k_axpy32, nb, kT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, N, s->partial, inner,
+                FS2D_LAUNCH(s, k_axpy32, nb, kT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, NX, P, N, s->partial, inner,
                             s->opt.ir_inner_tol);
-                rc = launch_wave2<MicForward32, 4, 16>(s, fwd, gf, done);
+                rc = launch_mic32<true>(s, fmaps, m.q, done);
                 if (rc) return rc;
-                rc = launch_wave2<MicBackward32, 4, 16>(s, bwd, gb, done);
+                rc = launch_mic32<false>(s, bmaps, m.z, done);
                 if (rc) return rc;
-                FS2D_LAUNCH(s, k_dot32, nb, kT, 0, m.z, m.r, N, s->partial, inner, 0, max_iters);
+                FS2D_LAUNCH(s, k_dot32, nb, kT, 0, m.z, m.r, NX, P, N, s->partial, inner, 0, max_iters);
                 if ((it + 1) % batch == 0 || it + 1 == max_iters) {
                     FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                               s->stream));
@@ -352,7 +401,7 @@ int projection_mixed(Sim* s, int* status) {
                     if (s->pcg32_host->done) break;
                 }
             }
-            FS2D_LAUNCH(s, k_update64, nb, kT, 0, s->p, m.e, outer, N);
+            FS2D_LAUNCH(s, k_update64, nb, kT, 0, s->p, m.e, outer, NX, P, N);
             FS2D_LAUNCH(s, k_resid64, nb, kT, 0, s->cell, s->Adiag, s->Ax, s->Ay, s->rhs, s->p, s->r, NX, N,
                         s->partial, outer);
             FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsign
     constexpr int RC = kW2Ring * kW2Tile;  // ring columns per row
     static_assert(kW2Tile % CH == 0 && kW2Publish % CH == 0 || CH % kW2Publish == 0, "chunking");
     if (skip != nullptr && *skip) return;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     const int ncols = g.i_hi - g.i_lo + 1;
