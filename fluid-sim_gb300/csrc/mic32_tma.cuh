@@ -57,6 +57,11 @@ struct Mic32Maps {
     CUtensorMap out_tail;
 };
 
+template <bool B>
+struct BoolTag {
+    static constexpr bool value = B;
+};
+
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
@@ -114,6 +119,8 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
     volatile int* top_ready = ctr + 2;      // top-row columns written to `top`
     volatile int* top_done = ctr + 3;       // top-row columns copied out and published
     volatile int* quit = ctr + 4;           // compute warp gave up (timeout)
+    volatile int* tiles_done = ctr + 5;     // tiles whose results are complete in shared memory
+    volatile int* tiles_freed = ctr + 6;    // tiles whose TMA store has finished reading shared memory
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(const_cast<int*>(ctr) + 8);
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -137,6 +144,8 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
         *top_ready = 0;
         *top_done = 0;
         *quit = 0;
+        *tiles_done = 0;
+        *tiles_freed = 0;
     }
     if (!below_in_grid) {
         for (int k = threadIdx.x; k < kM32BndChunks * kM32CH; k += blockDim.x) bnd[k] = 0.0f;
@@ -149,10 +158,31 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
         int hb = below_in_grid ? 0 : nchunks;    // next chunk of the row below to bring in
         int tc = 0;                              // top-row columns copied out
         const int tend = has_next ? ncols : 0;
+        int ts = 0;                              // next tile to store
         unsigned long long gavail = 0;
         long long idle = 0;
-        while (hb < nchunks || tc < tend) {
+        while (hb < nchunks || tc < tend || ts < nt) {
             bool moved = false;
+            if (ts < nt && *tiles_done > ts) {
+                // results of tile ts are complete (the compute warp fenced them
+                // for the async proxy before publishing tiles_done)
+                if (lane == 0) {
+                    const float* src = ring + (size_t)(ts & (kM32Slots - 1)) * kM32NA * kM32TileFloats;
+                    const int x = FWD ? ts * kM32Cols : P - (ts + 1) * kM32Cols;
+                    if (ybox >= 0) {
+                        tma_store_2d(&maps.out, x, ybox, src);
+                    } else {
+                        const int tail = NY % kM32Rows;
+                        tma_store_2d(&maps.out_tail, x, 0, src + (kM32Rows - tail) * kM32Cols);
+                    }
+                    bulk_commit();
+                    bulk_wait_read<0>();
+                    *tiles_freed = ts + 1;
+                }
+                __syncwarp();
+                ts++;
+                moved = true;
+            }
             if (hb < nchunks && hb < *bnd_used + kM32BndChunks - 1) {
                 const unsigned long long need = base + (unsigned long long)min((hb + 1) * kM32CH, ncols);
                 if (gavail < need) {
@@ -194,6 +224,8 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 break;
             }
         }
+        if (lane == 0) bulk_wait_all();
+        __syncwarp();
         return;
     }
 
@@ -223,6 +255,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
         }
     };
     auto spin_ge = [&](volatile int* flag, int need) {  // bounded wait on an I/O-warp counter
+        if (failed) return;  // after one timeout the results are invalid: do not wait again
         long long polls = 0;
         while (*flag < need) {
             if (++polls > 16 * kWaveSpinLimit) {
@@ -245,6 +278,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
         return slot_ptr(c >> 5) + row0 * kM32Cols + bc;
     };
     float o[4] = {0.f, 0.f, 0.f, 0.f};
+    float bn = 0.0f;         // lane 0's row-below value of the next step
     float vn[4][kM32NA];     // operands of the next step (loaded one step ahead)
     float* pn = nullptr;     // their address
     auto load_next = [&](float* p) {
@@ -254,18 +288,15 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             for (int a = 0; a < kM32NA; a++) vn[k][a] = p[k * rstep + a * kM32TileFloats];
     };
 
-    const int nsteps = ncols + 31;
-    int t = 0;
-    for (; t * kM32Cols < nsteps; t++) {
-        if (t < nt) wait_tile(t);
-        // top ring: do not run more than half a ring ahead of the I/O warp
-        if (has_next && t * kM32Cols - 31 - *top_done > kM32TopRing / 2) spin_ge(top_done, t * kM32Cols - 31 - kM32TopRing / 2);
-        __syncwarp();
-        const bool check = (t == 0) || (t >= nt);
+    // One tile of 32 steps.  CHECK: some lane's column may lie outside
+    // [0, ncols) (first and last tiles); a compile-time flag, so that the
+    // steady-state tiles carry no per-step range tests.
+    auto tile_steps = [&](int t, auto check_tag) {
+        constexpr bool check = decltype(check_tag)::value;
         {
             const int c0 = t * kM32Cols - lane;
             pn = cell_ptr(c0 < 0 ? 0 : c0);
-            load_next(pn);
+            load_next(pn);   // a tile starts on a chunk boundary: bn is read there
         }
 #pragma unroll
         for (int u = 0; u < kM32Cols; u++) {
@@ -277,6 +308,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 __threadfence_block();  // acquire: the chunk's values were written before bnd_ready
                 if (lane == 0) *bnd_used = h;
                 __syncwarp();
+                bn = bnd[(h % kM32BndChunks) * kM32CH];
             }
             float v[4][kM32NA];
 #pragma unroll
@@ -288,7 +320,9 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             pn = ((c + 1) & 31) ? p + cdir : cell_ptr(c + 1 < 0 ? 0 : c + 1);
             if (!check || (c + 1 >= 0 && c + 1 < ncols)) load_next(pn);
             float below = __shfl_up_sync(0xffffffffu, o[3], 1);
-            const float b0 = bnd[((s / kM32CH) % kM32BndChunks) * kM32CH + (s % kM32CH)];
+            const float b0 = bn;
+            // next step's row-below value (same chunk; a new chunk is read at its boundary)
+            if (((s + 1) % kM32CH) != 0) bn = bnd[((s / kM32CH) % kM32BndChunks) * kM32CH + ((s + 1) % kM32CH)];
             if (lane == 0) below = b0;
             if (!check || (c >= 0 && c < ncols)) {
                 float r[4];
@@ -311,29 +345,34 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 }
             }
         }
-        // tile t-1 is finished for every lane: store it, then reuse the slot of
-        // tile t-2 (stored one iteration ago) for tile t+2
+    };
+
+    const int nsteps = ncols + 31;
+    for (int t = 0; t * kM32Cols < nsteps; t++) {
+        if (t < nt) wait_tile(t);
+        // top ring: do not run more than half a ring ahead of the I/O warp
+        if (has_next && t * kM32Cols - 31 - *top_done > kM32TopRing / 2) spin_ge(top_done, t * kM32Cols - 31 - kM32TopRing / 2);
         __syncwarp();
+        if (t == 0 || t >= nt)
+            tile_steps(t, BoolTag<true>{});
+        else
+            tile_steps(t, BoolTag<false>{});
+        // tile t-1 is finished for every lane: hand it to the I/O warp for its
+        // TMA store; the slot of tile t-2 is reused for tile t+2 once that
+        // tile's store has read it
         if (t >= 1 && t - 1 < nt) {
             fence_async_smem();
             __syncwarp();
-            if (lane == 0) {
-                const float* src = slot_ptr(t - 1);
-                if (ybox >= 0) {
-                    tma_store_2d(&maps.out, tile_x(t - 1), ybox, src);
-                } else {
-                    const int tail = NY % kM32Rows;
-                    tma_store_2d(&maps.out_tail, tile_x(t - 1), 0, src + (kM32Rows - tail) * kM32Cols);
-                }
-                bulk_commit();
-                bulk_wait_read<1>();
-            }
-            __syncwarp();
+            if (lane == 0) *tiles_done = t;
         }
-        issue(t + 2);
+        if (t + 2 < nt) {
+            if (t >= 2 && *tiles_freed < t - 1) spin_ge(tiles_freed, t - 1);
+            __syncwarp();
+            issue(t + 2);
+        }
     }
-    if (lane == 0) bulk_wait_all();
     __syncwarp();
+    if (lane == 0) *tiles_done = nt;
     (void)failed;
 }
 

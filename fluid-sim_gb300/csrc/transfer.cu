@@ -332,41 +332,80 @@ __global__ void k_tile_max(const int2* __restrict__ tr, size_t n, unsigned int* 
 }
 
 // Layers [lo, hi] of one 32x32 tile, recomputed in shared memory inside a
-// halo of kBand cells.  Neighbours outside the region or the grid count as
-// absent; only region cells farther than kBand from the tile can be affected
-// by that, and none of them feeds a tile cell within the band.
+// halo of kBand cells.  Only region cells that can still reach the tile
+// within the band are recomputed: a cell of layer l at L1 distance d from the
+// tile feeds tile cells of layer >= l + d, so it is kept iff lo <= l <= hi and
+// d <= hi - l.  Every kept cell's lower-layer neighbours are either kept too
+// (their distance is at most d + 1 and their layer l - 1) or have a layer
+// below lo and are final in global memory; all of them lie inside the region
+// (d <= kBand - 1).  Kept cells are bucketed by layer, so each layer step
+// visits only its own front.  Layers are held relative to the band in one
+// byte: 0 below lo, 1 + (l - lo) inside, kBand + 1 above hi or unreachable.
+//
+// The mean divides by the neighbour count as the reference does; for counts
+// 1, 2 and 4 the quotient equals the product with the exact reciprocal (both
+// are the correctly rounded value of the same real number), so only a count
+// of 3 needs a division.
 __global__ void __launch_bounds__(256) k_extrap_band(double* a, const uint32_t* __restrict__ layer, int W, int H,
                                                      const int2* __restrict__ tile_range, int tiles_x, int lo, int hi) {
     __shared__ double val[kReg * kReg];
-    __shared__ uint32_t lay[kReg * kReg];
+    __shared__ unsigned char rel[kReg * kReg];
+    __shared__ unsigned short list[kReg * kReg];
+    __shared__ int cnt[kBand + 1], cur[kBand];
     int tx = blockIdx.x, ty = blockIdx.y;
     int2 tr = tile_range[(size_t)ty * tiles_x + tx];
     if (tr.y < lo || tr.x > hi) return;
-    int ox = tx * kTile - kBand, oy = ty * kTile - kBand;
+    const int ox = tx * kTile - kBand, oy = ty * kTile - kBand;
+    if (threadIdx.x <= kBand) cnt[threadIdx.x] = 0;
+    if (threadIdx.x < kBand) cur[threadIdx.x] = 0;
+    __syncthreads();
+    // L1 distance from region cell (rx, ry) to the output tile
+    auto tile_dist = [](int rx, int ry) {
+        int dx = rx < kBand ? kBand - rx : (rx >= kBand + kTile ? rx - (kBand + kTile - 1) : 0);
+        int dy = ry < kBand ? kBand - ry : (ry >= kBand + kTile ? ry - (kBand + kTile - 1) : 0);
+        return dx + dy;
+    };
     for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
         int rx = k % kReg, ry = k / kReg;
         int gx = ox + rx, gy = oy + ry;
+        uint32_t l = kUnknown;
+        double v = 0.0;
         if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
             size_t c = (size_t)gy * W + gx;
-            lay[k] = layer[c];
-            val[k] = a[c];
-        } else {
-            lay[k] = kUnknown;
-            val[k] = 0.0;
+            l = layer[c];
+            v = a[c];
         }
+        const int r = l < (uint32_t)lo ? 0 : (l <= (uint32_t)hi ? 1 + (int)(l - lo) : kBand + 1);
+        rel[k] = (unsigned char)r;
+        val[k] = v;
+        if (r >= 1 && r <= kBand && tile_dist(rx, ry) <= hi - lo + 1 - r) atomicAdd(&cnt[r], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int b = 1; b <= kBand; b++) cnt[b] += cnt[b - 1];   // cnt[b] = first slot of layer lo + b
+    __syncthreads();
+    for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
+        const int r = rel[k];
+        if (r >= 1 && r <= kBand && tile_dist(k % kReg, k / kReg) <= hi - lo + 1 - r)
+            list[cnt[r - 1] + atomicAdd(&cur[r - 1], 1)] = (unsigned short)k;
     }
     for (int L = lo; L <= hi; L++) {
         __syncthreads();
-        for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
-            if (lay[k] != (uint32_t)L) continue;
-            int rx = k % kReg, ry = k / kReg;
+        const int b = L - lo;
+        const int rl = b + 1;   // relative layer of L
+        for (int i = cnt[b] + threadIdx.x; i < cnt[b + 1]; i += blockDim.x) {
+            const int k = list[i];
             double sum = 0.0;
             int count = 0;
-            if (rx > 0 && lay[k - 1] < (uint32_t)L) { sum += val[k - 1]; count++; }
-            if (rx < kReg - 1 && lay[k + 1] < (uint32_t)L) { sum += val[k + 1]; count++; }
-            if (ry > 0 && lay[k - kReg] < (uint32_t)L) { sum += val[k - kReg]; count++; }
-            if (ry < kReg - 1 && lay[k + kReg] < (uint32_t)L) { sum += val[k + kReg]; count++; }
-            val[k] = count == 0 ? 0 : sum / count;
+            // neighbours in the reference's order: x-1, x+1, y-1, y+1
+            if (rel[k - 1] < rl) { sum += val[k - 1]; count++; }
+            if (rel[k + 1] < rl) { sum += val[k + 1]; count++; }
+            if (rel[k - kReg] < rl) { sum += val[k - kReg]; count++; }
+            if (rel[k + kReg] < rl) { sum += val[k + kReg]; count++; }
+            double r;
+            if (count == 3) r = sum / 3.0;
+            else r = sum * (count == 1 ? 1.0 : (count == 2 ? 0.5 : (count == 4 ? 0.25 : 0.0)));
+            val[k] = r;
         }
     }
     __syncthreads();
@@ -374,8 +413,8 @@ __global__ void __launch_bounds__(256) k_extrap_band(double* a, const uint32_t* 
         int rx = kBand + k % kTile, ry = kBand + k / kTile;
         int gx = ox + rx, gy = oy + ry;
         if (gx >= W || gy >= H) continue;
-        uint32_t l = lay[ry * kReg + rx];
-        if (l >= (uint32_t)lo && l <= (uint32_t)hi) a[(size_t)gy * W + gx] = val[ry * kReg + rx];
+        const int r = rel[ry * kReg + rx];
+        if (r >= 1 && r <= kBand) a[(size_t)gy * W + gx] = val[ry * kReg + rx];
     }
 }
 
