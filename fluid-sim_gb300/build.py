@@ -80,7 +80,7 @@ def build(force=False, verbose=False, extra=()):
         with ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             logs = list(ex.map(_run, jobs))
     if force or jobs or _stale(LIB, objs):
-        _run([nv, *ARCH, "-shared", "-o", LIB, *objs])
+        _run([nv, *ARCH, "-shared", "-Xlinker", "--no-undefined", "-o", LIB, *objs])
     return LIB, logs
 
 

@@ -6,6 +6,7 @@
 // loop order, so the same rand() state gives the same particles; every
 // stage then runs on the device.
 #include <cuda_runtime.h>
+#include <cudaTypedefs.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -86,6 +87,39 @@ void ktimer_collect(Sim* s) {
     s->kt_used = 0;
 }
 
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+int make_tensor_map_2d(CUtensorMap* map, void* base, CUtensorMapDataType dtype, int elem_bytes, int width,
+                       int height, int pitch_elems, int box_w, int box_h) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode();
+    if (!enc) {
+        set_error("cuTensorMapEncodeTiled is not available from the driver");
+        return FS2D_ERR_CUDA;
+    }
+    cuuint64_t dims[2] = {(cuuint64_t)width, (cuuint64_t)height};
+    cuuint64_t strides[1] = {(cuuint64_t)pitch_elems * (cuuint64_t)elem_bytes};
+    cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc(map, dtype, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                     CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+        return FS2D_ERR_CUDA;
+    }
+    return 0;
+}
+
 unsigned long long wave_begin(Sim* s) {
     // progress values are base + (columns done); columns < 2^24
     s->wave_launch++;
@@ -137,6 +171,9 @@ int alloc_particles(Sim* s, size_t cap) {
     if ((rc = dalloc(&s->vel, cap))) return rc;
     if ((rc = dalloc(&s->ent_u, 4 * cap))) return rc;
     if ((rc = dalloc(&s->ent_v, 4 * cap))) return rc;
+    cudaFree(s->pos_df);
+    s->pos_df = nullptr;
+    if ((rc = dalloc(&s->pos_df, std::max<size_t>(cap, 1)))) return rc;
     s->np_cap = cap;
     size_t need = std::max(std::max(s->N, std::max(s->NU, s->NV)), cap) / 32 + 4096;
     if (4 * need > s->partial_cap) {
@@ -160,7 +197,8 @@ int alloc_all(Sim* s) {
     A(v, NV);
     A(nu, NU);
     A(nv, NV);
-    A(t, N);
+    s->P = (s->NX + 31) / 32 * 32;
+    A(t, (size_t)s->P * s->NY);
     A(seed_key, N);
     A(phi_tmp, N);
     A(u0, NU);
@@ -196,11 +234,20 @@ int alloc_all(Sim* s) {
     A(pcg, 1);
     s->progress_cap = std::max(s->NX, s->NY) / 32 + 2;
     A(progress, (size_t)s->progress_cap);
+    A(cp_tab, (size_t)s->P + s->NY);
+    A(cpc, 1);
+    A(cp_hb_t, (size_t)s->progress_cap * s->P);
+    A(cp_hb_p, (size_t)s->progress_cap * s->P);
+    s->cpmaps = new (std::nothrow) CpMapsHost();
+    if (!s->cpmaps) {
+        set_error("out of host memory");
+        return FS2D_ERR_ALLOC;
+    }
+    if ((rc = cp_setup_maps(s))) return rc;
     A(stats, 1);
     A(err, 1);
     if (s->opt.precision == FS2D_PRECISION_MIXED) {
         Mixed32& m = s->m32;
-        s->P = (s->NX + 31) / 32 * 32;
         const size_t N = (size_t)s->P * s->NY;  // pitched FP32 arrays
         A(m32.a0, N);
         A(m32.ax, N);
@@ -246,12 +293,14 @@ void free_all(Sim* s) {
                     s->Adiag, s->Ax, s->Ay, s->rhs, s->precon, s->cfx, s->cfy, s->cbx, s->cby, s->r, s->z, s->q, s->w, s->s0,
                     s->s1, s->partial, s->pcg, s->progress, s->stats, s->err, s->m32.a0, s->m32.ax, s->m32.ay,
                     s->m32.pc, s->m32.fa, s->m32.fb, s->m32.fc, s->m32.fd, s->m32.r, s->m32.rp, s->m32.q,
-                    s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32};
+                    s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32, s->pos_df,
+                    s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->pcg_host) cudaFreeHost(s->pcg_host);
     if (s->pcg32_host) cudaFreeHost(s->pcg32_host);
     delete s->m32maps;
+    delete s->cpmaps;
     if (s->stats_host) cudaFreeHost(s->stats_host);
     if (s->err_host) cudaFreeHost(s->err_host);
     for (auto& e : s->ev)

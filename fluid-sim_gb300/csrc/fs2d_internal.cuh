@@ -15,7 +15,7 @@
 #include <utility>
 #include <vector>
 
-#include "../../include/fs2d.h"
+#include "fs2d.h"
 
 namespace fs2d {
 
@@ -67,6 +67,20 @@ struct Mic32MapsHost {
     alignas(64) unsigned char bwd[4 * 128 + 128];
 };
 
+// TMA descriptors of the closest-point sweeps (see cp_sweep.cuh).
+struct CpMapsHost {
+    alignas(64) unsigned char b[3 * 128];
+};
+// Constants of the FP32 closest-point decision (computed on the device per
+// level-set build, see cp_sweep.cuh).
+struct CpConst {
+    float A42;       // 2^-42 A, A >= every |coordinate| of particles and cell corners
+    float C0;        // 2^-80 A^2 + 2^-120
+    float tiny_q;    // >= 2^-20 dr^2
+    unsigned amax;   // bits of max |h| over particle coordinates (non-negative float)
+    int fast;        // 0: dr or A not finite/representable, every decision is exact
+};
+
 struct Sim {
     // configuration
     int NX = 0, NY = 0, ppc_sqrt = 0, mode = 0;
@@ -84,7 +98,13 @@ struct Sim {
     size_t np = 0, np_cap = 0;
 
     // level-set scratch
-    int* t = nullptr;                 // closest particle of each cell (-1 = none)
+    int* t = nullptr;                 // closest particle of each cell (-1 = none), row pitch P
+    float4* pos_df = nullptr;         // float-pair particle positions (np_cap)
+    float2* cp_tab = nullptr;         // float-pair corner coordinates: P columns, then NY rows
+    CpConst* cpc = nullptr;           // constants of the FP32 closest-point decision
+    int* cp_hb_t = nullptr;           // closest-point strip hand-off rows (progress_cap x P)
+    float4* cp_hb_p = nullptr;
+    CpMapsHost* cpmaps = nullptr;
     unsigned long long* seed_key = nullptr;
     double* phi_tmp = nullptr;
     uint8_t* surface = nullptr;
@@ -114,7 +134,7 @@ struct Sim {
     PcgScalars* pcg = nullptr;
     PcgScalars* pcg_host = nullptr;                  // pinned mirror for polling
     Mixed32 m32;                                     // MIXED precision only
-    int P = 0;                                       // row pitch of the FP32 arrays
+    int P = 0;                                       // row pitch of the pitched arrays (NX rounded up to 32)
     Mic32MapsHost* m32maps = nullptr;
     PcgScalars* pcg32 = nullptr;                     // inner FP32 solve scalars
     PcgScalars* pcg32_host = nullptr;
@@ -185,6 +205,10 @@ void ktimer_collect(Sim* s);  // after the stream drained
         if (_rc) return _rc;                                                          \
     } while (0)
 
+// 2D tensor map (TMA descriptor) of a pitched row-major array.
+int make_tensor_map_2d(CUtensorMap* map, void* base, CUtensorMapDataType dtype, int elem_bytes, int width,
+                       int height, int pitch_elems, int box_w, int box_h);
+
 inline unsigned int blocks_for(size_t n, int threads) { return (unsigned int)((n + threads - 1) / threads); }
 
 // ---- stage entry points (implemented in the per-stage .cu files) ----
@@ -196,6 +220,7 @@ int projection(Sim* s, int* status);      // applyProjection, FP64
 int projection_mixed(Sim* s, int* status);  // applyProjection, FP32 PCG in FP64 refinement
 int projection_build(Sim* s);             // FP64 matrix, rhs, p = 0, r = rhs, ||rhs||
 int mixed_setup_maps(Sim* s);             // TMA descriptors of the FP32 MIC(0) sweeps
+int cp_setup_maps(Sim* s);                // TMA descriptors of the closest-point sweeps
 int update_velocity(Sim* s);              // updateVelocity
 int g2p(Sim* s);                          // updateParticleVelocities
 int advect_particles(Sim* s);             // applyAdvection

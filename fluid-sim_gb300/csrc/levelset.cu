@@ -11,17 +11,23 @@
 //     integer image of d, then an atomic minimum of the particle index among
 //     the particles that reach it — the same (smallest d, then first index)
 //     winner as the reference's "if (d < phi)" loop;
-//   * every Gauss-Seidel sweep runs as a strip wavefront (wave_kernel),
-//     which visits each cell after exactly the neighbours the serial loop
-//     visits before it;
+//   * every Gauss-Seidel sweep runs as a strip wavefront, which visits each
+//     cell after exactly the neighbours the serial loop visits before it;
+//   * the closest-point sweeps carry the particle index alone and decide
+//     each "d(e) < phi" from FP32 squared distances with a rigorous error
+//     bound, falling back to the FP64 expression when the bound cannot
+//     decide (cp_sweep.cuh); phi = d(t) is evaluated once at the end;
 //   * a sweep that would change no cell is skipped: a parallel check first
 //     evaluates every cell's update against the current values, and if none
 //     would change, the serial sweep would not change anything either.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <limits.h>
+#include <string.h>
+#include <algorithm>
 #include "fs2d_device.cuh"
 #include "wave2.cuh"
+#include "cp_sweep.cuh"
 
 namespace fs2d {
 namespace {
@@ -30,23 +36,13 @@ __device__ __forceinline__ unsigned long long order_key(double d) {
     unsigned long long b = (unsigned long long)__double_as_longlong(d);
     return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
 }
-__device__ __forceinline__ double order_key_inv(unsigned long long k) {
-    unsigned long long b = (k >> 63) ? (k & 0x7FFFFFFFFFFFFFFFull) : ~k;
-    return __longlong_as_double((long long)b);
-}
-
-// d = |particle - cell corner (i dx, j dx)| - dr  (src/FluidSim2D.cpp:768,785)
-__device__ __forceinline__ double corner_dist(double2 p, int i, int j, double dx, double dr) {
-    double ax = p.x - i * dx, ay = p.y - j * dx;
-    return sqrt(ax * ax + ay * ay) - dr;
-}
-
-__global__ void k_seed_init(double* phi, int* t, unsigned long long* key, size_t n) {
+// Seeds (src/FluidSim2D.cpp:763-773).  t is pitched (row pitch P); the
+// padding columns stay -1.
+__global__ void k_seed_init(int* t, unsigned long long* key, int NX, int NY, int P) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (c >= n) return;
-    phi[c] = HUGE_VAL;
+    if (c >= (size_t)P * NY) return;
     t[c] = INT_MAX;
-    key[c] = ~0ull;
+    if (c < (size_t)NX * NY) key[c] = ~0ull;
 }
 
 __global__ void k_seed_min(const double2* __restrict__ pos, size_t np, unsigned long long* key, int NX, int NY,
@@ -60,106 +56,109 @@ __global__ void k_seed_min(const double2* __restrict__ pos, size_t np, unsigned 
 }
 
 __global__ void k_seed_idx(const double2* __restrict__ pos, size_t np, const unsigned long long* __restrict__ key,
-                           int* t, int NX, int NY, double dx, double dr) {
+                           int* t, int NX, int NY, int P, double dx, double dr) {
     size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (e >= np) return;
     double2 p = pos[e];
     int x = (int)(p.x / dx), y = (int)(p.y / dx);
     if (x < 0 || x >= NX || y < 0 || y >= NY) return;
-    size_t c = (size_t)y * NX + x;
-    if (order_key(corner_dist(p, x, y, dx, dr)) == key[c]) atomicMin(t + c, (int)e);
+    if (order_key(corner_dist(p, x, y, dx, dr)) == key[(size_t)y * NX + x]) atomicMin(t + (size_t)y * P + x, (int)e);
 }
 
-__global__ void k_seed_write(double* phi, int* t, const unsigned long long* __restrict__ key, size_t n) {
+__global__ void k_seed_write(int* t, size_t n) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (c >= n) return;
-    if (t[c] == INT_MAX) {
-        t[c] = -1;
-        phi[c] = HUGE_VAL;
-    } else {
-        phi[c] = order_key_inv(key[c]);
-    }
+    if (t[c] == INT_MAX) t[c] = -1;
 }
 
 // ---- closest-point propagation (the fastSweepIterate lambda) ----
 
-struct CPCarry {
-    int t;
-};
-
-// Candidate order of the reference: (i-1,j), (i+1,j), (i,j-1), (i,j+1); each
-// replaces the current value when strictly smaller.  A candidate equal to the
-// current particle gives the same d and never wins, so it is skipped.
-__device__ __forceinline__ void cp_candidate(int e, const double2* __restrict__ pos, int i, int j, double dx,
-                                             double dr, double& cur, int& ct) {
-    if (e != -1 && e != ct) {
-        double d = corner_dist(pos[e], i, j, dx, dr);
-        if (d < cur) {
-            cur = d;
-            ct = e;
-        }
-    }
+// Float-pair positions (h = nearest float, l = nearest float of the rest)
+// and the largest |h| over all particles.
+__device__ __forceinline__ float2 split_f2(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
 }
 
-struct ClosestPointOp {
-    static constexpr const char* kName = "wave_ClosestPointOp";
-    typedef CPCarry Carry;
-    double* phi;
-    int* t;
-    const double2* pos;
-    int NX, NY, sx, sy;
-    double dx, dr;
+__global__ void k_posdf(const double2* __restrict__ pos, size_t np, float4* pos_df, CpConst* kc) {
+    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    float m = 0.f;
+    if (e < np) {
+        const double2 p = pos[e];
+        const float2 x = split_f2(p.x), y = split_f2(p.y);
+        pos_df[e] = make_float4(x.x, x.y, y.x, y.y);
+        m = fmaxf(fabsf(x.x), fabsf(y.x));
+        if (!(m <= 3.0e38f)) m = INFINITY;   // NaN or overflow: no fast decisions
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.f) atomicMax(&kc->amax, __float_as_uint(m));
+}
 
-    __device__ void prefetch(int i, int j) const {
-        size_t c = (size_t)j * NX + i;
-        prefetch_l1(phi + c);
-        prefetch_l1(t + c);
-        if (j + sy >= 0 && j + sy < NY) prefetch_l1(t + (size_t)(j + sy) * NX + i);
-    }
-    __device__ Carry fetch(int i, int j, bool l2) const {
-        if (i < 0 || i >= NX || j < 0 || j >= NY) return Carry{-1};
-        const int* a = t + (size_t)j * NX + i;
-        return Carry{l2 ? __ldcg(a) : *a};
-    }
-    __device__ Carry update(int i, int j, Carry left, Carry below) const {
-        size_t c = (size_t)j * NX + i;
-        double cur = phi[c];
-        int ct = t[c];
-        const int cur_t0 = ct;
-        int tx_next = (i + sx >= 0 && i + sx < NX) ? t[c + sx] : -1;
-        int ty_next = (j + sy >= 0 && j + sy < NY) ? t[(size_t)(j + sy) * NX + i] : -1;
-        int tm = sx > 0 ? left.t : tx_next;
-        int tp = sx > 0 ? tx_next : left.t;
-        int td = sy > 0 ? below.t : ty_next;
-        int tu = sy > 0 ? ty_next : below.t;
-        cp_candidate(tm, pos, i, j, dx, dr, cur, ct);
-        cp_candidate(tp, pos, i, j, dx, dr, cur, ct);
-        cp_candidate(td, pos, i, j, dx, dr, cur, ct);
-        cp_candidate(tu, pos, i, j, dx, dr, cur, ct);
-        if (ct != cur_t0) {
-            phi[c] = cur;
-            t[c] = ct;
-        }
-        return Carry{ct};
-    }
-    static __device__ Carry shfl_up(Carry v) { return Carry{__shfl_up_sync(0xffffffffu, v.t, 1)}; }
-};
+// Corner coordinate tables and the constants of the FP32 decision.
+__global__ void k_cp_tabs(float2* xtab, float2* ytab, int P, int NY, double dx) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < P) xtab[k] = split_f2(k * dx);
+    if (k < NY) ytab[k] = split_f2(k * dx);
+}
 
-// Would any cell change under one closest-point update with the current values?
-__global__ void k_cp_check(const double* __restrict__ phi, const int* __restrict__ t,
-                           const double2* __restrict__ pos, int NX, int NY, double dx, double dr, int* noop) {
+__global__ void k_cp_const(CpConst* kc, int NX, int NY, double dx, double dr) {
+    const double grid = (double)(NX > NY ? NX : NY) * dx;
+    double A = fmax((double)__uint_as_float(kc->amax), grid) * (1.0 + 0x1p-20);
+    const bool ok = isfinite(dr) && isfinite(A) && A < 0x1p60;
+    kc->fast = ok ? 1 : 0;
+    if (!ok) A = 1.0;
+    kc->A42 = __double2float_ru(A * 0x1p-42);
+    kc->C0 = __double2float_ru(A * A * 0x1p-80 + 0x1p-120);
+    kc->tiny_q = ok ? __double2float_ru(dr * dr * 0x1p-20) : INFINITY;
+}
+
+// Would any cell change under one closest-point update with the current
+// values?  (Every candidate in the reference's order, against the cell's own.)
+__global__ void k_cp_check(const int* __restrict__ t, const float4* __restrict__ pos_df,
+                           const double2* __restrict__ pos, const float2* __restrict__ xtab,
+                           const float2* __restrict__ ytab, const CpConst* __restrict__ kcp, int NX, int NY, int P,
+                           double dx, double dr, int* noop) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= NX) return;
-    size_t c = (size_t)j * NX + i;
-    double cur = phi[c];
-    int ct = t[c];
-    const int t0 = ct;
-    cp_candidate(i > 0 ? t[c - 1] : -1, pos, i, j, dx, dr, cur, ct);
-    cp_candidate(i < NX - 1 ? t[c + 1] : -1, pos, i, j, dx, dr, cur, ct);
-    cp_candidate(j > 0 ? t[c - NX] : -1, pos, i, j, dx, dr, cur, ct);
-    cp_candidate(j < NY - 1 ? t[c + NX] : -1, pos, i, j, dx, dr, cur, ct);
-    if (ct != t0) *noop = 0;
+    const CpConst kc = *kcp;
+    const size_t c = (size_t)j * P + i;
+    const float2 xc = xtab[i], yc = ytab[j];
+    CpCur cur;
+    cur.t = t[c];
+    const int own = cur.t;
+    cur.q = cur.E = 0.f;
+    cur.p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (own >= 0) {
+        cur.p = pos_df[own];
+        cp_q32(cur.p, xc, yc, kc, cur.q, cur.E);
+    }
+    const int nb[4] = {i > 0 ? t[c - 1] : -1, i < NX - 1 ? t[c + 1] : -1, j > 0 ? t[c - P] : -1,
+                       j < NY - 1 ? t[c + P] : -1};
+    float4 np4[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) np4[k] = nb[k] >= 0 ? pos_df[nb[k]] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 own_p = cur.p;
+    bool und = false;
+#pragma unroll
+    for (int k = 0; k < 4; k++) cp_offer_fast(nb[k], np4[k], true, cur, xc, yc, kc, und);
+    if (und) {
+        float4 sp;
+        cur.t = cp_cell_slow(own, own_p, nb[0], np4[0], true, nb[1], np4[1], true, nb[2], np4[2], true, nb[3], np4[3],
+                             true, xc, yc, kc, pos, i, j, dx, dr, &sp);
+    }
+    if (cur.t != own) *noop = 0;
+}
+
+// phi = d(t) of every cell (HUGE_VAL without a particle), as the reference
+// stores it with t.
+__global__ void k_cp_phi(const int* __restrict__ t, const double2* __restrict__ pos, double* phi, int NX, int NY,
+                         int P, double dx, double dr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= NX) return;
+    const int e = t[(size_t)j * P + i];
+    phi[(size_t)j * NX + i] = e < 0 ? HUGE_VAL : corner_dist(pos[e], i, j, dx, dr);
 }
 
 // ---- redistance ----
@@ -305,23 +304,94 @@ __global__ void k_particle_energy(const double2* __restrict__ pos, const double2
 
 }  // namespace
 
+template <int SX, int SY>
+static int launch_cp_sweep_dir(Sim* s, const int* skip) {
+    const int nstrips = (s->NY + 31) / 32;
+    if (nstrips > s->progress_cap) {
+        set_error("closest-point sweep: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
+        return FS2D_ERR_INVALID;
+    }
+    static bool configured = false;
+    if (!configured) {
+        int rc0 = check_cuda(cudaFuncSetAttribute((const void*)cp_sweep_kernel<SX, SY>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCpSmem),
+                             "cudaFuncSetAttribute");
+        if (rc0) return rc0;
+        configured = true;
+    }
+    CpArgs a;
+    a.pos_df = s->pos_df;
+    a.pos = s->pos;
+    a.xtab = s->cp_tab;
+    a.ytab = s->cp_tab + s->P;
+    a.kc = s->cpc;
+    a.hb_t = s->cp_hb_t;
+    a.hb_p = s->cp_hb_p;
+    a.progress = s->progress;
+    a.base = wave_begin(s);
+    a.err = s->err;
+    a.skip = skip;
+    a.np = (int)s->np;
+    a.NX = s->NX;
+    a.NY = s->NY;
+    a.P = s->P;
+    a.dx = s->dx;
+    a.dr = s->dr;
+    const CpMaps* maps = reinterpret_cast<const CpMaps*>(s->cpmaps->b);
+    void* args[] = {(void*)maps, (void*)&a};
+    s->launches++;
+    long long kt = ktimer_begin(s, "cp_sweep");
+    int rc = check_cuda(cudaLaunchCooperativeKernel((const void*)cp_sweep_kernel<SX, SY>, dim3(nstrips), dim3(64),
+                                                    args, kCpSmem, s->stream),
+                        "cp_sweep");
+    ktimer_end(s, kt);
+    return rc;
+}
+
+static int launch_cp_sweep(Sim* s, int sx, int sy, const int* skip) {
+    if (sx > 0) return sy > 0 ? launch_cp_sweep_dir<1, 1>(s, skip) : launch_cp_sweep_dir<1, -1>(s, skip);
+    return sy > 0 ? launch_cp_sweep_dir<-1, 1>(s, skip) : launch_cp_sweep_dir<-1, -1>(s, skip);
+}
+
+// TMA descriptors of the closest-point sweeps over the pitched index array.
+int cp_setup_maps(Sim* s) {
+    static_assert(sizeof(CpMaps) <= sizeof(CpMapsHost::b), "tensor map storage");
+    CpMaps m{};
+    const int tail = s->NY % 32;
+    int rc = make_tensor_map_2d(&m.ld, s->t, CU_TENSOR_MAP_DATA_TYPE_INT32, 4, s->P, s->NY, s->P, kCpCols, kCpBoxRows);
+    if (!rc) rc = make_tensor_map_2d(&m.st, s->t, CU_TENSOR_MAP_DATA_TYPE_INT32, 4, s->P, s->NY, s->P, kCpCols, 32);
+    if (!rc)
+        rc = make_tensor_map_2d(&m.st_tail, s->t, CU_TENSOR_MAP_DATA_TYPE_INT32, 4, s->P, s->NY, s->P, kCpCols,
+                                tail > 0 ? tail : 32);
+    if (rc) return rc;
+    memcpy(s->cpmaps->b, &m, sizeof(m));
+    return 0;
+}
+
 int levelset_create(Sim* s) {
     const int NX = s->NX, NY = s->NY;
-    const size_t N = s->N;
     const int T = 256;
     // one extra int per sweep for the no-op flags, at the end of `partial`'s
     // companion: reuse the err-adjacent scratch in `max_layer`
     int* noop = (int*)s->max_layer + 4;
 
-    // constructFromParticles: seed
-    FS2D_LAUNCH(s, k_seed_init, blocks_for(N, T), T, 0, s->phi, s->t, s->seed_key, N);
+    const int P = s->P;
+    const size_t NP = (size_t)P * NY;
+    // constructFromParticles: seed (pitched t)
+    FS2D_LAUNCH(s, k_seed_init, blocks_for(NP, T), T, 0, s->t, s->seed_key, NX, NY, P);
     if (s->np > 0) {
         FS2D_LAUNCH(s, k_seed_min, blocks_for(s->np, T), T, 0, s->pos, s->np, s->seed_key, NX, NY, s->dx, s->dr,
                     s->err);
-        FS2D_LAUNCH(s, k_seed_idx, blocks_for(s->np, T), T, 0, s->pos, s->np, s->seed_key, s->t, NX, NY, s->dx,
+        FS2D_LAUNCH(s, k_seed_idx, blocks_for(s->np, T), T, 0, s->pos, s->np, s->seed_key, s->t, NX, NY, P, s->dx,
                     s->dr);
     }
-    FS2D_LAUNCH(s, k_seed_write, blocks_for(N, T), T, 0, s->phi, s->t, s->seed_key, N);
+    FS2D_LAUNCH(s, k_seed_write, blocks_for(NP, T), T, 0, s->t, NP);
+
+    // decision constants, float-pair positions and corner tables
+    FS2D_CUDA(cudaMemsetAsync(s->cpc, 0, sizeof(CpConst), s->stream));
+    if (s->np > 0) FS2D_LAUNCH(s, k_posdf, blocks_for(s->np, T), T, 0, s->pos, s->np, s->pos_df, s->cpc);
+    FS2D_LAUNCH(s, k_cp_tabs, blocks_for(std::max(P, NY), T), T, 0, s->cp_tab, s->cp_tab + P, P, NY, s->dx);
+    FS2D_LAUNCH(s, k_cp_const, 1, 1, 0, s->cpc, NX, NY, s->dx, s->dr);
 
     // fastSweepIterate: 4 x {(+,+), (-,+), (+,-), (-,-)}
     const int dirs[4][2] = {{1, 1}, {-1, 1}, {1, -1}, {-1, -1}};
@@ -329,13 +399,13 @@ int levelset_create(Sim* s) {
     for (int rep = 0; rep < 4; rep++) {
         for (int d = 0; d < 4; d++) {
             FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));  // -1 -> nonzero = no-op
-            FS2D_LAUNCH(s, k_cp_check, g2, 128, 0, s->phi, s->t, s->pos, NX, NY, s->dx, s->dr, noop);
-            ClosestPointOp op{s->phi, s->t, s->pos, NX, NY, dirs[d][0], dirs[d][1], s->dx, s->dr};
-            WaveGeom g{dirs[d][0], dirs[d][1], 0, NX - 1, 0, NY - 1};
-            int rc = launch_wave(s, op, g, noop);
+            FS2D_LAUNCH(s, k_cp_check, g2, 128, 0, s->t, s->pos_df, s->pos, s->cp_tab, s->cp_tab + P, s->cpc, NX, NY,
+                        P, s->dx, s->dr, noop);
+            int rc = launch_cp_sweep(s, dirs[d][0], dirs[d][1], noop);
             if (rc) return rc;
         }
     }
+    FS2D_LAUNCH(s, k_cp_phi, g2, 128, 0, s->t, s->pos, s->phi, NX, NY, P, s->dx, s->dr);
 
     // redistance
     FS2D_LAUNCH(s, k_surface, g2, 128, 0, s->phi, s->phi_tmp, NX, NY);

@@ -286,37 +286,8 @@ __global__ void k_update64(double* p, const float* __restrict__ e, const PcgScal
 
 }  // namespace
 
-static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
-    }
-    return fn;
-}
-
 int mic32_make_map(CUtensorMap* map, float* base, int P, int NY, int box_rows) {
-    PFN_cuTensorMapEncodeTiled_v12000 enc = get_encode();
-    if (!enc) {
-        set_error("cuTensorMapEncodeTiled is not available from the driver");
-        return FS2D_ERR_CUDA;
-    }
-    cuuint64_t dims[2] = {(cuuint64_t)P, (cuuint64_t)NY};
-    cuuint64_t strides[1] = {(cuuint64_t)P * sizeof(float)};
-    cuuint32_t box[2] = {(cuuint32_t)kM32Cols, (cuuint32_t)box_rows};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
-                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) {
-        set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
-        return FS2D_ERR_CUDA;
-    }
-    return 0;
+    return make_tensor_map_2d(map, base, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NY, P, kM32Cols, box_rows);
 }
 
 static_assert(sizeof(Mic32Maps) <= sizeof(Mic32MapsHost::fwd), "tensor map storage");

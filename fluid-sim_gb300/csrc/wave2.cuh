@@ -34,6 +34,7 @@
 #pragma once
 
 #include "fs2d_device.cuh"
+#include "tma.cuh"
 
 namespace fs2d {
 
@@ -50,9 +51,6 @@ __device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
     unsigned s = (unsigned)__cvta_generic_to_shared(smem);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(s), "l"(gmem) : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 template <typename T>
 __device__ __forceinline__ T ldcg_t(const T* p) { return __ldcg(p); }
