@@ -120,6 +120,47 @@ int make_tensor_map_2d(CUtensorMap* map, void* base, CUtensorMapDataType dtype, 
     return 0;
 }
 
+cudaError_t launch_clustered(const void* kernel, int nblocks, int cluster, int threads, size_t smem,
+                             cudaStream_t stream, void** args) {
+    if (cluster < 1) cluster = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((nblocks + cluster - 1) / cluster * cluster));
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute at[2];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    at[1].id = cudaLaunchAttributeClusterDimension;
+    at[1].val.clusterDim.x = (unsigned)cluster;
+    at[1].val.clusterDim.y = 1;
+    at[1].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = cluster > 1 ? 2 : 1;
+    return cudaLaunchKernelExC(&cfg, kernel, args);
+}
+
+int choose_cluster(const void* kernel, int nblocks, int threads, size_t smem) {
+    for (int cs = nblocks < 8 ? nblocks : 8; cs > 1; cs--) {
+        const int grid = (nblocks + cs - 1) / cs * cs;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3((unsigned)threads);
+        cfg.dynamicSmemBytes = smem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)cs;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, kernel, &cfg) == cudaSuccess && n * cs >= grid) return cs;
+        (void)cudaGetLastError();
+    }
+    return 1;
+}
+
 unsigned long long wave_begin(Sim* s) {
     // progress values are base + (columns done); columns < 2^24
     s->wave_launch++;
@@ -238,8 +279,11 @@ int alloc_all(Sim* s) {
     A(cpc, 1);
     A(cp_hb_t, (size_t)s->progress_cap * s->P);
     A(cp_hb_p, (size_t)s->progress_cap * s->P);
+    A(phi_p, (size_t)s->P * s->NY);
+    A(emask, (size_t)s->P * s->NY);
     s->cpmaps = new (std::nothrow) CpMapsHost();
-    if (!s->cpmaps) {
+    s->ekmaps = new (std::nothrow) CpMapsHost();
+    if (!s->cpmaps || !s->ekmaps) {
         set_error("out of host memory");
         return FS2D_ERR_ALLOC;
     }
@@ -294,13 +338,14 @@ void free_all(Sim* s) {
                     s->s1, s->partial, s->pcg, s->progress, s->stats, s->err, s->m32.a0, s->m32.ax, s->m32.ay,
                     s->m32.pc, s->m32.fa, s->m32.fb, s->m32.fc, s->m32.fd, s->m32.r, s->m32.rp, s->m32.q,
                     s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32, s->pos_df,
-                    s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p};
+                    s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p, s->phi_p, s->emask};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->pcg_host) cudaFreeHost(s->pcg_host);
     if (s->pcg32_host) cudaFreeHost(s->pcg32_host);
     delete s->m32maps;
     delete s->cpmaps;
+    delete s->ekmaps;
     if (s->stats_host) cudaFreeHost(s->stats_host);
     if (s->err_host) cudaFreeHost(s->err_host);
     for (auto& e : s->ev)

@@ -105,6 +105,9 @@ struct Sim {
     int* cp_hb_t = nullptr;           // closest-point strip hand-off rows (progress_cap x P)
     float4* cp_hb_p = nullptr;
     CpMapsHost* cpmaps = nullptr;
+    double* phi_p = nullptr;          // pitched level set of the Eikonal sweeps (P x NY)
+    uint8_t* emask = nullptr;         // Eikonal: cells whose update changes them (P x NY)
+    CpMapsHost* ekmaps = nullptr;     // TMA descriptors of the Eikonal sweeps
     unsigned long long* seed_key = nullptr;
     double* phi_tmp = nullptr;
     uint8_t* surface = nullptr;
@@ -136,6 +139,7 @@ struct Sim {
     Mixed32 m32;                                     // MIXED precision only
     int P = 0;                                       // row pitch of the pitched arrays (NX rounded up to 32)
     Mic32MapsHost* m32maps = nullptr;
+    int m32_cluster = 0;                             // cluster size of the FP32 MIC(0) sweeps (0: not chosen)
     PcgScalars* pcg32 = nullptr;                     // inner FP32 solve scalars
     PcgScalars* pcg32_host = nullptr;
 
@@ -208,6 +212,14 @@ void ktimer_collect(Sim* s);  // after the stream drained
 // 2D tensor map (TMA descriptor) of a pitched row-major array.
 int make_tensor_map_2d(CUtensorMap* map, void* base, CUtensorMapDataType dtype, int elem_bytes, int width,
                        int height, int pitch_elems, int box_w, int box_h);
+
+// Cooperative launch of `nblocks` blocks (rounded up to whole clusters of
+// `cluster` blocks when cluster > 1).
+cudaError_t launch_clustered(const void* kernel, int nblocks, int cluster, int threads, size_t smem,
+                             cudaStream_t stream, void** args);
+// Largest cluster size (<= 8) with which every cluster of a grid of
+// `nblocks` blocks can be co-resident; 1 when clusters are not usable.
+int choose_cluster(const void* kernel, int nblocks, int threads, size_t smem);
 
 inline unsigned int blocks_for(size_t n, int threads) { return (unsigned int)((n + threads - 1) / threads); }
 

@@ -28,6 +28,7 @@
 #include "fs2d_device.cuh"
 #include "wave2.cuh"
 #include "cp_sweep.cuh"
+#include "eik_sweep.cuh"
 
 namespace fs2d {
 namespace {
@@ -166,7 +167,7 @@ __global__ void k_cp_phi(const int* __restrict__ t, const double2* __restrict__ 
 // Surface flags from the sign changes the reference tests
 // (src/FluidSim2D.cpp:803-834: pairs with the base cell in [0,NX-2]x[0,NY-2]),
 // then non-surface negative cells -> -inf (:836-842).  Reads phi, writes out.
-__global__ void k_surface(const double* __restrict__ phi, double* out, int NX, int NY) {
+__global__ void k_surface(const double* __restrict__ phi, double* out, int NX, int NY, int P) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= NX) return;
@@ -177,7 +178,7 @@ __global__ void k_surface(const double* __restrict__ phi, double* out, int NX, i
     if (i >= 1 && j <= NY - 2 && phi[c - 1] * p < 0) surf = true;
     if (i <= NX - 2 && j <= NY - 2 && p * phi[c + NX] < 0) surf = true;
     if (i <= NX - 2 && j >= 1 && phi[c - NX] * p < 0) surf = true;
-    out[c] = (!surf && p < 0) ? -HUGE_VAL : p;
+    out[(size_t)j * P + i] = (!surf && p < 0) ? -HUGE_VAL : p;
 }
 
 // One Eikonal update (src/FluidSim2D.cpp:848-857); a = upwind x neighbour,
@@ -192,45 +193,35 @@ __device__ __forceinline__ double eikonal(double own, double a, double b, double
     return (d < -own) ? -d : own;
 }
 
-struct Eikonal64 {
-    static constexpr const char* kName = "wave2_Eikonal64";
-    typedef double T;
-    static constexpr int NA = 1;
-    const double* in[1];  // phi before the sweep (the output array itself)
-    double* out;
-    int pitch;
-    double dx;
-    __device__ double stored(const double*, double r) const { return r; }
-    __device__ double border(int i, int j) const { return out[(size_t)j * pitch + i]; }
-    __device__ double compute(const double* v, double left, double below, int, int) const {
-        return eikonal(v[0], left, below, dx);
-    }
-};
 
-__global__ void k_eik_check(const double* __restrict__ phi, int NX, int i_lo, int i_hi, int j_lo, int j_hi, int sx,
-                            int sy, double dx, int* noop) {
+__global__ void k_eik_check(const double* __restrict__ phi, uint8_t* mask, int P, int i_lo, int i_hi, int j_lo,
+                            int j_hi, int sx, int sy, double dx, int* noop) {
     int i = i_lo + blockIdx.x * blockDim.x + threadIdx.x;
     int j = j_lo + blockIdx.y;
     if (i > i_hi || j > j_hi) return;
-    size_t c = (size_t)j * NX + i;
+    size_t c = (size_t)j * P + i;
     double own = phi[c];
-    if (own >= 0) return;
-    double nv = eikonal(own, phi[c - sx], phi[(size_t)(j - sy) * NX + i], dx);
-    if (nv != own) *noop = 0;
+    bool ch = false;
+    if (own < 0) {
+        double nv = eikonal(own, phi[c - sx], phi[(size_t)(j - sy) * P + i], dx);
+        ch = nv != own;
+    }
+    mask[c] = ch ? 1 : 0;
+    if (ch) *noop = 0;
 }
 
 // Min-smoothing pass (src/FluidSim2D.cpp:904-919): Jacobi, interior cells.
-__global__ void k_smooth(const double* __restrict__ oldp, double* out, int NX, int NY) {
+__global__ void k_smooth(const double* __restrict__ oldp, int pin, double* out, int NX, int NY) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= NX) return;
-    size_t c = (size_t)j * NX + i;
+    size_t c = (size_t)j * pin + i;
     double o = oldp[c];
     if (i >= 1 && i <= NX - 2 && j >= 1 && j <= NY - 2) {
-        double avg = 0.25 * (oldp[c - 1] + oldp[c + 1] + oldp[c - NX] + oldp[c + NX]);
+        double avg = 0.25 * (oldp[c - 1] + oldp[c + 1] + oldp[c - pin] + oldp[c + pin]);
         if (avg < o) o = avg;
     }
-    out[c] = o;
+    out[(size_t)j * NX + i] = o;
 }
 
 // Labels (src/FluidSim2D.cpp:657-664) and grid statistics (:709-722).
@@ -348,6 +339,52 @@ static int launch_cp_sweep_dir(Sim* s, const int* skip) {
     return rc;
 }
 
+template <int SX, int SY>
+static int launch_eik_sweep_dir(Sim* s, const WaveGeom& g, const int* skip) {
+    const int nstrips = (s->NY + kEkRows - 1) / kEkRows;
+    if (nstrips > s->progress_cap) {
+        set_error("Eikonal sweep: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
+        return FS2D_ERR_INVALID;
+    }
+    static bool configured = false;
+    if (!configured) {
+        int rc0 = check_cuda(cudaFuncSetAttribute((const void*)eik_sweep_kernel<SX, SY>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEkSmem),
+                             "cudaFuncSetAttribute");
+        if (rc0) return rc0;
+        configured = true;
+    }
+    EkArgs a;
+    a.hb = reinterpret_cast<double2*>(s->cp_hb_p);
+    a.progress = s->progress;
+    a.base = wave_begin(s);
+    a.err = s->err;
+    a.skip = skip;
+    a.NX = s->NX;
+    a.NY = s->NY;
+    a.P = s->P;
+    a.i_lo = g.i_lo;
+    a.i_hi = g.i_hi;
+    a.j_lo = g.j_lo;
+    a.j_hi = g.j_hi;
+    a.dx = s->dx;
+    a.c2 = 2 * s->dx * s->dx;
+    const EkMaps* maps = reinterpret_cast<const EkMaps*>(s->ekmaps->b);
+    void* args[] = {(void*)maps, (void*)&a};
+    s->launches++;
+    long long kt = ktimer_begin(s, "eik_sweep");
+    int rc = check_cuda(cudaLaunchCooperativeKernel((const void*)eik_sweep_kernel<SX, SY>, dim3(nstrips), dim3(64),
+                                                    args, kEkSmem, s->stream),
+                        "eik_sweep");
+    ktimer_end(s, kt);
+    return rc;
+}
+
+static int launch_eik_sweep(Sim* s, const WaveGeom& g, const int* skip) {
+    if (g.sx > 0) return g.sy > 0 ? launch_eik_sweep_dir<1, 1>(s, g, skip) : launch_eik_sweep_dir<1, -1>(s, g, skip);
+    return g.sy > 0 ? launch_eik_sweep_dir<-1, 1>(s, g, skip) : launch_eik_sweep_dir<-1, -1>(s, g, skip);
+}
+
 static int launch_cp_sweep(Sim* s, int sx, int sy, const int* skip) {
     if (sx > 0) return sy > 0 ? launch_cp_sweep_dir<1, 1>(s, skip) : launch_cp_sweep_dir<1, -1>(s, skip);
     return sy > 0 ? launch_cp_sweep_dir<-1, 1>(s, skip) : launch_cp_sweep_dir<-1, -1>(s, skip);
@@ -365,6 +402,17 @@ int cp_setup_maps(Sim* s) {
                                 tail > 0 ? tail : 32);
     if (rc) return rc;
     memcpy(s->cpmaps->b, &m, sizeof(m));
+    static_assert(sizeof(EkMaps) <= sizeof(CpMapsHost::b), "tensor map storage");
+    EkMaps e{};
+    rc = make_tensor_map_2d(&e.ld, s->phi_p, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, s->P, s->NY, s->P, kEkCols, kEkRows);
+    if (!rc)
+        rc = make_tensor_map_2d(&e.st_tail, s->phi_p, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 8, s->P, s->NY, s->P, kEkCols,
+                                tail > 0 ? tail : kEkRows);
+    if (!rc)
+        rc = make_tensor_map_2d(&e.mask, s->emask, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, s->P, s->NY, s->P, kEkCols,
+                                kEkRows);
+    if (rc) return rc;
+    memcpy(s->ekmaps->b, &e, sizeof(e));
     return 0;
 }
 
@@ -407,8 +455,8 @@ int levelset_create(Sim* s) {
     }
     FS2D_LAUNCH(s, k_cp_phi, g2, 128, 0, s->t, s->pos, s->phi, NX, NY, P, s->dx, s->dr);
 
-    // redistance
-    FS2D_LAUNCH(s, k_surface, g2, 128, 0, s->phi, s->phi_tmp, NX, NY);
+    // redistance on the pitched copy phi_p
+    FS2D_LAUNCH(s, k_surface, g2, 128, 0, s->phi, s->phi_p, NX, NY, P);
     for (int rep = 0; rep < 4; rep++) {
         for (int d = 0; d < 4; d++) {
             int sx = dirs[d][0], sy = dirs[d][1];
@@ -416,15 +464,15 @@ int levelset_create(Sim* s) {
             int j_lo = sy > 0 ? 1 : 0, j_hi = sy > 0 ? NY - 1 : NY - 2;
             FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));
             dim3 gc(blocks_for(i_hi - i_lo + 1, 128), j_hi - j_lo + 1);
-            FS2D_LAUNCH(s, k_eik_check, gc, 128, 0, s->phi_tmp, NX, i_lo, i_hi, j_lo, j_hi, sx, sy, s->dx, noop);
-            Eikonal64 op{{s->phi_tmp}, s->phi_tmp, NX, s->dx};
+            FS2D_LAUNCH(s, k_eik_check, gc, 128, 0, s->phi_p, s->emask, P, i_lo, i_hi, j_lo, j_hi, sx, sy, s->dx,
+                        noop);
             WaveGeom g{sx, sy, i_lo, i_hi, j_lo, j_hi};
-            int rc = launch_wave2<Eikonal64, 2, 8>(s, op, g, noop);
+            int rc = launch_eik_sweep(s, g, noop);
             if (rc) return rc;
         }
     }
-    FS2D_LAUNCH(s, k_smooth, g2, 128, 0, s->phi_tmp, s->phi, NX, NY);
-    FS2D_LAUNCH(s, k_smooth, g2, 128, 0, s->phi, s->phi_tmp, NX, NY);
+    FS2D_LAUNCH(s, k_smooth, g2, 128, 0, s->phi_p, P, s->phi, NX, NY);
+    FS2D_LAUNCH(s, k_smooth, g2, 128, 0, s->phi, NX, s->phi_tmp, NX, NY);
 
     // labels + statistics (phi_tmp -> phi)
     FS2D_LAUNCH(s, k_labels_stats, g2, 128, 0, s->phi_tmp, s->phi, s->cell, s->u, s->v, NX, NY, s->dx, s->rho, s->gx,

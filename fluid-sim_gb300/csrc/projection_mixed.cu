@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <string.h>
+#include <algorithm>
 #include <cudaTypedefs.h>
 #include "fs2d_device.cuh"
 #include "wave2.cuh"
@@ -57,18 +58,6 @@ __device__ __forceinline__ DF df_warp_sum(DF v) {
     return v;
 }
 // Block sum of per-thread products as FP64 (valid in thread 0).
-__device__ __forceinline__ double block_dot(DF v, double* sh) {
-    v = df_warp_sum(v);
-    double d = (double)v.hi + (double)v.lo;
-    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) sh[wid] = d;
-    __syncthreads();
-    int nw = (blockDim.x + 31) >> 5;
-    d = (threadIdx.x < nw) ? sh[threadIdx.x] : 0.0;
-    if (wid == 0) d = warp_sum(d);
-    return d;
-}
 
 // FP32 copies of the FP64 matrix in the pitched layout (Adiag keeps its
 // -0.0 non-fluid marker).
@@ -179,22 +168,73 @@ __global__ void k_inner_init(const double* __restrict__ r64, const PcgScalars* _
     }
 }
 
-__global__ void k_dot32(const float* __restrict__ z, const float* __restrict__ r, int NX, int P, size_t N,
-                        double* partial, PcgScalars* pcg, int init, int max_iters) {
-    __shared__ double sh[32];
-    if (pcg->done) return;
-    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    DF a{0.f, 0.f};
-    if (c < N) {
-        size_t k = (c / NX) * (size_t)P + (c % NX);
-        a = df_prod(z[k], r[k]);
+// ---- inner FP32 PCG kernels ----
+// Row-segment layout: block (bx, by) covers columns bx*kRT .. bx*kRT+kRT-1
+// of rows by, by + gridDim.y, ...; sums are accumulated and reduced in
+// double-float (FP32 pairs), in a fixed order (deterministic), and the
+// last block finishes the scalar.
+constexpr int kRT = 256;
+
+__device__ __forceinline__ void df_block_partial(DF v, float2* partial, float2* sh) {
+    v = df_warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = make_float2(v.hi, v.lo);
+    __syncthreads();
+    if (wid == 0) {
+        DF t = lane < nw ? DF{sh[lane].x, sh[lane].y} : DF{0.f, 0.f};
+        t = df_warp_sum(t);
+        if (lane == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = make_float2(t.hi, t.lo);
     }
-    double d = block_dot(a, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = d;
+}
+
+// Sum of the partials of every block (called by the last block).
+__device__ __forceinline__ double df_final(const float2* partial, int n, float2* sh) {
+    DF acc{0.f, 0.f};
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const float2 v = partial[k];
+        df_add(acc, DF{v.x, v.y});
+    }
+    acc = df_warp_sum(acc);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = make_float2(acc.hi, acc.lo);
+    __syncthreads();
+    DF t = (wid == 0 && lane < nw) ? DF{sh[lane].x, sh[lane].y} : DF{0.f, 0.f};
+    if (wid == 0) t = df_warp_sum(t);
+    return (double)t.hi + (double)t.lo;
+}
+
+__device__ __forceinline__ float block_max_f(float v, float* sh) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    v = lane < nw ? sh[lane] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(kRT) k_dot32(const float* __restrict__ z, const float* __restrict__ r, int NX,
+                                               int NY, int P, float2* partial, PcgScalars* pcg, int init,
+                                               int max_iters) {
+    __shared__ float2 sh[32];
+    if (pcg->done) return;
+    const int i = blockIdx.x * kRT + threadIdx.x;
+    DF a{0.f, 0.f};
+    if (i < NX) {
+#pragma unroll 4
+        for (int j = blockIdx.y; j < NY; j += gridDim.y) {
+            const size_t k = (size_t)j * P + i;
+            df_add(a, df_prod(z[k], r[k]));
+        }
+    }
+    df_block_partial(a, partial, sh);
     if (last_block(&pcg->ticket[1])) {
-        double s = 0;
-        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) s += partial[k];
-        s = block_sum(s, sh);
+        const double s = df_final(partial, gridDim.x * gridDim.y, sh);
         if (threadIdx.x == 0) {
             if (init) {
                 pcg->sigma = s;
@@ -209,67 +249,73 @@ __global__ void k_dot32(const float* __restrict__ z, const float* __restrict__ r
     }
 }
 
-__global__ void k_spmv32(const uint8_t* __restrict__ cell, const float* __restrict__ a0,
-                         const float* __restrict__ ax, const float* __restrict__ ay, const float* __restrict__ z,
-                         const float* __restrict__ s_old, float* s_new, float* w, int NX, int P, size_t N,
-                         double* partial, PcgScalars* pcg) {
-    __shared__ double sh[32];
+// s_new = z + beta s_old (z on the first iteration), w = A s_new on fluid
+// cells, alpha = sigma / (w . s_new).
+__global__ void __launch_bounds__(kRT) k_spmv32(const uint8_t* __restrict__ cell, const float* __restrict__ a0,
+                                                const float* __restrict__ ax, const float* __restrict__ ay,
+                                                const float* __restrict__ z, const float* __restrict__ s_old,
+                                                float* s_new, float* w, int NX, int NY, int P, float2* partial,
+                                                PcgScalars* pcg) {
+    __shared__ float2 sh[32];
     if (pcg->done) return;
     const bool first = pcg->first != 0;
     const float beta = (float)pcg->beta;
-    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * kRT + threadIdx.x;
     DF a{0.f, 0.f};
-    if (c < N) {
-        size_t k = (c / NX) * (size_t)P + (c % NX);
-        float sc = first ? z[k] : fmaf(beta, s_old[k], z[k]);
-        s_new[k] = sc;
-        float out = 0.0f;
-        if (cell[c] == kFluid) {
-            float sl = first ? z[k - 1] : fmaf(beta, s_old[k - 1], z[k - 1]);
-            float sr = first ? z[k + 1] : fmaf(beta, s_old[k + 1], z[k + 1]);
-            float sd = first ? z[k - P] : fmaf(beta, s_old[k - P], z[k - P]);
-            float su = first ? z[k + P] : fmaf(beta, s_old[k + P], z[k + P]);
-            out = a0[k] * sc + ax[k - 1] * sl + ax[k] * sr + ay[k - P] * sd + ay[k] * su;
+    if (i < NX) {
+        for (int j = blockIdx.y; j < NY; j += gridDim.y) {
+            const size_t k = (size_t)j * P + i;
+            const float sc = first ? z[k] : fmaf(beta, s_old[k], z[k]);
+            s_new[k] = sc;
+            float out = 0.0f;
+            if (cell[(size_t)j * NX + i] == kFluid) {
+                const float sl = first ? z[k - 1] : fmaf(beta, s_old[k - 1], z[k - 1]);
+                const float sr = first ? z[k + 1] : fmaf(beta, s_old[k + 1], z[k + 1]);
+                const float sd = first ? z[k - P] : fmaf(beta, s_old[k - P], z[k - P]);
+                const float su = first ? z[k + P] : fmaf(beta, s_old[k + P], z[k + P]);
+                out = a0[k] * sc + ax[k - 1] * sl + ax[k] * sr + ay[k - P] * sd + ay[k] * su;
+            }
+            w[k] = out;
+            df_add(a, df_prod(out, sc));
         }
-        w[k] = out;
-        a = df_prod(out, sc);
     }
-    double d = block_dot(a, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = d;
+    df_block_partial(a, partial, sh);
     if (last_block(&pcg->ticket[2])) {
-        double s = 0;
-        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) s += partial[k];
-        s = block_sum(s, sh);
+        const double sum = df_final(partial, gridDim.x * gridDim.y, sh);
         if (threadIdx.x == 0) {
-            if (s == 0.0) pcg->done = 1;
-            else pcg->alpha = pcg->sigma / s;
+            if (sum == 0.0) pcg->done = 1;
+            else pcg->alpha = pcg->sigma / sum;
         }
     }
 }
 
-__global__ void k_axpy32(float* e, float* r, float* rp, const float* __restrict__ pc, const float* __restrict__ s,
-                         const float* __restrict__ w, int NX, int P, size_t N, double* partial, PcgScalars* pcg,
-                         double inner_tol) {
-    __shared__ double sh[32];
+// e += alpha s, r -= alpha w, rp = r pc^2, ||r||inf (stop when below inner_tol).
+__global__ void __launch_bounds__(kRT) k_axpy32(float* e, float* r, float* rp, const float* __restrict__ pc,
+                                                const float* __restrict__ s, const float* __restrict__ w, int NX,
+                                                int NY, int P, float* partial, PcgScalars* pcg, double inner_tol) {
+    __shared__ float sh[32];
     if (pcg->done) return;
     const float alpha = (float)pcg->alpha;
-    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    double m = 0;
-    if (c < N) {
-        size_t k = (c / NX) * (size_t)P + (c % NX);
-        e[k] = fmaf(alpha, s[k], e[k]);
-        float rv = fmaf(-alpha, w[k], r[k]);
-        r[k] = rv;
-        float p = pc[k];
-        rp[k] = rv * (p * p);
-        m = fabsf(rv);
+    const int i = blockIdx.x * kRT + threadIdx.x;
+    float m = 0.f;
+    if (i < NX) {
+#pragma unroll 2
+        for (int j = blockIdx.y; j < NY; j += gridDim.y) {
+            const size_t k = (size_t)j * P + i;
+            e[k] = fmaf(alpha, s[k], e[k]);
+            const float rv = fmaf(-alpha, w[k], r[k]);
+            r[k] = rv;
+            const float p = pc[k];
+            rp[k] = rv * (p * p);
+            m = fmaxf(m, fabsf(rv));
+        }
     }
-    m = block_max(m, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+    m = block_max_f(m, sh);
+    if (threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = m;
     if (last_block(&pcg->ticket[3])) {
-        double mm = 0;
-        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) mm = fmax(mm, partial[k]);
-        mm = block_max(mm, sh);
+        float mm = 0.f;
+        for (int k = threadIdx.x; k < (int)(gridDim.x * gridDim.y); k += blockDim.x) mm = fmaxf(mm, partial[k]);
+        mm = block_max_f(mm, sh);
         if (threadIdx.x == 0) {
             pcg->r_norm = mm;
             if (mm <= inner_tol) pcg->done = 1;
@@ -336,6 +382,11 @@ int projection_mixed(Sim* s, int* status) {
     const Mic32Maps& bmaps = *reinterpret_cast<const Mic32Maps*>(s->m32maps->bwd);
     const int max_iters = s->opt.pcg_max_iters;
     const int batch = 4;
+    // inner kernels: ~8 blocks per SM of row segments
+    const int gx = (NX + kRT - 1) / kRT;
+    const dim3 rg(gx, std::max(1, std::min(NY, 1216 / gx)));
+    float2* part2 = reinterpret_cast<float2*>(s->partial);
+    float* partf = reinterpret_cast<float*>(s->partial);
     int total_iters = 0, outer_iters = 0, status_out = 0;
 
     FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, outer, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
@@ -351,20 +402,20 @@ int projection_mixed(Sim* s, int* status) {
             if (rc) return rc;
             rc = launch_mic32<false>(s, bmaps, m.z, done);
             if (rc) return rc;
-            FS2D_LAUNCH(s, k_dot32, nb, kT, 0, m.z, m.r, NX, P, N, s->partial, inner, 1, max_iters);
+            FS2D_LAUNCH(s, k_dot32, rg, kRT, 0, m.z, m.r, NX, NY, P, part2, inner, 1, max_iters);
             float* sbuf[2] = {m.s0, m.s1};
             for (int it = 0; it < max_iters; it++) {
                 float* s_old = sbuf[it & 1];
                 float* s_new = sbuf[(it + 1) & 1];
-                FS2D_LAUNCH(s, k_spmv32, nb, kT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, P, N,
-                            s->partial, inner);
-                FS2D_LAUNCH(s, k_axpy32, nb, kT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, NX, P, N, s->partial, inner,
+                FS2D_LAUNCH(s, k_spmv32, rg, kRT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, NY, P,
+                            part2, inner);
+                FS2D_LAUNCH(s, k_axpy32, rg, kRT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, NX, NY, P, partf, inner,
                             s->opt.ir_inner_tol);
                 rc = launch_mic32<true>(s, fmaps, m.q, done);
                 if (rc) return rc;
                 rc = launch_mic32<false>(s, bmaps, m.z, done);
                 if (rc) return rc;
-                FS2D_LAUNCH(s, k_dot32, nb, kT, 0, m.z, m.r, NX, P, N, s->partial, inner, 0, max_iters);
+                FS2D_LAUNCH(s, k_dot32, rg, kRT, 0, m.z, m.r, NX, NY, P, part2, inner, 0, max_iters);
                 if ((it + 1) % batch == 0 || it + 1 == max_iters) {
                     FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
                                               s->stream));
