@@ -9,9 +9,11 @@ dt = 1/960, pressure solve MIC(0)-PCG to a relative residual of 1e-6
 Seeded synthetic input (the reference ships no datasets).
 
 A step is one FluidSim2D::runFrame (all eight stages).  Metric: grid-cell
-steps/s = NX * NY * steps / time.
+steps/s = NX * NY * steps / time.  The headline runs the mixed-precision
+projection (FP32 MIC(0)-PCG inside FP64 iterative refinement, the same FP64
+stopping test); the all-FP64 GPU path is measured beside it ("fp64_path").
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|mixed]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
   python bench.py --impl reference ...   # the reference's CPU path (oracle port)
 
 One JSON line is printed by rank 0.  Multi-GPU runs are independent
@@ -35,10 +37,18 @@ METRIC = "grid-cell steps/s at 1024^2 (PIC/FLIP step, MIC(0)-PCG to 1e-6 rel res
 UNIT = "grid-cell steps/s"
 SEED = 12345
 FLUSH_BYTES = 256 << 20          # > 129 MB L2
-DOMINANT = ("wave2_MicForward64", "wave2_MicBackward64", "wave2_MicForward32", "wave2_MicBackward32")
-# algorithmic bytes per cell of one MIC(0) triangular solve: read r (or q),
-# two coefficients and precon, write q (or z): 5 values of b bytes
-MIC_VALUES_PER_CELL = 5
+# kernels timed per launch during the timed region, with their algorithmic
+# bytes per grid cell and launch:
+#   mic32_*: FP32 MIC(0) solve, read the right-hand side and two folded
+#            coefficients, write the result: 4 x 4 B
+#   wave2_Mic*64: FP64 MIC(0) solve, read r (or q), two coefficients and the
+#            preconditioner, write q (or z): 5 x 8 B
+#   eik_sweep: read phi (8 B) and the changeability byte, write phi: 17 B
+#   cp_sweep: read the closest-particle index (4 B) and its 16-byte
+#            position pair, write the index: 24 B
+KERNEL_BYTES_PER_CELL = {"mic32_forward": 16, "mic32_backward": 16, "wave2_MicForward64": 40,
+                         "wave2_MicBackward64": 40, "eik_sweep": 17, "cp_sweep": 24}
+DOMINANT = tuple(KERNEL_BYTES_PER_CELL)
 
 
 def parse():
@@ -48,7 +58,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=1024)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--fp64-steps", type=int, default=8, help="steps of the all-FP64 path measured beside it")
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
@@ -233,7 +244,6 @@ def main():
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     # ---- timed region: device-resident state, per-step CUDA events ----
-    sim.set_kernel_timing(",".join(DOMINANT))
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
@@ -255,9 +265,25 @@ def main():
     barrier()
     total_ms = sum(a.elapsed_time(b) for a, b in evs)
     launches = sim.launch_count() - l0
+    clk = clocks.stop()
+    stage_ms = [round(x, 3) for x in sim.stage_times()]
+
+    # ---- per-kernel times (CUDA events on the simulation's stream around
+    # each launch) from a few extra steps outside the headline region ----
+    kt_steps = 3
+    sim.set_kernel_timing(",".join(DOMINANT))
+    kt_total = 0.0
+    for _ in range(kt_steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.runFrame()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        kt_total += e0.elapsed_time(e1)
     ktimes = sim.kernel_times()
     sim.set_kernel_timing("")
-    clk = clocks.stop()
     if world > 1:
         t = torch.tensor([total_ms], device="cuda", dtype=torch.float64)
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -266,12 +292,11 @@ def main():
     value = cells * args.steps * world / (total_ms / 1000.0)
 
     # ---- roofline of the dominant kernel ----
-    b = 8 if args.precision == "fp64" else 4
     dom = max((k for k in ktimes if k in DOMINANT), key=lambda k: ktimes[k][1], default=None)
     roofline = None
     if dom is not None:
         n_launch, ms = ktimes[dom]
-        alg_bytes = MIC_VALUES_PER_CELL * b * cells
+        alg_bytes = KERNEL_BYTES_PER_CELL[dom] * cells
         achieved = alg_bytes / (ms / n_launch / 1000.0) / 1e9
         peak, peak_src = 6800.0, "fallback"
         try:
@@ -290,7 +315,9 @@ def main():
                     "frac": round(achieved / peak, 4), "peak_source": peak_src,
                     "traffic": traffic, "launches": n_launch, "avg_launch_us": round(1000 * ms / n_launch, 2),
                     "algorithmic_bytes_per_launch": alg_bytes,
-                    "share_of_step": round(sum(v[1] for k, v in ktimes.items() if k in DOMINANT) / total_ms, 3)}
+                    "share_of_step": round(ktimes[dom][1] / kt_total, 3),
+                    "kernel_ms_per_step": {k: round(v[1] / kt_steps, 3) for k, v in sorted(ktimes.items())},
+                    "timed_over": f"{kt_steps} extra steps with per-launch events"}
 
     # ---- e2e: through the C ABI with host buffers (upload + frame + download) ----
     st = sim.get_state()
@@ -308,12 +335,38 @@ def main():
     e2e_s = time.perf_counter() - t0
     e2e_value = cells * args.e2e_steps * world / e2e_s
 
+    # ---- the all-FP64 GPU path on the same workload (fewer steps) ----
+    fp64_path = None
+    if args.precision == "mixed" and args.fp64_steps > 0:
+        sim64 = fs2d.FluidSim2D(sc, seed=SEED, **dict(opts, precision="fp64"))
+        sim64.set_stream(stream.cuda_stream)
+        for _ in range(min(args.warmup, 3)):
+            sim64.runFrame()
+        torch.cuda.synchronize()
+        ms64 = 0.0
+        for _ in range(args.fp64_steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sim64.runFrame()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms64 += e0.elapsed_time(e1)
+        fp64_path = {"value": cells * args.fp64_steps / (ms64 / 1000.0), "unit": UNIT,
+                     "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps,
+                     "stage_ms_last_step": [round(x, 3) for x in sim64.stage_times()],
+                     "pcg_iterations_last_step": sim64.stats()["pcgIterations"]}
+        sim64.close()
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (seeded dam break + disk, libc rand() particle jitter)",
         "config": config_dict(args, n_particles, {"pcg_iterations_per_step": iters}),
+        "stage_ms_last_step": stage_ms,
+        "fp64_path": fp64_path,
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,

@@ -397,6 +397,10 @@ int projection_mixed(Sim* s, int* status) {
     if (rhs_norm > 1e-12) {
         for (outer_iters = 0; outer_iters < s->opt.ir_max_outer; outer_iters++) {
             if (r_norm <= tol_abs) break;
+            // each inner solve works on r / ||r||inf: it has to reduce that
+            // by tol_abs / ||r||inf (with a factor 2 of margin for the FP32
+            // recurrence), but never asks for more than ir_inner_tol
+            const double inner_tol = std::max(s->opt.ir_inner_tol, 0.5 * tol_abs / r_norm);
             FS2D_LAUNCH(s, k_inner_init, nb, kT, 0, s->r, outer, m.pc, m.r, m.rp, m.e, NX, P, N, inner);
             rc = launch_mic32<true>(s, fmaps, m.q, done);
             if (rc) return rc;
@@ -410,7 +414,7 @@ int projection_mixed(Sim* s, int* status) {
                 FS2D_LAUNCH(s, k_spmv32, rg, kRT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, NY, P,
                             part2, inner);
                 FS2D_LAUNCH(s, k_axpy32, rg, kRT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, NX, NY, P, partf, inner,
-                            s->opt.ir_inner_tol);
+                            inner_tol);
                 rc = launch_mic32<true>(s, fmaps, m.q, done);
                 if (rc) return rc;
                 rc = launch_mic32<false>(s, bmaps, m.z, done);

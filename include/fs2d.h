@@ -103,7 +103,8 @@ typedef struct fs2d_options {
     double mic_sigma;       /* MIC(0) safety parameter; reference 0.25 */
     double pcg_tol;         /* stop when ||r||inf <= tol * ||b||inf; reference 1e-12 */
     int pcg_max_iters;      /* reference 200 */
-    double ir_inner_tol;    /* MIXED only: relative tolerance of each FP32 inner solve; default 1e-4 */
+    double ir_inner_tol;    /* MIXED only: tightest relative tolerance of an FP32 inner solve (a sweep that
+                               only needs a smaller reduction stops earlier); default 1e-4 */
     int ir_max_outer;       /* MIXED only: cap on refinement sweeps; default 30 */
     int p2g_mode;           /* FS2D_P2G_*; default ORDERED */
     int extrapolate_band;   /* 0 = every BFS layer (the reference); k > 0 = layers <= k only */
