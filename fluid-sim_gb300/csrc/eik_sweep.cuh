@@ -21,7 +21,13 @@
 // same pitch.  One 64-thread CTA per strip of 32 rows: warp 0 computes (lane
 // l owns row l of the strip and works on column s - l at step s), warp 1
 // moves data (tile stores, the strip's top row to the next strip, the row
-// below in).
+// below in).  Strips are launched in clusters; a boundary column travels as
+// two 64-bit words (low and high half of the value), each tagged with its
+// column (the high word's tag also carries the changed flag), so a column is
+// valid once both tags match and no flag or fence orders the words.  Inside
+// a cluster the I/O warp writes them into the next strip's shared ring;
+// across clusters they go through global memory with a released progress
+// counter.
 #pragma once
 
 #include <cuda.h>
@@ -34,13 +40,14 @@ constexpr int kEkCols = 32;
 constexpr int kEkRows = 32;
 constexpr int kEkSlots = 8;
 constexpr int kEkAhead = 4;
-constexpr int kEkCH = 16;
-constexpr int kEkBndChunks = 8;
+constexpr int kEkCH = 16;          // columns per arrival check / flow-control chunk
+constexpr int kEkRingChunks = 16;
+constexpr int kEkRing = kEkRingChunks * kEkCH;   // boundary ring, columns
 constexpr int kEkTopRing = 256;
 constexpr unsigned kEkTileBytes = kEkCols * kEkRows * 8;
 constexpr unsigned kEkMaskBytes = kEkCols * kEkRows;
-constexpr size_t kEkSmem = (size_t)kEkSlots * (kEkTileBytes + kEkMaskBytes) + kEkBndChunks * kEkCH * 16 +
-                           kEkTopRing * 16 + 16 * 4 + kEkSlots * 8;
+constexpr size_t kEkSmem = (size_t)kEkSlots * (kEkTileBytes + kEkMaskBytes) + (size_t)(kEkRing + kEkTopRing) * 16 +
+                           16 * 4 + kEkSlots * 8;
 
 struct EkMaps {
     CUtensorMap ld;       // phi, box 32 x 32 (load and store of full strips)
@@ -60,17 +67,13 @@ __device__ __forceinline__ double eik_ref(double own, double a, double b, double
     return (d < -own) ? -d : own;
 }
 
-__device__ __noinline__ double eik_ref_call(double own, double a, double b, double dx, double c2) {
-    return eik_ref(own, a, b, dx, c2);
-}
-
 // The same update with bit-pattern comparisons (identical results).
 __device__ __forceinline__ double eik_fast(double own, double a, double b, double dx, double c2) {
     const unsigned long long kSign = 0x8000000000000000ull, kInf = 0x7FF0000000000000ull;
     const unsigned long long ob = (unsigned long long)__double_as_longlong(own);
     const unsigned long long ab = (unsigned long long)__double_as_longlong(a) & ~kSign;
     const unsigned long long bb = (unsigned long long)__double_as_longlong(b) & ~kSign;
-    if ((ob & ~kSign) > kInf || ab > kInf || bb > kInf) return eik_ref_call(own, a, b, dx, c2);
+    if ((ob & ~kSign) > kInf || ab > kInf || bb > kInf) return eik_ref(own, a, b, dx, c2);
     if (!(ob >> 63) || ob == kSign) return own;   // own >= 0 (+0, -0, positive)
     const unsigned long long p0 = bb < ab ? bb : ab;   // min(|a|, |b|) as (y < x) ? y : x
     const unsigned long long p1 = ab < bb ? bb : ab;   // max(|a|, |b|) as (x < y) ? y : x
@@ -99,22 +102,37 @@ struct EkArgs {
     double dx, c2;
 };
 
+// Tagged boundary words of column c: value halves, tags 2c and 2c + changed.
+__device__ __forceinline__ unsigned long long ek_w0(int c, double v) {
+    return ((unsigned long long)(2u * (unsigned)c) << 32) | (unsigned)__double_as_longlong(v);
+}
+__device__ __forceinline__ unsigned long long ek_w1(int c, double v, bool chg) {
+    return ((unsigned long long)(2u * (unsigned)c + (chg ? 1u : 0u)) << 32) |
+           (unsigned)((unsigned long long)__double_as_longlong(v) >> 32);
+}
+__device__ __forceinline__ bool ek_w0_is(unsigned long long w, int c) { return (unsigned)(w >> 32) == 2u * (unsigned)c; }
+__device__ __forceinline__ bool ek_w1_is(unsigned long long w, int c) { return (unsigned)(w >> 33) == (unsigned)c; }
+__device__ __forceinline__ double ek_value(unsigned long long w0, unsigned long long w1) {
+    return __longlong_as_double((long long)(((w1 & 0xffffffffull) << 32) | (w0 & 0xffffffffull)));
+}
+__device__ __forceinline__ bool ek_changed(unsigned long long w1) { return ((w1 >> 32) & 1ull) != 0; }
+
 template <int SX, int SY>
 __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ EkMaps maps, const EkArgs a) {
     if (a.skip != nullptr && *a.skip) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     double* tiles = reinterpret_cast<double*>(smem_raw);
     unsigned char* mtiles = smem_raw + (size_t)kEkSlots * kEkTileBytes;
-    double2* bnd = reinterpret_cast<double2*>(mtiles + (size_t)kEkSlots * kEkMaskBytes);
-    double2* top = bnd + kEkBndChunks * kEkCH;
-    volatile int* ctr = reinterpret_cast<volatile int*>(top + kEkTopRing);
-    volatile int* bnd_ready = ctr + 0;
-    volatile int* bnd_used = ctr + 1;
-    volatile int* top_ready = ctr + 2;
-    volatile int* top_done = ctr + 3;
-    volatile int* quit = ctr + 4;
-    volatile int* tiles_done = ctr + 5;
-    volatile int* tiles_freed = ctr + 6;
+    // row below the strip: 2 tagged words per column
+    volatile unsigned long long* bnd =
+        reinterpret_cast<volatile unsigned long long*>(mtiles + (size_t)kEkSlots * kEkMaskBytes);
+    volatile unsigned long long* top = bnd + 2 * kEkRing;   // the strip's top row, 2 words per column
+    volatile int* ctr = reinterpret_cast<volatile int*>(const_cast<unsigned long long*>(top + 2 * kEkTopRing));
+    volatile int* bnd_used = ctr + 0;     // chunks of the row below the compute warp has finished
+    volatile int* top_done = ctr + 1;     // top-row columns forwarded by the I/O warp
+    volatile int* quit = ctr + 2;
+    volatile int* tiles_done = ctr + 3;
+    volatile int* tiles_freed = ctr + 4;
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(const_cast<int*>(ctr) + 16);
 
     const int lane = threadIdx.x & 31;
@@ -123,38 +141,104 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
     const int NX = a.NX, NY = a.NY, P = a.P;
     const int nstrips = (NY + kEkRows - 1) / kEkRows;
     const int nt = P / kEkCols;
-    const int nchunks = P / kEkCH;
     const bool has_next = strip + 1 < nstrips;
     const bool below_in_grid = strip > 0;
+    const bool active = strip < nstrips;                       // the grid is rounded up to whole clusters
+    const unsigned crank = cluster_ctarank(), csize = cluster_nctarank();
+    const bool prev_local = below_in_grid && crank > 0;        // the previous strip fills this ring
+    const bool next_local = has_next && crank + 1 < csize;     // this strip fills the next strip's ring
     const int y0 = SY > 0 ? kEkRows * strip : NY - kEkRows - kEkRows * strip;   // memory row of box row 0
 
     if (threadIdx.x == 0) {
         for (int k = 0; k < kEkSlots; k++) mbar_init(bars + k, 1);
         fence_mbar_init();
-        *bnd_ready = below_in_grid ? 0 : nchunks;
         *bnd_used = 0;
-        *top_ready = 0;
         *top_done = 0;
         *quit = 0;
         *tiles_done = 0;
         *tiles_freed = 0;
     }
-    if (!below_in_grid) {
-        for (int k = threadIdx.x; k < kEkBndChunks * kEkCH; k += blockDim.x) bnd[k] = make_double2(0.0, 0.0);
-    }
-    __syncthreads();
+    for (int k = threadIdx.x; k < 2 * kEkRing; k += blockDim.x) bnd[k] = ~0ull;      // no column matches
+    for (int k = threadIdx.x; k < 2 * kEkTopRing; k += blockDim.x) top[k] = ~0ull;
+    cluster_sync_all();   // every ring and counter of the cluster is initialised
 
-    if (warp == 1) {
+    if (warp == 1 && active) {
         // ---------------- I/O warp ----------------
         const unsigned long long* gprev = below_in_grid ? a.progress + (strip - 1) : nullptr;
-        int hbk = below_in_grid ? 0 : nchunks;
-        int tc = 0;
+        int hb = (below_in_grid && !prev_local) ? 0 : P;   // next column of the row below to fetch
+        int tc = 0;                                        // top-row columns forwarded
         const int tend = has_next ? P : 0;
+        int rused = 0;                                     // last seen chunk position of the consumer
+        const unsigned r_bnd = next_local ? mapa_shared((const void*)bnd, crank + 1) : 0u;
+        const unsigned r_used = next_local ? mapa_shared((const void*)bnd_used, crank + 1) : 0u;
         int ts = 0;
         unsigned long long gavail = 0;
         long long idle = 0;
-        while (hbk < nchunks || tc < tend || ts < nt) {
+        while (hb < P || tc < tend || ts < nt) {
             bool moved = false;
+            // row below from global memory (the previous strip is in another cluster)
+            if (hb < P && hb < (*bnd_used + kEkRingChunks - 2) * kEkCH) {
+                const int n = min(32, P - hb);
+                const unsigned long long need = a.base + (unsigned long long)(hb + n);
+                if (gavail < need) {
+                    unsigned long long v = 0;
+                    if (lane == 0) v = ld_acquire(gprev);
+                    gavail = __shfl_sync(0xffffffffu, v, 0);
+                }
+                const int avail = (int)min((unsigned long long)n, gavail > a.base + hb ? gavail - a.base - hb : 0ull);
+                if (avail > 0) {
+                    __syncwarp();   // lane 0's acquire orders the reads below
+                    const int c = hb + lane;
+                    if (lane < avail) {
+                        const double2 e = __ldcg(a.hb + (size_t)(strip - 1) * P + c);
+                        bnd[2 * (c % kEkRing)] = ek_w0(c, e.x);
+                        bnd[2 * (c % kEkRing) + 1] = ek_w1(c, e.x, e.y != 0.0);
+                    }
+                    __syncwarp();
+                    hb += avail;
+                    moved = true;
+                }
+            }
+            // top row out: to the next strip's ring (same cluster) or to global memory
+            if (tc < tend) {
+                const int c = tc + lane;
+                unsigned long long w0 = 0ull, w1 = 0ull;
+                if (c < P) {
+                    w0 = top[2 * (c % kEkTopRing)];
+                    w1 = top[2 * (c % kEkTopRing) + 1];
+                }
+                const bool ok = c >= P || (ek_w0_is(w0, c) && ek_w1_is(w1, c));
+                const unsigned bad = __ballot_sync(0xffffffffu, !ok);
+                int n = bad ? __ffs(bad) - 1 : 32;
+                n = min(n, P - tc);
+                if (n > 0 && next_local) {
+                    if (tc + n > (rused + kEkRingChunks - 2) * kEkCH) {
+                        int v = 0;
+                        if (lane == 0) v = ld_volatile_cluster_remote(r_used);
+                        rused = __shfl_sync(0xffffffffu, v, 0);
+                    }
+                    n = min(n, (rused + kEkRingChunks - 2) * kEkCH - tc);
+                }
+                if (n > 0) {
+                    if (next_local) {
+                        if (lane < n) {
+                            const unsigned slot = 16u * (unsigned)(c % kEkRing);
+                            st_cluster_u64(r_bnd + slot, w0);
+                            st_cluster_u64(r_bnd + slot + 8u, w1);
+                        }
+                        __syncwarp();
+                    } else {
+                        if (lane < n)
+                            a.hb[(size_t)strip * P + c] = make_double2(ek_value(w0, w1), ek_changed(w1) ? 1.0 : 0.0);
+                        __threadfence();
+                        __syncwarp();
+                        if (lane == 0) st_release(a.progress + strip, a.base + (unsigned long long)(tc + n));
+                    }
+                    tc += n;
+                    if (lane == 0) *top_done = tc;
+                    moved = true;
+                }
+            }
             if (ts < nt && *tiles_done > ts) {
                 if (lane == 0) {
                     const double* src = tiles + (size_t)(ts % kEkSlots) * (kEkCols * kEkRows);
@@ -173,39 +257,6 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                 ts++;
                 moved = true;
             }
-            if (hbk < nchunks && hbk < *bnd_used + kEkBndChunks - 1) {
-                const unsigned long long need = a.base + (unsigned long long)min((hbk + 1) * kEkCH, P);
-                if (gavail < need) {
-                    unsigned long long v = 0;
-                    if (lane == 0) v = ld_acquire(gprev);
-                    gavail = __shfl_sync(0xffffffffu, v, 0);
-                }
-                if (gavail >= need) {
-                    if (lane < kEkCH)
-                        bnd[(hbk % kEkBndChunks) * kEkCH + lane] =
-                            __ldcg(a.hb + (size_t)(strip - 1) * P + hbk * kEkCH + lane);
-                    __threadfence_block();
-                    __syncwarp();
-                    hbk++;
-                    if (lane == 0) *bnd_ready = hbk;
-                    moved = true;
-                }
-            }
-            if (tc < tend) {
-                const int tr = *top_ready;
-                if (tr > tc) {
-                    __threadfence_block();
-                    for (int c = tc + lane; c < tr; c += 32) a.hb[(size_t)strip * P + c] = top[c % kEkTopRing];
-                    __threadfence();
-                    __syncwarp();
-                    tc = tr;
-                    if (lane == 0) {
-                        st_release(a.progress + strip, a.base + (unsigned long long)tc);
-                        *top_done = tc;
-                    }
-                    moved = true;
-                }
-            }
             if (moved) {
                 idle = 0;
             } else if (++idle > 16 * kWaveSpinLimit || *quit || ((idle & 1023) == 0 && *(volatile int*)a.err)) {
@@ -215,134 +266,155 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         }
         if (lane == 0) bulk_wait_all();
         __syncwarp();
-        return;
-    }
-
-    // ---------------- compute warp ----------------
-    const bool rowvalid = kEkRows * strip + lane < NY;
-    const int j = SY > 0 ? kEkRows * strip + lane : NY - 1 - kEkRows * strip - lane;
-    const bool jupd = rowvalid && j >= a.j_lo && j <= a.j_hi;
-    const int brow = SY > 0 ? lane : kEkRows - 1 - lane;    // box row of the lane's row
-    auto tile_x = [&](int t) { return SX > 0 ? t * kEkCols : P - (t + 1) * kEkCols; };
-    auto bc_of = [&](int c) { return SX > 0 ? (c & 31) : 31 - (c & 31); };
-    auto issue = [&](int t) {
-        if (lane == 0 && t < nt) {
+    } else if (warp == 0 && active) {
+        // ---------------- compute warp ----------------
+        const bool rowvalid = kEkRows * strip + lane < NY;
+        const int j = SY > 0 ? kEkRows * strip + lane : NY - 1 - kEkRows * strip - lane;
+        const bool jupd = rowvalid && j >= a.j_lo && j <= a.j_hi;
+        const int brow = SY > 0 ? lane : kEkRows - 1 - lane;    // box row of the lane's row
+        auto tile_x = [&](int t) { return SX > 0 ? t * kEkCols : P - (t + 1) * kEkCols; };
+        auto bc_of = [&](int c) { return SX > 0 ? (c & 31) : 31 - (c & 31); };
+        auto issue = [&](int t) {
+            if (lane == 0 && t < nt) {
+                unsigned long long* bar = bars + (t % kEkSlots);
+                mbar_expect_tx(bar, kEkTileBytes + kEkMaskBytes);
+                tma_load_2d(tiles + (size_t)(t % kEkSlots) * (kEkCols * kEkRows), &maps.ld, tile_x(t), y0, bar);
+                tma_load_2d(mtiles + (size_t)(t % kEkSlots) * kEkMaskBytes, &maps.mask, tile_x(t), y0, bar);
+            }
+        };
+        bool failed = false;
+        auto wait_tile = [&](int t) {
             unsigned long long* bar = bars + (t % kEkSlots);
-            mbar_expect_tx(bar, kEkTileBytes + kEkMaskBytes);
-            tma_load_2d(tiles + (size_t)(t % kEkSlots) * (kEkCols * kEkRows), &maps.ld, tile_x(t), y0, bar);
-            tma_load_2d(mtiles + (size_t)(t % kEkSlots) * kEkMaskBytes, &maps.mask, tile_x(t), y0, bar);
-        }
-    };
-    bool failed = false;
-    auto wait_tile = [&](int t) {
-        unsigned long long* bar = bars + (t % kEkSlots);
-        const unsigned parity = (unsigned)((t / kEkSlots) & 1);
-        long long polls = 0;
-        while (!mbar_try_wait(bar, parity)) {
-            if (++polls > kWaveSpinLimit) {
-                failed = true;
-                atomicOr(a.err, 1);
-                break;
+            const unsigned parity = (unsigned)((t / kEkSlots) & 1);
+            long long polls = 0;
+            while (!mbar_try_wait(bar, parity)) {
+                if (++polls > kWaveSpinLimit) {
+                    failed = true;
+                    atomicOr(a.err, 1);
+                    break;
+                }
             }
-        }
-    };
-    auto spin_ge = [&](volatile int* flag, int need) {
-        if (failed) return;
-        long long polls = 0;
-        while (*flag < need) {
-            if (++polls > 16 * kWaveSpinLimit) {
-                failed = true;
-                atomicOr(a.err, 1);
-                *quit = 1;
-                return;
+        };
+        auto spin_ge = [&](volatile int* flag, int need) {
+            if (failed) return;
+            long long polls = 0;
+            while (*flag < need) {
+                if (++polls > 16 * kWaveSpinLimit) {
+                    failed = true;
+                    atomicOr(a.err, 1);
+                    *quit = 1;
+                    return;
+                }
             }
-        }
-    };
+        };
+        // plain views of the rings for the per-step accesses (tags validate them)
+        const unsigned long long* bnd_p = const_cast<const unsigned long long*>(bnd);
+        unsigned long long* top_p = const_cast<unsigned long long*>(top);
 
-    for (int t = 0; t < kEkAhead; t++) issue(t);
+        for (int t = 0; t < kEkAhead; t++) issue(t);
 
-    double o_v = 0.0;     // output of the previous step (the left value)
-    bool o_c = false;     // ... and whether the sweep changed it
+        double o_v = 0.0;     // output of the previous step (the left value)
+        bool o_c = false;     // ... and whether the sweep changed it
+        unsigned long long bw0 = 0ull, bw1 = 0ull;   // row-below words of lane 0's column
 
-    auto tile_steps = [&](int t, auto check_tag) {
-        constexpr bool check = decltype(check_tag)::value;
+        auto tile_steps = [&](int t, auto check_tag) {
+            constexpr bool check = decltype(check_tag)::value;
 #pragma unroll 4
-        for (int u = 0; u < kEkCols; u++) {
-            const int s = t * kEkCols + u;
-            const int c = s - lane;
-            if ((s % kEkCH) == 0 && s < P) {   // lane 0 enters a new chunk of the row below
-                const int h = s / kEkCH;
-                if (*bnd_ready <= h) spin_ge(bnd_ready, h + 1);
-                __threadfence_block();
-                if (lane == 0) *bnd_used = h;
-                __syncwarp();
-            }
-            double b_v = __shfl_up_sync(0xffffffffu, o_v, 1);
-            bool b_c = __shfl_up_sync(0xffffffffu, (int)o_c, 1) != 0;
-            if (lane == 0) {
-                const double2 e = bnd[((s / kEkCH) % kEkBndChunks) * kEkCH + (s % kEkCH)];
-                b_v = e.x;
-                b_c = e.y != 0.0;
-            }
-            const bool cin = !check || (c >= 0 && c < P);
-            const int i = SX > 0 ? c : P - 1 - c;
-            double own = 0.0;
-            double* cell = nullptr;
-            bool act = false;
-            if (rowvalid && cin && i < NX) {
-                const int slot = (c >> 5) % kEkSlots;   // c >= 0 here
-                const int in_tile = brow * kEkCols + bc_of(c);
-                cell = tiles + (size_t)slot * (kEkCols * kEkRows) + in_tile;
-                own = *cell;
-                const bool upd = jupd && i >= a.i_lo && i <= a.i_hi;
-                act = upd && (o_c || b_c || mtiles[(size_t)slot * kEkMaskBytes + in_tile] != 0);
-            }
-            double out = own;
-            bool chg = false;
-            if (__any_sync(0xffffffffu, act)) {
-                if (act) {
-                    out = eik_fast(own, o_v, b_v, a.dx, a.c2);
-                    chg = !same_bits(out, own);
-                    if (chg) *cell = out;
+            for (int u = 0; u < kEkCols; u++) {
+                const int s = t * kEkCols + u;
+                const int c = s - lane;
+                if (below_in_grid && (u % kEkCH) == 0 && s < P) {
+                    // lane 0 enters a chunk of the row below: every word of it
+                    // must have arrived (one word per lane, one vote)
+                    const int cc = s + (lane & (kEkCH - 1));
+                    const int wi = 2 * (cc % kEkRing) + (lane >> 4);
+                    bool ok = cc >= P || ((lane >> 4) ? ek_w1_is(bnd_p[wi], cc) : ek_w0_is(bnd_p[wi], cc));
+                    if (!__all_sync(0xffffffffu, ok)) {
+                        long long polls = 0;
+                        while (!ok && !failed) {
+                            const unsigned long long w = bnd[wi];
+                            ok = (lane >> 4) ? ek_w1_is(w, cc) : ek_w0_is(w, cc);
+                            if (!ok && ++polls > 16 * kWaveSpinLimit) {
+                                failed = true;
+                                atomicOr(a.err, 1);
+                                *quit = 1;
+                            }
+                        }
+                    }
+                    __syncwarp();   // lane 0 reads the words its neighbours validated
+                    if (lane == 0) *bnd_used = s / kEkCH;
+                }
+                if (below_in_grid && (!check || s < P)) {
+                    bw0 = bnd_p[2 * (s % kEkRing)];
+                    bw1 = bnd_p[2 * (s % kEkRing) + 1];
+                }
+                double b_v = __shfl_up_sync(0xffffffffu, o_v, 1);
+                bool b_c = __shfl_up_sync(0xffffffffu, (int)o_c, 1) != 0;
+                if (lane == 0) {
+                    b_v = below_in_grid ? ek_value(bw0, bw1) : 0.0;
+                    b_c = below_in_grid && ek_changed(bw1);
+                }
+                const bool cin = !check || (c >= 0 && c < P);
+                const int i = SX > 0 ? c : P - 1 - c;
+                double own = 0.0;
+                double* cell = nullptr;
+                bool act = false;
+                if (rowvalid && cin && i < NX) {
+                    const int slot = (c >> 5) % kEkSlots;   // c >= 0 here
+                    const int in_tile = brow * kEkCols + bc_of(c);
+                    cell = tiles + (size_t)slot * (kEkCols * kEkRows) + in_tile;
+                    own = *cell;
+                    const bool upd = jupd && i >= a.i_lo && i <= a.i_hi;
+                    act = upd && (o_c || b_c || mtiles[(size_t)slot * kEkMaskBytes + in_tile] != 0);
+                }
+                double out = own;
+                bool chg = false;
+                if (__any_sync(0xffffffffu, act)) {
+                    if (act) {
+                        out = eik_fast(own, o_v, b_v, a.dx, a.c2);
+                        chg = !same_bits(out, own);
+                        if (chg) *cell = out;
+                    }
+                }
+                o_v = out;
+                o_c = chg;
+                if (has_next && lane == 31 && cin) {
+                    top_p[2 * (c % kEkTopRing)] = ek_w0(c, out);
+                    top_p[2 * (c % kEkTopRing) + 1] = ek_w1(c, out, chg);
                 }
             }
-            o_v = out;
-            o_c = chg;
-            if (has_next && lane == 31 && cin) {
-                top[c % kEkTopRing] = make_double2(out, chg ? 1.0 : 0.0);
-                if (((c + 1) % 8) == 0 || c == P - 1) {
-                    __threadfence_block();
-                    *top_ready = c + 1;
-                }
-            }
-        }
-    };
+        };
 
-    const int nsteps = P + 31;
-    for (int t = 0; t * kEkCols < nsteps; t++) {
-        if (t < nt) wait_tile(t);
-        if (has_next && t * kEkCols - 31 - *top_done > kEkTopRing / 2)
-            spin_ge(top_done, t * kEkCols - 31 - kEkTopRing / 2);
+        const int nsteps = P + 31;
+        for (int t = 0; t * kEkCols < nsteps; t++) {
+            if (t < nt) wait_tile(t);
+            if (has_next && t * kEkCols - 31 - *top_done > kEkTopRing / 2)
+                spin_ge(top_done, t * kEkCols - 31 - kEkTopRing / 2);
+            __syncwarp();
+            if (t == 0 || t >= nt)
+                tile_steps(t, BoolTag<true>{});
+            else
+                tile_steps(t, BoolTag<false>{});
+            if (t >= 1 && t - 1 < nt) {
+                fence_async_smem();
+                __syncwarp();
+                if (lane == 0) *tiles_done = t;
+            }
+            const int nx = t + kEkAhead;
+            if (nx < nt) {
+                if (nx >= kEkSlots && *tiles_freed < nx - kEkSlots + 1) spin_ge(tiles_freed, nx - kEkSlots + 1);
+                __syncwarp();
+                issue(nx);
+            }
+        }
         __syncwarp();
-        if (t == 0 || t >= nt)
-            tile_steps(t, BoolTag<true>{});
-        else
-            tile_steps(t, BoolTag<false>{});
-        if (t >= 1 && t - 1 < nt) {
-            fence_async_smem();
-            __syncwarp();
-            if (lane == 0) *tiles_done = t;
+        if (lane == 0) {
+            *tiles_done = nt;
+            if (below_in_grid) *bnd_used = P / kEkCH + kEkRingChunks;
         }
-        const int nx = t + kEkAhead;
-        if (nx < nt) {
-            if (nx >= kEkSlots && *tiles_freed < nx - kEkSlots + 1) spin_ge(tiles_freed, nx - kEkSlots + 1);
-            __syncwarp();
-            issue(nx);
-        }
+        (void)failed;
     }
-    __syncwarp();
-    if (lane == 0) *tiles_done = nt;
-    (void)failed;
+    cluster_sync_all();   // no CTA leaves while a neighbour may still touch its shared memory
 }
 
 }  // namespace fs2d

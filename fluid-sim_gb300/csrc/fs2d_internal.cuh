@@ -108,6 +108,7 @@ struct Sim {
     double* phi_p = nullptr;          // pitched level set of the Eikonal sweeps (P x NY)
     uint8_t* emask = nullptr;         // Eikonal: cells whose update changes them (P x NY)
     CpMapsHost* ekmaps = nullptr;     // TMA descriptors of the Eikonal sweeps
+    int ek_cluster = 0;               // cluster size of the Eikonal sweeps (0: not chosen)
     unsigned long long* seed_key = nullptr;
     double* phi_tmp = nullptr;
     uint8_t* surface = nullptr;

@@ -194,17 +194,19 @@ __device__ __forceinline__ double eikonal(double own, double a, double b, double
 }
 
 
-__global__ void k_eik_check(const double* __restrict__ phi, uint8_t* mask, int P, int i_lo, int i_hi, int j_lo,
-                            int j_hi, int sx, int sy, double dx, int* noop) {
-    int i = i_lo + blockIdx.x * blockDim.x + threadIdx.x;
-    int j = j_lo + blockIdx.y;
-    if (i > i_hi || j > j_hi) return;
+__global__ void k_eik_check(const double* __restrict__ phi, uint8_t* mask, int NX, int NY, int P, int i_lo,
+                            int i_hi, int j_lo, int j_hi, int sx, int sy, double dx, int* noop) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= NX) return;
     size_t c = (size_t)j * P + i;
-    double own = phi[c];
     bool ch = false;
-    if (own < 0) {
-        double nv = eikonal(own, phi[c - sx], phi[(size_t)(j - sy) * P + i], dx);
-        ch = nv != own;
+    if (i >= i_lo && i <= i_hi && j >= j_lo && j <= j_hi) {
+        double own = phi[c];
+        if (own < 0) {
+            double nv = eikonal(own, phi[c - sx], phi[(size_t)(j - sy) * P + i], dx);
+            ch = nv != own;
+        }
     }
     mask[c] = ch ? 1 : 0;
     if (ch) *noop = 0;
@@ -373,9 +375,15 @@ static int launch_eik_sweep_dir(Sim* s, const WaveGeom& g, const int* skip) {
     void* args[] = {(void*)maps, (void*)&a};
     s->launches++;
     long long kt = ktimer_begin(s, "eik_sweep");
-    int rc = check_cuda(cudaLaunchCooperativeKernel((const void*)eik_sweep_kernel<SX, SY>, dim3(nstrips), dim3(64),
-                                                    args, kEkSmem, s->stream),
-                        "eik_sweep");
+    int& cs = s->ek_cluster;   // 0: not chosen yet
+    if (cs == 0) cs = choose_cluster((const void*)eik_sweep_kernel<SX, SY>, nstrips, 64, kEkSmem);
+    cudaError_t e = launch_clustered((const void*)eik_sweep_kernel<SX, SY>, nstrips, cs, 64, kEkSmem, s->stream, args);
+    if (e != cudaSuccess && cs > 1) {   // clusters refused: plain cooperative launch
+        (void)cudaGetLastError();
+        cs = 1;
+        e = launch_clustered((const void*)eik_sweep_kernel<SX, SY>, nstrips, 1, 64, kEkSmem, s->stream, args);
+    }
+    int rc = check_cuda(e, "eik_sweep");
     ktimer_end(s, kt);
     return rc;
 }
@@ -463,9 +471,8 @@ int levelset_create(Sim* s) {
             int i_lo = sx > 0 ? 1 : 0, i_hi = sx > 0 ? NX - 1 : NX - 2;
             int j_lo = sy > 0 ? 1 : 0, j_hi = sy > 0 ? NY - 1 : NY - 2;
             FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));
-            dim3 gc(blocks_for(i_hi - i_lo + 1, 128), j_hi - j_lo + 1);
-            FS2D_LAUNCH(s, k_eik_check, gc, 128, 0, s->phi_p, s->emask, P, i_lo, i_hi, j_lo, j_hi, sx, sy, s->dx,
-                        noop);
+            FS2D_LAUNCH(s, k_eik_check, g2, 128, 0, s->phi_p, s->emask, NX, NY, P, i_lo, i_hi, j_lo, j_hi, sx, sy,
+                        s->dx, noop);
             WaveGeom g{sx, sy, i_lo, i_hi, j_lo, j_hi};
             int rc = launch_eik_sweep(s, g, noop);
             if (rc) return rc;

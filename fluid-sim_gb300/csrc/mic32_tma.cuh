@@ -72,9 +72,6 @@ __device__ __forceinline__ unsigned long long m32_entry(int c, float v) {
 }
 __device__ __forceinline__ bool m32_entry_is(unsigned long long e, int c) { return (unsigned)(e >> 32) == (unsigned)c; }
 __device__ __forceinline__ float m32_entry_value(unsigned long long e) { return __uint_as_float((unsigned)e); }
-__device__ __forceinline__ void st_cluster_u64(unsigned addr, unsigned long long v) {
-    asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v) : "memory");
-}
 
 // FWD: out = v0 - v1*left - v2*below  (forward, on q~ = q*pc)
 // BWD: same form with the backward coefficients.

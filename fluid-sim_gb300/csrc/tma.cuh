@@ -85,6 +85,11 @@ __device__ __forceinline__ void st_cluster_v4f32(unsigned addr, float4 v) {
                  "f"(v.w)
                  : "memory");
 }
+// Remote store of a tagged 64-bit word (validated by its tag on the reading
+// side, so no compiler memory clobber).
+__device__ __forceinline__ void st_cluster_u64(unsigned addr, unsigned long long v) {
+    asm volatile("st.shared::cluster.u64 [%0], %1;" ::"r"(addr), "l"(v));
+}
 __device__ __forceinline__ void st_cluster_s32(unsigned addr, int v) {
     asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
 }
