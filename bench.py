@@ -320,7 +320,8 @@ def main():
                     "timed_over": f"{kt_steps} extra steps with per-launch events"}
 
     # ---- e2e: through the C ABI with host buffers (upload + frame + download) ----
-    st = sim.get_state()
+    e2e = None
+    st = sim.get_state() if args.e2e_steps > 0 else {}
     host_in = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in st.items()}
     host_out = {k: torch.from_numpy(v.copy()).pin_memory().numpy() for k, v in st.items()}
     h2d = state_bytes(host_in)
@@ -333,7 +334,10 @@ def main():
         sim.get_state(out=host_out)
         host_in, host_out = host_out, host_in
     e2e_s = time.perf_counter() - t0
-    e2e_value = cells * args.e2e_steps * world / e2e_s
+    if args.e2e_steps > 0:
+        e2e = {"value": cells * args.e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
+               "path": "fs2d_upload_state + fs2d_run_frame + fs2d_download_state, full state, pinned host buffers"}
 
     # ---- the all-FP64 GPU path on the same workload (fewer steps) ----
     fp64_path = None
@@ -370,9 +374,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,
-        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": args.e2e_steps, "path": "fs2d_upload_state + fs2d_run_frame + fs2d_download_state, "
-                                                 "full state, pinned host buffers"},
+        "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args, args.cpu_budget, 10)
