@@ -579,6 +579,32 @@ int fs2d_run_stage(fs2d_sim* p, int stage) {
     return rc ? rc : status;
 }
 
+int fs2d_solve_pressure(fs2d_sim* p, const uint8_t* cell, const double* phi, const double* u, const double* v,
+                        double* pressure, fs2d_stats* stats) {
+    if (!p || !cell || !phi || !u || !v || !pressure) {
+        set_error("fs2d_solve_pressure: cell, phi, u, v and pressure are required");
+        return FS2D_ERR_INVALID;
+    }
+    fs2d_state in{};
+    in.cell = const_cast<uint8_t*>(cell);
+    in.phi = const_cast<double*>(phi);
+    in.u = const_cast<double*>(u);
+    in.v = const_cast<double*>(v);
+    int rc = fs2d_upload_state(p, &in);
+    if (rc) return rc;
+    const int status = fs2d_run_stage(p, FS2D_STAGE_APPLY_PROJECTION);
+    if (status && status != FS2D_ERR_NOT_CONVERGED) return status;
+    fs2d_state out{};
+    out.p = pressure;
+    rc = fs2d_download_state(p, &out);
+    if (rc) return rc;
+    if (stats) {
+        rc = fs2d_get_stats(p, stats);
+        if (rc) return rc;
+    }
+    return status;
+}
+
 int fs2d_run_frame(fs2d_sim* p) {
     if (!p) return FS2D_ERR_INVALID;
     Host* h = H(p);

@@ -85,6 +85,8 @@ SIGNATURES = {
     "fs2d_avg_pressure": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "fs2d_avg_pressure_in_fluid": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "fs2d_max_velocity": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "fs2d_solve_pressure": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p]),
     "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
     "fs2d_save_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
     "fs2d_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -229,6 +231,20 @@ class FluidSim2D:
         arrs = {k: np.ascontiguousarray(v) for k, v in arrs.items() if v is not None}
         st = state_view(arrs)
         _check(load().fs2d_upload_state(self.h, C.byref(st)))
+
+    def solve_pressure(self, cell, phi, u, v):
+        """The projection's pressure solve on the given labels, level set and
+        face velocities; returns (pressure, stats)."""
+        NX, NY = self.nx, self.ny
+        cell = np.ascontiguousarray(cell, dtype=np.uint8).reshape(-1)
+        phi, u, v = (np.ascontiguousarray(a, dtype=np.float64).reshape(-1) for a in (phi, u, v))
+        assert cell.size == NX * NY and phi.size == NX * NY and u.size == (NX + 1) * NY and v.size == NX * (NY + 1)
+        out = np.empty(NX * NY)
+        st = Stats()
+        rc = load().fs2d_solve_pressure(self.h, cell.ctypes.data, phi.ctypes.data, u.ctypes.data, v.ctypes.data,
+                                        out.ctypes.data, C.byref(st))
+        _check(rc, allow=(4,))
+        return out, {k: getattr(st, k) for k, _ in Stats._fields_}
 
     def set_params(self, gravityX, gravityY, picFlipAlpha, dt):
         _check(load().fs2d_set_params(self.h, gravityX, gravityY, picFlipAlpha, dt))

@@ -166,6 +166,19 @@ int fs2d_destroy(fs2d_sim* sim);
  * cap (the reference logs and continues; so does this call). */
 int fs2d_run_frame(fs2d_sim* sim);
 
+/* The pressure solve alone (applyProjection, src/FluidSim2D.cpp:252-467) on
+ * caller-supplied host arrays: labels `cell` and level set `phi`
+ * (sizeX*sizeY), face velocities `u` ((sizeX+1)*sizeY) and `v`
+ * (sizeX*(sizeY+1)).  They replace the handle's fields; the matrix and
+ * right-hand side are built as the reference builds them, the system is
+ * solved with the handle's precision and stopping rule, and the pressure is
+ * written to `pressure` (sizeX*sizeY).  `stats` (may be NULL) receives the
+ * iteration count and final relative residual.  Returns
+ * FS2D_ERR_NOT_CONVERGED (with the last iterate in `pressure`) when the
+ * iteration cap was reached. */
+int fs2d_solve_pressure(fs2d_sim* sim, const uint8_t* cell, const double* phi, const double* u, const double* v,
+                        double* pressure, fs2d_stats* stats);
+
 /* Runs `nframes` frames back to back without host synchronisation between them
  * (except the pressure solver's convergence polls). */
 int fs2d_step(fs2d_sim* sim, int nframes);
