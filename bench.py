@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--fp64-steps", type=int, default=8, help="steps of the all-FP64 path measured beside it")
+    ap.add_argument("--pressure-size", type=int, default=2048,
+                    help="grid of the standalone pressure-solve comparison (0: skip)")
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
@@ -363,6 +365,38 @@ def main():
                      "pcg_iterations_last_step": sim64.stats()["pcgIterations"]}
         sim64.close()
 
+    # ---- standalone pressure solve: random disks, N(0,1) velocities, 1e-10 ----
+    pressure = None
+    if args.pressure_size > 0:
+        import scenes
+        n = args.pressure_size
+        psc, pcell, pphi, pu, pv = scenes.pressure_disks(n, n, seed=n)
+        pressure = {"grid": [n, n], "tol": 1e-10, "labels": "fluid with random air (~25%) and solid (~5%) disks",
+                    "rhs": "divergence of N(0,1) FP32 face velocities", "timing": "CUDA events around the solve, "
+                    "inputs resident on the device, after one untimed solve"}
+        sols = {}
+        for prec in ("fp64", "mixed"):
+            ps = fs2d.FluidSim2D(psc, seed=1, precision=prec, pcg_tol=1e-10, pcg_max_iters=5000, ir_inner_tol=1e-4,
+                                 device=local)
+            ps.set_stream(stream.cuda_stream)
+            ps.set_state({"cell": pcell, "phi": pphi, "u": pu, "v": pv})
+            ps.stage("applyProjection")
+            ps.set_state({"cell": pcell, "phi": pphi, "u": pu, "v": pv})
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ps.stage("applyProjection")
+            e1.record(stream)
+            torch.cuda.synchronize()
+            st = ps.stats()
+            sols[prec] = ps.get_state(["p"])["p"]
+            pressure[prec] = {"ms": e0.elapsed_time(e1), "pcg_iterations": st["pcgIterations"],
+                              "refinement_sweeps": st["irOuterIterations"], "rel_residual": st["pcgRelResidual"]}
+            ps.close()
+        pressure["fp64_over_mixed_time"] = pressure["fp64"]["ms"] / pressure["mixed"]["ms"]
+        pressure["max_rel_diff_mixed_vs_fp64"] = float(np.abs(sols["mixed"] - sols["fp64"]).max() /
+                                                       np.abs(sols["fp64"]).max())
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -371,6 +405,7 @@ def main():
         "config": config_dict(args, n_particles, {"pcg_iterations_per_step": iters}),
         "stage_ms_last_step": stage_ms,
         "fp64_path": fp64_path,
+        "pressure_solve": pressure,
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,

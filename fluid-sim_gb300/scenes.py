@@ -64,3 +64,36 @@ def pic_dam_break_disk(nx=256, dt=None):
     if dt is None:
         dt = (1.0 / 240) * (256.0 / nx)
     return dam_break(nx, mode=PICFLIP, dt=dt, disk=(0.7, 0.7, 0.1), pic_flip_alpha=0.05)
+
+
+def pressure_disks(nx, ny=None, seed=0):
+    """Standalone pressure-solve case: a fluid background with random disks
+    of air (about 25 % of the cells) and then solid (about 5 %), a solid
+    border, a level set of -/+ (0.25..0.75) dx in fluid / non-fluid cells,
+    and face velocities drawn from N(0, 1) in FP32.  Returns
+    (scene, cell, phi, u, v) with flat arrays in the reference's layouts."""
+    ny = nx if ny is None else ny
+    rng = np.random.default_rng(seed)
+    x = (np.arange(nx) + 0.5)[None, :]
+    y = (np.arange(ny) + 0.5)[:, None]
+    cells = np.full((ny, nx), FLUID, np.uint8)
+
+    def cover(label, frac):
+        target = frac * nx * ny
+        while (cells == label).sum() < target:
+            cx, cy = rng.uniform(0, nx), rng.uniform(0, ny)
+            r = rng.uniform(0.02, 0.08) * min(nx, ny)
+            cells[(x - cx) ** 2 + (y - cy) ** 2 < r * r] = label
+
+    cover(EMPTY, 0.25)
+    cover(SOLID, 0.05)
+    cells[0, :] = cells[-1, :] = SOLID
+    cells[:, 0] = cells[:, -1] = SOLID
+    sc = dict(dam_break(nx, ny, mode=SEMILAGRANGIAN, extent=(0.0, 0.0)))
+    sc["cells"] = cells.reshape(-1)
+    dx = sc["dx"]
+    mag = (0.25 + 0.5 * rng.random((ny, nx))) * dx
+    phi = np.where(cells == FLUID, -mag, mag).reshape(-1)
+    u = rng.standard_normal((nx + 1) * ny).astype(np.float32).astype(np.float64)
+    v = rng.standard_normal(nx * (ny + 1)).astype(np.float32).astype(np.float64)
+    return sc, cells.reshape(-1), phi, u, v

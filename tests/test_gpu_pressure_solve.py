@@ -27,31 +27,7 @@ MIXED_VS_FP64_2048 = 1e-5
 
 
 def disk_scene(nx, ny, seed):
-    rng = np.random.default_rng(seed)
-    x = (np.arange(nx) + 0.5)[None, :]
-    y = (np.arange(ny) + 0.5)[:, None]
-    cells = np.full((ny, nx), scenes.FLUID, np.uint8)
-
-    def cover(label, frac):
-        target = frac * nx * ny
-        while (cells == label).sum() < target:
-            cx, cy = rng.uniform(0, nx), rng.uniform(0, ny)
-            r = rng.uniform(0.02, 0.08) * min(nx, ny)
-            cells[(x - cx) ** 2 + (y - cy) ** 2 < r * r] = label
-
-    cover(scenes.EMPTY, 0.25)
-    cover(scenes.SOLID, 0.05)
-    cells[0, :] = cells[-1, :] = scenes.SOLID
-    cells[:, 0] = cells[:, -1] = scenes.SOLID
-    sc = scenes.dam_break(nx, ny, mode=scenes.SEMILAGRANGIAN, extent=(0.0, 0.0))
-    sc = dict(sc)
-    sc["cells"] = cells.reshape(-1)
-    dx = sc["dx"]
-    mag = (0.25 + 0.5 * rng.random((ny, nx))) * dx
-    phi = np.where(cells == scenes.FLUID, -mag, mag).reshape(-1)
-    u = rng.standard_normal((nx + 1) * ny).astype(np.float32).astype(np.float64)
-    v = rng.standard_normal(nx * (ny + 1)).astype(np.float32).astype(np.float64)
-    return sc, cells.reshape(-1), phi, u, v
+    return scenes.pressure_disks(nx, ny, seed)
 
 
 def oracle_pressure(sc, cell, phi, u, v, tol):
