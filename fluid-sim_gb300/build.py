@@ -31,6 +31,7 @@ UNITS = {
     "advect.cu": ["--fmad=false"],
     "projection.cu": ["--fmad=false"],
     "projection_mixed.cu": [],
+    "render.cu": ["--fmad=false"],
 }
 
 

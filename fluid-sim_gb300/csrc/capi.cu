@@ -579,6 +579,11 @@ int fs2d_run_stage(fs2d_sim* p, int stage) {
     return rc ? rc : status;
 }
 
+int fs2d_render_export(fs2d_sim* p, fs2d_render* r) {
+    if (!p || !r) return FS2D_ERR_INVALID;
+    return render_export(&H(p)->sim, r);
+}
+
 int fs2d_solve_pressure(fs2d_sim* p, const uint8_t* cell, const double* phi, const double* u, const double* v,
                         double* pressure, fs2d_stats* stats) {
     if (!p || !cell || !phi || !u || !v || !pressure) {

@@ -235,7 +235,8 @@ int projection_build(Sim* s);             // FP64 matrix, rhs, p = 0, r = rhs, |
 int mixed_setup_maps(Sim* s);             // TMA descriptors of the FP32 MIC(0) sweeps
 int cp_setup_maps(Sim* s);                // TMA descriptors of the closest-point sweeps
 int update_velocity(Sim* s);              // updateVelocity
-int g2p(Sim* s);                          // updateParticleVelocities
+int g2p(Sim* s);
+int render_export(Sim* s, fs2d_render* r);    // headless render data (render.cu)                          // updateParticleVelocities
 int advect_particles(Sim* s);             // applyAdvection
 int diagnostics(Sim* s);                  // avgPressure, avgPressureInFluid, maxVelocity
 int extrapolate(Sim* s, double* a, uint32_t* mask, int W, int H, double* b, uint32_t* mask_b, int Wb, int Hb);

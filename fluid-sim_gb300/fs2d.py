@@ -87,6 +87,7 @@ SIGNATURES = {
     "fs2d_max_velocity": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "fs2d_solve_pressure": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p]),
+    "fs2d_render_export": (C.c_int, [C.c_void_p, C.c_void_p]),
     "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
     "fs2d_save_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
     "fs2d_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -164,6 +165,14 @@ def state_view(arrs):
     parts = arrs.get("particles")
     st.numParticles = 0 if parts is None else len(parts) // 2
     return st
+
+
+class Render(C.Structure):
+    _fields_ = [("waterCells", C.c_void_p), ("waterCap", C.c_size_t), ("waterCount", C.POINTER(C.c_size_t)),
+                ("solidCells", C.c_void_p), ("solidCap", C.c_size_t), ("solidCount", C.POINTER(C.c_size_t)),
+                ("pressureCells", C.c_void_p), ("pressureValues", C.c_void_p), ("pressureCap", C.c_size_t),
+                ("pressureCount", C.POINTER(C.c_size_t)), ("cellVels", C.c_void_p), ("particleLines", C.c_void_p),
+                ("phiValues", C.c_void_p)]
 
 
 class FluidSim2D:
@@ -245,6 +254,19 @@ class FluidSim2D:
                                         out.ctypes.data, C.byref(st))
         _check(rc, allow=(4,))
         return out, {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def render_export(self, buffers, caps):
+        """fs2d_render_export into device buffers: `buffers` maps field names
+        of fs2d_render to device pointers (ints), `caps` the list capacities;
+        returns the list counts (water, solid, pressure)."""
+        r = Render()
+        counts = [C.c_size_t(0) for _ in range(3)]
+        for k, v in buffers.items():
+            setattr(r, k, v)
+        r.waterCap, r.solidCap, r.pressureCap = caps.get("water", 0), caps.get("solid", 0), caps.get("pressure", 0)
+        r.waterCount, r.solidCount, r.pressureCount = (C.pointer(c) for c in counts)
+        _check(load().fs2d_render_export(self.h, C.byref(r)))
+        return tuple(c.value for c in counts)
 
     def set_params(self, gravityX, gravityY, picFlipAlpha, dt):
         _check(load().fs2d_set_params(self.h, gravityX, gravityY, picFlipAlpha, dt))

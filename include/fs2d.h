@@ -248,6 +248,29 @@ int fs2d_get_stage_times(fs2d_sim* sim, float* ms, int cap, int* n);
  * in the reference's formats.  Either path may be NULL to skip that file. */
 int fs2d_save_stats(fs2d_sim* sim, const char* perfPath, const char* conservationPath);
 
+/* Headless render data: what the reference's renderer gathers each frame
+ * (FluidRenderer2D::updateBuffers, demo/FluidRenderer2D.cpp:435-486),
+ * computed on the device into caller-owned DEVICE buffers (float pairs).
+ * NULL buffers are skipped; list counts are written to the host size_t's.
+ * Lists keep the reference's row-major cell order; at most `*Cap` entries
+ * are written, the count is the full one. */
+typedef struct fs2d_render {
+    float* waterCells;      /* corner (i dx, j dx) of each FLUID cell: 2 floats per cell */
+    size_t waterCap;
+    size_t* waterCount;
+    float* solidCells;      /* corner of each SOLID cell */
+    size_t solidCap;
+    size_t* solidCount;
+    float* pressureCells;   /* corner of each cell with p != 0 */
+    float* pressureValues;  /* sigmoid(0.01 p) of those cells */
+    size_t pressureCap;
+    size_t* pressureCount;
+    float* cellVels;        /* (sizeX-1)*(sizeY-1) segments: centre, centre + dt*velInterp(centre): 4 floats each */
+    float* particleLines;   /* one segment per particle: position, position + dt*velInterp(position) */
+    float* phiValues;       /* sizeX*sizeY values sigmoid(100 phi) */
+} fs2d_render;
+int fs2d_render_export(fs2d_sim* sim, fs2d_render* r);
+
 /* Use `stream` (a cudaStream_t) for all subsequent work of this handle;
  * NULL restores the handle's own stream. */
 int fs2d_set_stream(fs2d_sim* sim, void* stream);
