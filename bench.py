@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=8, help="steps of the all-FP64 path measured beside it")
     ap.add_argument("--pressure-size", type=int, default=2048,
                     help="grid of the standalone pressure-solve comparison (0: skip)")
+    ap.add_argument("--adjoint-size", type=int, default=128, help="closed-box rollout grid (0: skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=64)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
@@ -397,6 +399,45 @@ def main():
         pressure["max_rel_diff_mixed_vs_fp64"] = float(np.abs(sols["mixed"] - sols["fp64"]).max() /
                                                        np.abs(sols["fp64"]).max())
 
+    # ---- differentiable rollout: closed box, forward and hand-written adjoint ----
+    adjoint = None
+    if args.adjoint_size > 0:
+        import scenes
+        n, T = args.adjoint_size, args.adjoint_steps
+        asc = scenes.closed_box(n)
+        au0, av0 = scenes.fourier_faces(n, n, seed=1)
+        aut, avt = scenes.fourier_faces(n, n, seed=2)
+        dev = [torch.tensor(a, device=f"cuda:{local}") for a in (au0, av0, aut, avt)]
+        gdu, gdv = torch.empty_like(dev[0]), torch.empty_like(dev[1])
+        asim = fs2d.FluidSim2D(asc, seed=1, precision="fp64", pcg_tol=1e-12, pcg_max_iters=2000, device=local)
+        asim.set_stream(stream.cuda_stream)
+        ptrs = [t.data_ptr() for t in dev]
+        asim.forward(T, *ptrs)                      # warm-up pair
+        asim.backward(gdu.data_ptr(), gdv.data_ptr())
+        fwd_ms, bwd_ms, reps = 0.0, 0.0, 3
+        l0 = asim.launch_count()
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            loss = asim.forward(T, *ptrs)
+            e1.record(stream)
+            asim.backward(gdu.data_ptr(), gdv.data_ptr())
+            e2.record(stream)
+            torch.cuda.synchronize()
+            fwd_ms += e0.elapsed_time(e1)
+            bwd_ms += e1.elapsed_time(e2)
+        every = int(np.ceil(np.sqrt(T)))
+        adjoint = {"grid": [n, n], "steps": T, "checkpoint_every": every, "dt": asc["dt"], "dtype": "f64",
+                   "initial": "16-mode Fourier field, amplitude 1", "loss": loss,
+                   "forward_ms": fwd_ms / reps, "backward_ms": bwd_ms / reps,
+                   "backward_over_forward": bwd_ms / fwd_ms,
+                   "cell_steps_per_s_forward": n * n * T / (fwd_ms / reps / 1000.0),
+                   "gpu_launches_per_pair": (asim.launch_count() - l0) // reps,
+                   "timing": "CUDA events on the handle's stream, inputs resident on the device, after one untimed pair; "
+                             "backward includes recomputing the checkpointed segments"}
+        asim.close()
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -406,6 +447,7 @@ def main():
         "stage_ms_last_step": stage_ms,
         "fp64_path": fp64_path,
         "pressure_solve": pressure,
+        "adjoint": adjoint,
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,

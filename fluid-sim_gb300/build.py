@@ -32,6 +32,7 @@ UNITS = {
     "projection.cu": ["--fmad=false"],
     "projection_mixed.cu": [],
     "render.cu": ["--fmad=false"],
+    "adjoint.cu": ["--fmad=false"],
 }
 
 

@@ -331,6 +331,7 @@ int alloc_all(Sim* s) {
 }
 
 void free_all(Sim* s) {
+    rollout_free(s);
     void* ptrs[] = {s->cell, s->phi, s->p, s->u, s->v, s->nu, s->nv, s->pos, s->vel, s->t, s->seed_key,
                     s->phi_tmp, s->surface, s->u0, s->v0, s->udiv, s->vdiv, s->mask_u, s->mask_v, s->cnt_u,
                     s->cnt_v, s->fill_u, s->fill_v, s->ent_u, s->ent_v, s->scan_tmp, s->tile_range, s->max_layer,
@@ -608,6 +609,26 @@ int fs2d_solve_pressure(fs2d_sim* p, const uint8_t* cell, const double* phi, con
         if (rc) return rc;
     }
     return status;
+}
+
+int fs2d_forward(fs2d_sim* p, int steps, int checkpointEvery, const double* u0, const double* v0,
+                 const double* uTarget, const double* vTarget, double* loss) {
+    if (!p || !loss) {
+        set_error("fs2d_forward: handle and loss are required");
+        return FS2D_ERR_INVALID;
+    }
+    Host* h = H(p);
+    int rc = rollout_forward(&h->sim, steps, checkpointEvery, u0, v0, uTarget, vTarget, loss);
+    int rc2 = finish(h);
+    return rc ? rc : rc2;
+}
+
+int fs2d_backward(fs2d_sim* p, double* gradU0, double* gradV0) {
+    if (!p) return FS2D_ERR_INVALID;
+    Host* h = H(p);
+    int rc = rollout_backward(&h->sim, gradU0, gradV0);
+    int rc2 = finish(h);
+    return rc ? rc : rc2;
 }
 
 int fs2d_run_frame(fs2d_sim* p) {

@@ -175,6 +175,9 @@ struct Sim {
     int last_status = 0;
     int device = 0;
 
+    // differentiable rollout (fs2d_forward / fs2d_backward), allocated on first use
+    struct Rollout* ro = nullptr;
+
     // opt-in per-kernel event timing (fs2d_set_kernel_timing)
     std::string kt_patterns;
     std::map<const char*, bool> kt_match;
@@ -232,11 +235,12 @@ int apply_gravity(Sim* s);                // applyGravity
 int projection(Sim* s, int* status);      // applyProjection, FP64
 int projection_mixed(Sim* s, int* status);  // applyProjection, FP32 PCG in FP64 refinement
 int projection_build(Sim* s);             // FP64 matrix, rhs, p = 0, r = rhs, ||rhs||
+int projection_solve_custom(Sim* s, const double* b, int* status);  // A p = b (device b), FP64 PCG
 int mixed_setup_maps(Sim* s);             // TMA descriptors of the FP32 MIC(0) sweeps
 int cp_setup_maps(Sim* s);                // TMA descriptors of the closest-point sweeps
 int update_velocity(Sim* s);              // updateVelocity
-int g2p(Sim* s);
-int render_export(Sim* s, fs2d_render* r);    // headless render data (render.cu)                          // updateParticleVelocities
+int g2p(Sim* s);                          // updateParticleVelocities
+int render_export(Sim* s, fs2d_render* r);    // headless render data (render.cu)
 int advect_particles(Sim* s);             // applyAdvection
 int diagnostics(Sim* s);                  // avgPressure, avgPressureInFluid, maxVelocity
 int extrapolate(Sim* s, double* a, uint32_t* mask, int W, int H, double* b, uint32_t* mask_b, int Wb, int Hb);
@@ -251,6 +255,12 @@ size_t extrap_tiles(int W, int H);
 int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double* const a[2], uint32_t* const m[2],
                      const int W[2], const int H[2], int band);
 int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n);
+
+// ---- differentiable rollout (adjoint.cu) ----
+int rollout_forward(Sim* s, int steps, int every, const double* u0, const double* v0, const double* ut,
+                    const double* vt, double* loss);
+int rollout_backward(Sim* s, double* gu, double* gv);
+void rollout_free(Sim* s);
 
 // ---- wavefront plumbing ----
 // Reserves `n` progress counters and returns the base value for this launch.

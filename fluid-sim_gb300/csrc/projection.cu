@@ -383,7 +383,43 @@ __global__ void k_diag(const uint8_t* __restrict__ cell, const double* __restric
     }
 }
 
+// A caller-supplied right-hand side b on the fluid cells (0 elsewhere): r = b,
+// p = 0 and the solver scalars reset as k_build does for the physical one.
+__global__ void k_custom_rhs(const uint8_t* __restrict__ cell, const double* __restrict__ b, double* rhs, double* r,
+                             double* p, size_t N, double* partial, PcgScalars* pcg, double tol) {
+    __shared__ double sh[32];
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    double bn = 0.0;
+    if (c < N) {
+        const double v = cell[c] == kFluid ? b[c] : 0.0;
+        rhs[c] = v;
+        r[c] = v;
+        p[c] = 0.0;
+        bn = fabs(v);
+    }
+    double m = block_max(bn, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = m;
+    if (last_block(&pcg->ticket[0])) {
+        double mm = 0;
+        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) mm = fmax(mm, partial[k]);
+        mm = block_max(mm, sh);
+        if (threadIdx.x == 0) {
+            pcg->rhs_norm = mm;
+            pcg->tol_abs = tol * mm;
+            pcg->r_norm = mm;
+            pcg->iter = 0;
+            pcg->done = 0;
+            pcg->first = 1;
+            pcg->sigma = 0;
+            pcg->alpha = 0;
+            pcg->beta = 0;
+        }
+    }
+}
+
 }  // namespace
+
+static int projection_pcg(Sim* s, int* status);
 
 int projection_build(Sim* s) {
     const double scaleA = s->dt / (s->rho * s->dx * s->dx);
@@ -393,13 +429,26 @@ int projection_build(Sim* s) {
 }
 
 int projection(Sim* s, int* status) {
+    int rc0 = projection_build(s);
+    if (rc0) return rc0;
+    return projection_pcg(s, status);
+}
+
+// A p = b for a caller-supplied device array b (the matrix of the current
+// labels and level set); the solution is left in s->p.
+int projection_solve_custom(Sim* s, const double* b, int* status) {
+    int rc0 = projection_build(s);
+    if (rc0) return rc0;
+    FS2D_LAUNCH(s, k_custom_rhs, blocks_for(s->N, kT), kT, 0, s->cell, b, s->rhs, s->r, s->p, s->N, s->partial,
+                s->pcg, s->opt.pcg_tol);
+    return projection_pcg(s, status);
+}
+
+// MIC(0) factor and the PCG loop on the built system (rhs, r, p = 0).
+static int projection_pcg(Sim* s, int* status) {
     const int NX = s->NX, NY = s->NY;
     const size_t N = s->N;
     const unsigned nb = blocks_for(N, kT);
-    {
-        int rc0 = projection_build(s);
-        if (rc0) return rc0;
-    }
     {
         MicFactor64 op{{s->Adiag, s->Ax - 1, s->Ay - 1, s->Ay - NX, s->Ax - NX}, s->precon, NX, s->opt.mic_tau,
                        s->opt.mic_sigma};

@@ -88,6 +88,9 @@ SIGNATURES = {
     "fs2d_solve_pressure": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p]),
     "fs2d_render_export": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fs2d_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.POINTER(C.c_double)]),
+    "fs2d_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
     "fs2d_save_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
     "fs2d_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -254,6 +257,39 @@ class FluidSim2D:
                                         out.ctypes.data, C.byref(st))
         _check(rc, allow=(4,))
         return out, {k: getattr(st, k) for k, _ in Stats._fields_}
+
+    def forward(self, steps, u0, v0, u_target, v_target, checkpoint_every=0):
+        """Differentiable rollout of `steps` semi-Lagrangian velocity steps
+        from (u0, v0) on the scene's fixed labels; returns the loss
+        ||(u_T, v_T) - (u_target, v_target)||_2.  Arrays are host numpy
+        arrays or device addresses (ints)."""
+        NX, NY = self.nx, self.ny
+        keep = []
+
+        def ptr(a, n):
+            if isinstance(a, int):
+                return a
+            a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+            assert a.size == n
+            keep.append(a)
+            return a.ctypes.data
+
+        NU, NV = (NX + 1) * NY, NX * (NY + 1)
+        loss = C.c_double(0.0)
+        _check(load().fs2d_forward(self.h, int(steps), int(checkpoint_every), ptr(u0, NU), ptr(v0, NV),
+                                   ptr(u_target, NU), ptr(v_target, NV), C.byref(loss)))
+        return loss.value
+
+    def backward(self, grad_u=None, grad_v=None):
+        """dL/du0, dL/dv0 of the last forward(); into the given device
+        addresses, else returned as numpy arrays."""
+        NX, NY = self.nx, self.ny
+        if grad_u is not None:
+            _check(load().fs2d_backward(self.h, grad_u, grad_v))
+            return None
+        gu, gv = np.empty((NX + 1) * NY), np.empty(NX * (NY + 1))
+        _check(load().fs2d_backward(self.h, gu.ctypes.data, gv.ctypes.data))
+        return gu, gv
 
     def render_export(self, buffers, caps):
         """fs2d_render_export into device buffers: `buffers` maps field names

@@ -97,3 +97,39 @@ def pressure_disks(nx, ny=None, seed=0):
     u = rng.standard_normal((nx + 1) * ny).astype(np.float32).astype(np.float64)
     v = rng.standard_normal(nx * (ny + 1)).astype(np.float32).astype(np.float64)
     return sc, cells.reshape(-1), phi, u, v
+
+
+def closed_box(nx, ny=None, *, dt=1.0 / 60, rho=997.0, gravity=(0.0, 0.0)):
+    """A closed box of fluid: every interior cell FLUID inside the one-cell
+    SOLID border, semi-Lagrangian mode, one particle per cell (the velocity
+    rollout does not use them)."""
+    ny = nx if ny is None else ny
+    sc = dam_break(nx, ny, mode=SEMILAGRANGIAN, dt=dt, extent=(2.0, 2.0), ppc_sqrt=1, rho=rho, gravity=gravity)
+    return sc
+
+
+def fourier_faces(nx, ny, seed, modes=16, amplitude=1.0):
+    """A smooth random face-velocity field (u, v): each component is a sum of
+    `modes` plane waves a sin(2 pi (kx x + ky y) + phase) with integer wave
+    numbers 1..4, N(0, 1) amplitudes and uniform phases, scaled so that its
+    largest magnitude over the faces is `amplitude`.  Evaluated at the face
+    centres of a unit-width grid (dx = 1/nx): u at (i dx, (j + .5) dx), v at
+    ((i + .5) dx, j dx)."""
+    rng = np.random.default_rng(seed)
+    dx = 1.0 / nx
+
+    def field(x, y):
+        k = rng.integers(1, 5, size=(modes, 2))
+        a = rng.standard_normal(modes)
+        ph = rng.uniform(0, 2 * np.pi, modes)
+        f = np.zeros(np.broadcast(x, y).shape)
+        for m in range(modes):
+            f += a[m] * np.sin(2 * np.pi * (k[m, 0] * x + k[m, 1] * y) + ph[m])
+        return f
+
+    iu, ju = np.meshgrid(np.arange(nx + 1), np.arange(ny))
+    u = field(iu * dx, (ju + 0.5) * dx)
+    iv, jv = np.meshgrid(np.arange(nx), np.arange(ny + 1))
+    v = field((iv + 0.5) * dx, jv * dx)
+    s = amplitude / max(np.abs(u).max(), np.abs(v).max())
+    return (u * s).reshape(-1), (v * s).reshape(-1)

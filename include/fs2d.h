@@ -179,6 +179,26 @@ int fs2d_run_frame(fs2d_sim* sim);
 int fs2d_solve_pressure(fs2d_sim* sim, const uint8_t* cell, const double* phi, const double* u, const double* v,
                         double* pressure, fs2d_stats* stats);
 
+/* Differentiable rollout.  No reference counterpart: the reference has no
+ * derivatives.  The forward pass is the semi-Lagrangian frame's velocity
+ * stages (applySemiLagrangianAdvection, applyGravity, applyProjection in
+ * FP64, updateVelocity; src/FluidSim2D.cpp:100-113) repeated `steps` times
+ * from the face velocities (u0, v0), on the handle's fixed labels, which may
+ * hold no EMPTY cell (a closed box: the projection is then a fixed linear
+ * map).  The loss is the L2 distance sqrt(sum (u_T - uTarget)^2 +
+ * sum (v_T - vTarget)^2) over all faces.  The state before every
+ * `checkpointEvery`-th step is kept (0: ceil(sqrt(steps))).
+ *
+ * fs2d_backward then writes dL/du_0 and dL/dv_0 (reverse mode, hand-written
+ * adjoint kernels), recomputing each segment from its checkpoint.  The
+ * handle's u and v afterwards hold an intermediate state.  All pointers may
+ * be host or device memory; sizes are the handle's face grids.
+ * FS2D_ERR_INVALID for a mode other than FS2D_SEMILAGRANGIAN or a scene with
+ * an EMPTY cell; FS2D_ERR_NOT_CONVERGED if a pressure solve hit its cap. */
+int fs2d_forward(fs2d_sim* sim, int steps, int checkpointEvery, const double* u0, const double* v0,
+                 const double* uTarget, const double* vTarget, double* loss);
+int fs2d_backward(fs2d_sim* sim, double* gradU0, double* gradV0);
+
 /* Runs `nframes` frames back to back without host synchronisation between them
  * (except the pressure solver's convergence polls). */
 int fs2d_step(fs2d_sim* sim, int nframes);
