@@ -64,6 +64,8 @@ def parse():
                     help="grid of the standalone pressure-solve comparison (0: skip)")
     ap.add_argument("--adjoint-size", type=int, default=128, help="closed-box rollout grid (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=64)
+    ap.add_argument("--batch-scenes", type=int, default=256, help="batched dam breaks (0: skip)")
+    ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
@@ -438,6 +440,42 @@ def main():
                              "backward includes recomputing the checkpointed segments"}
         asim.close()
 
+    # ---- batch: independent PIC/FLIP dam breaks of uneven sizes ----
+    batch = None
+    if args.batch_scenes > 0:
+        import scenes
+        bscs = scenes.batch_dam_breaks(args.batch_scenes, seed=SEED)
+        bcells = sum(sc["sizeX"] * sc["sizeY"] for sc in bscs)
+        bt = fs2d.Batch(bscs, workers=0, seed=SEED, precision="mixed", pcg_tol=args.tol, pcg_max_iters=200,
+                        device=local)
+        t0 = time.perf_counter()
+        bt.step(max(args.warmup, 3))                 # the first frames choose the worker count
+        warm_s = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        l0 = sum(bt.scene(k).launch_count() for k in range(len(bscs)))
+        t0 = time.perf_counter()
+        bt.step(args.batch_steps)
+        torch.cuda.synchronize()
+        conc_s = time.perf_counter() - t0
+        l1 = sum(bt.scene(k).launch_count() for k in range(len(bscs)))
+        workers = bt.workers
+        bt.workers = 1
+        t0 = time.perf_counter()
+        bt.step(1)
+        torch.cuda.synchronize()
+        seq_s = time.perf_counter() - t0
+        sides = sorted(sc["sizeX"] for sc in bscs)
+        batch = {"scenes": len(bscs), "cells": bcells, "side_min": sides[0], "side_median": sides[len(sides) // 2],
+                 "side_max": sides[-1], "steps": args.batch_steps, "workers": workers,
+                 "value": bcells * args.batch_steps / conc_s, "unit": UNIT,
+                 "ms_per_batch_step": 1000.0 * conc_s / args.batch_steps,
+                 "sequential_value": bcells / seq_s, "concurrency_speedup": seq_s / (conc_s / args.batch_steps),
+                 "gpu_launches_per_batch_step": (l1 - l0) // max(args.batch_steps, 1),
+                 "warmup_s": warm_s,
+                 "timing": "host wall clock around fs2d_batch_step (each frame returns after its device work); "
+                           "sequential = the same batch with one worker, one step"}
+        bt.close()
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -448,6 +486,7 @@ def main():
         "fp64_path": fp64_path,
         "pressure_solve": pressure,
         "adjoint": adjoint,
+        "batch": batch,
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,

@@ -33,6 +33,7 @@ UNITS = {
     "projection_mixed.cu": [],
     "render.cu": ["--fmad=false"],
     "adjoint.cu": ["--fmad=false"],
+    "batch.cu": [],
 }
 
 

@@ -264,15 +264,9 @@ int launch_wave(Sim* s, const Op& op, WaveGeom g, const int* skip) {
     // One strip per SM: the strips of a sweep run concurrently and, on GB300,
     // strips sharing an SM contend for its small FP64 pipe.  Reserving more
     // than half of the SM's shared memory keeps every strip on its own SM.
-    static bool configured = false;
     const int kReserve = 120 * 1024;
-    if (!configured) {
-        int rc0 = check_cuda(cudaFuncSetAttribute((const void*)wave_kernel<Op>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, kReserve),
-                             "cudaFuncSetAttribute");
-        if (rc0) return rc0;
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)wave_kernel<Op>, kReserve)) return rc0;
     unsigned long long base = wave_begin(s);
     void* args[] = {(void*)&op, (void*)&g, (void*)&s->progress, (void*)&base, (void*)&s->err, (void*)&skip};
     s->launches++;

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stddef.h>
+#include <atomic>
 #include <map>
 #include <string>
 #include <utility>
@@ -224,6 +225,18 @@ cudaError_t launch_clustered(const void* kernel, int nblocks, int cluster, int t
 // Largest cluster size (<= 8) with which every cluster of a grid of
 // `nblocks` blocks can be co-resident; 1 when clusters are not usable.
 int choose_cluster(const void* kernel, int nblocks, int threads, size_t smem);
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per kernel and
+// device; `done` is the kernel's own bit set of configured devices.  Safe
+// from several host threads (batches drive their scenes concurrently).
+inline int ensure_smem_attr(std::atomic<unsigned long long>& done, int device, const void* fn, int bytes) {
+    const unsigned long long bit = 1ull << (device & 63);
+    if (done.load(std::memory_order_acquire) & bit) return 0;
+    int rc = check_cuda(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes),
+                        "cudaFuncSetAttribute");
+    if (!rc) done.fetch_or(bit, std::memory_order_acq_rel);
+    return rc;
+}
 
 inline unsigned int blocks_for(size_t n, int threads) { return (unsigned int)((n + threads - 1) / threads); }
 

@@ -304,14 +304,8 @@ static int launch_cp_sweep_dir(Sim* s, const int* skip) {
         set_error("closest-point sweep: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
         return FS2D_ERR_INVALID;
     }
-    static bool configured = false;
-    if (!configured) {
-        int rc0 = check_cuda(cudaFuncSetAttribute((const void*)cp_sweep_kernel<SX, SY>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kCpSmem),
-                             "cudaFuncSetAttribute");
-        if (rc0) return rc0;
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)cp_sweep_kernel<SX, SY>, (int)kCpSmem)) return rc0;
     CpArgs a;
     a.pos_df = s->pos_df;
     a.pos = s->pos;
@@ -348,14 +342,8 @@ static int launch_eik_sweep_dir(Sim* s, const WaveGeom& g, const int* skip) {
         set_error("Eikonal sweep: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
         return FS2D_ERR_INVALID;
     }
-    static bool configured = false;
-    if (!configured) {
-        int rc0 = check_cuda(cudaFuncSetAttribute((const void*)eik_sweep_kernel<SX, SY>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kEkSmem),
-                             "cudaFuncSetAttribute");
-        if (rc0) return rc0;
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)eik_sweep_kernel<SX, SY>, (int)kEkSmem)) return rc0;
     EkArgs a;
     a.hb = reinterpret_cast<double2*>(s->cp_hb_p);
     a.progress = s->progress;

@@ -402,14 +402,8 @@ int launch_mic32(Sim* s, const Mic32Maps& maps, float* out, const int* skip) {
         set_error("mic32: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
         return FS2D_ERR_INVALID;
     }
-    static bool configured = false;
-    if (!configured) {
-        int rc0 = check_cuda(cudaFuncSetAttribute((const void*)mic32_kernel<FWD>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kM32Smem),
-                             "cudaFuncSetAttribute");
-        if (rc0) return rc0;
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)mic32_kernel<FWD>, (int)kM32Smem)) return rc0;
     unsigned long long base = wave_begin(s);
     int P = s->P, NY = s->NY;
     void* args[] = {(void*)&maps, (void*)&out, (void*)&P, (void*)&NY, (void*)&s->progress, (void*)&base,

@@ -325,14 +325,8 @@ int launch_wave2(Sim* s, const Op& op, WaveGeom g, const int* skip) {
         return FS2D_ERR_INVALID;
     }
     constexpr size_t smem = wave2_smem_bytes<Op, W, CH>();
-    static bool configured = false;
-    if (!configured) {
-        int rc0 = check_cuda(cudaFuncSetAttribute((const void*)wave2_kernel<Op, W, CH>,
-                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem),
-                             "cudaFuncSetAttribute");
-        if (rc0) return rc0;
-        configured = true;
-    }
+    static std::atomic<unsigned long long> configured{0};
+    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)wave2_kernel<Op, W, CH>, (int)smem)) return rc0;
     unsigned long long base = wave_begin(s);
     void* args[] = {(void*)&op, (void*)&g, (void*)&s->progress, (void*)&base, (void*)&s->err, (void*)&skip};
     s->launches++;

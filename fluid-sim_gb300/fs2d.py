@@ -91,6 +91,13 @@ SIGNATURES = {
     "fs2d_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.POINTER(C.c_double)]),
     "fs2d_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fs2d_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "fs2d_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "fs2d_batch_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "fs2d_batch_scene": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
+    "fs2d_batch_workers": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "fs2d_batch_set_workers": (C.c_int, [C.c_void_p, C.c_int]),
+    "fs2d_batch_destroy": (C.c_int, [C.c_void_p]),
     "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
     "fs2d_save_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
     "fs2d_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -369,7 +376,76 @@ class FluidSim2D:
 
     def close(self):
         if getattr(self, "h", None):
-            load().fs2d_destroy(self.h)
+            if getattr(self, "_owned", True):
+                load().fs2d_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @classmethod
+    def _view(cls, handle, scene):
+        """A non-owning wrapper of a handle that a batch owns."""
+        self = cls.__new__(cls)
+        self.nx, self.ny, self.mode = scene["sizeX"], scene["sizeY"], scene["mode"]
+        self.h = handle
+        self._owned = False
+        return self
+
+
+class Batch:
+    """fs2d_batch: independent scenes advanced together by `workers` host
+    threads (0: chosen on the first frames).  With use_seed, scene k is
+    seeded with seed + k."""
+
+    def __init__(self, scenes, workers=0, seed=None, **options):
+        lib = load()
+        self.scenes = list(scenes)
+        n = len(self.scenes)
+        self.cfgs = (Config * n)()
+        self._keep = []
+        for k, sc in enumerate(self.scenes):
+            cfg = make_config(sc)
+            self._keep.append(cfg._keep)
+            self.cfgs[k] = cfg
+        if seed is not None:
+            options.setdefault("use_seed", 1)
+            options.setdefault("seed", seed)
+        self.opt = default_options(**options)
+        h = C.c_void_p()
+        _check(lib.fs2d_batch_create(C.cast(self.cfgs, C.c_void_p), n, C.byref(self.opt), int(workers), C.byref(h)))
+        self.h = h
+
+    def step(self, nframes=1):
+        return _check(load().fs2d_batch_step(self.h, int(nframes)), allow=(4,))
+
+    def __len__(self):
+        n = C.c_int()
+        _check(load().fs2d_batch_size(self.h, C.byref(n)))
+        return n.value
+
+    def scene(self, k):
+        """Scene k as a FluidSim2D view (state, statistics); owned by the batch."""
+        h = C.c_void_p()
+        _check(load().fs2d_batch_scene(self.h, int(k), C.byref(h)))
+        return FluidSim2D._view(h, self.scenes[k])
+
+    @property
+    def workers(self):
+        w = C.c_int()
+        _check(load().fs2d_batch_workers(self.h, C.byref(w)))
+        return w.value
+
+    @workers.setter
+    def workers(self, w):
+        _check(load().fs2d_batch_set_workers(self.h, int(w)))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().fs2d_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -133,3 +133,17 @@ def fourier_faces(nx, ny, seed, modes=16, amplitude=1.0):
     v = field((iv + 0.5) * dx, jv * dx)
     s = amplitude / max(np.abs(u).max(), np.abs(v).max())
     return (u * s).reshape(-1), (v * s).reshape(-1)
+
+
+def batch_dam_breaks(count, seed=0, lo=64, hi=512):
+    """Independent PIC/FLIP dam breaks of uneven sizes: square grids with a
+    side drawn log-uniformly from [lo, hi], fluid block extents (x and y)
+    uniform in [0.2, 0.6], 4 particles per cell, FLIP ratio 0.95, dt =
+    1/240 scaled by 256/side (the CFL number of the 256^2 scene)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+        ex, ey = rng.uniform(0.2, 0.6, 2)
+        out.append(dam_break(n, mode=PICFLIP, dt=(1.0 / 240) * (256.0 / n), extent=(ex, ey), pic_flip_alpha=0.05))
+    return out

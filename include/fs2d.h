@@ -199,6 +199,30 @@ int fs2d_forward(fs2d_sim* sim, int steps, int checkpointEvery, const double* u0
                  const double* uTarget, const double* vTarget, double* loss);
 int fs2d_backward(fs2d_sim* sim, double* gradU0, double* gradV0);
 
+/* Batches of independent scenes.  No reference counterpart (the reference
+ * runs one scene per process).  fs2d_batch_create makes one handle per
+ * scene (cfgs[k], all with the options `opt`, which may be NULL; with
+ * use_seed, scene k is seeded with seed + k) in order, each on its own CUDA
+ * stream.  fs2d_batch_step advances every scene by `nframes` frames
+ * (fs2d_run_frame each) with `workers` host threads issuing the scenes'
+ * frames concurrently, scenes assigned longest-first to the least-loaded
+ * thread; workers = 0 lets the first frames choose the count (one frame
+ * timed per candidate; those are ordinary frames of the run).  A scene's
+ * results do not depend on the worker count.  fs2d_batch_step starts and
+ * joins its threads within the call; it returns the first error, or
+ * FS2D_ERR_NOT_CONVERGED if a scene's last pressure solve hit its cap.
+ * At most min(scenes, 64) workers are used.
+ * fs2d_batch_scene gives scene k's handle for the per-scene calls (state,
+ * statistics); do not destroy it or use it during fs2d_batch_step. */
+typedef struct fs2d_batch fs2d_batch;
+int fs2d_batch_create(const fs2d_config* cfgs, int n, const fs2d_options* opt, int workers, fs2d_batch** out);
+int fs2d_batch_step(fs2d_batch* batch, int nframes);
+int fs2d_batch_size(fs2d_batch* batch, int* n);
+int fs2d_batch_scene(fs2d_batch* batch, int k, fs2d_sim** sim);
+int fs2d_batch_workers(fs2d_batch* batch, int* workers);   /* 0 until chosen */
+int fs2d_batch_set_workers(fs2d_batch* batch, int workers); /* 0: choose again on the next frames */
+int fs2d_batch_destroy(fs2d_batch* batch);
+
 /* Runs `nframes` frames back to back without host synchronisation between them
  * (except the pressure solver's convergence polls). */
 int fs2d_step(fs2d_sim* sim, int nframes);

@@ -1,0 +1,63 @@
+"""Batches of independent scenes (fs2d_batch_*): PIC/FLIP dam breaks of
+uneven sizes advanced concurrently by host worker threads, each scene on
+its own stream.  Every scene's state after the batch's frames must equal,
+bit for bit, the state of the same scene run alone through fs2d_run_frame
+(same seed), whatever the worker count, including the count the batch
+chooses itself on its first frames."""
+import numpy as np
+import pytest
+
+fs2d = pytest.importorskip("fs2d")
+scenes = pytest.importorskip("scenes")
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("cell", "phi", "p", "u", "v", "particles", "particleVels")
+OPTS = dict(precision="mixed", pcg_tol=1e-6)
+
+
+def alone(sc, seed, frames):
+    sim = fs2d.FluidSim2D(sc, seed=seed, **OPTS)
+    sim.step(frames)
+    st = sim.get_state(FIELDS)
+    sim.close()
+    return st
+
+
+def assert_same(a, b):
+    for f in FIELDS:
+        assert np.array_equal(a[f], b[f]), f
+
+
+@pytest.mark.parametrize("workers", [1, 3])
+def test_batch_matches_scenes_run_alone(workers):
+    scs = scenes.batch_dam_breaks(5, seed=7, lo=40, hi=100)
+    b = fs2d.Batch(scs, workers=workers, seed=100, **OPTS)
+    assert len(b) == 5 and b.workers == workers
+    b.step(3)
+    for k, sc in enumerate(scs):
+        assert_same(b.scene(k).get_state(FIELDS), alone(sc, 100 + k, 3))
+        assert b.scene(k).stats()["frames"] == 3
+    b.close()
+
+
+def test_batch_chooses_its_worker_count():
+    scs = scenes.batch_dam_breaks(12, seed=8, lo=32, hi=72)
+    b = fs2d.Batch(scs, workers=0, seed=5, **OPTS)
+    assert b.workers == 0
+    b.step(4)
+    assert b.workers in (4, 8, 16, 32) or 1 <= b.workers <= 12
+    for k in (0, 5, 11):
+        assert_same(b.scene(k).get_state(FIELDS), alone(scs[k], 5 + k, 4))
+    b.close()
+
+
+def test_batch_rejects_bad_arguments():
+    scs = scenes.batch_dam_breaks(2, seed=1, lo=32, hi=40)
+    with pytest.raises(fs2d.FS2DError):
+        fs2d.Batch([], workers=1)
+    with pytest.raises(fs2d.FS2DError):
+        fs2d.Batch(scs, workers=-1)
+    b = fs2d.Batch(scs, workers=2, seed=1)
+    with pytest.raises(fs2d.FS2DError):
+        b.scene(2)
+    b.close()
