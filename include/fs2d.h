@@ -10,8 +10,9 @@
  * fallback: if no CUDA device is usable, fs2d_create fails with
  * FS2D_ERR_CUDA.
  *
- * Threading: a handle is used by one host thread at a time; the library
- * starts no host threads.
+ * Threading: a handle is used by one host thread at a time; different
+ * handles may be used from different threads at once.  The library starts
+ * host threads only inside fs2d_batch_step and joins them before returning.
  *
  * Layout conventions follow the reference exactly:
  *   - grids are row-major, element (i, j) at index j*NX + i
