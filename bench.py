@@ -411,34 +411,40 @@ def main():
         aut, avt = scenes.fourier_faces(n, n, seed=2)
         dev = [torch.tensor(a, device=f"cuda:{local}") for a in (au0, av0, aut, avt)]
         gdu, gdv = torch.empty_like(dev[0]), torch.empty_like(dev[1])
-        asim = fs2d.FluidSim2D(asc, seed=1, precision="fp64", pcg_tol=1e-12, pcg_max_iters=2000, device=local)
-        asim.set_stream(stream.cuda_stream)
         ptrs = [t.data_ptr() for t in dev]
-        asim.forward(T, *ptrs)                      # warm-up pair
-        asim.backward(gdu.data_ptr(), gdv.data_ptr())
-        fwd_ms, bwd_ms, reps = 0.0, 0.0, 3
-        l0 = asim.launch_count()
-        for _ in range(reps):
-            torch.cuda.synchronize()
-            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
-            e0.record(stream)
-            loss = asim.forward(T, *ptrs)
-            e1.record(stream)
-            asim.backward(gdu.data_ptr(), gdv.data_ptr())
-            e2.record(stream)
-            torch.cuda.synchronize()
-            fwd_ms += e0.elapsed_time(e1)
-            bwd_ms += e1.elapsed_time(e2)
         every = int(np.ceil(np.sqrt(T)))
-        adjoint = {"grid": [n, n], "steps": T, "checkpoint_every": every, "dt": asc["dt"], "dtype": "f64",
-                   "initial": "16-mode Fourier field, amplitude 1", "loss": loss,
-                   "forward_ms": fwd_ms / reps, "backward_ms": bwd_ms / reps,
-                   "backward_over_forward": bwd_ms / fwd_ms,
-                   "cell_steps_per_s_forward": n * n * T / (fwd_ms / reps / 1000.0),
-                   "gpu_launches_per_pair": (asim.launch_count() - l0) // reps,
-                   "timing": "CUDA events on the handle's stream, inputs resident on the device, after one untimed pair; "
-                             "backward includes recomputing the checkpointed segments"}
-        asim.close()
+        adjoint = {"grid": [n, n], "steps": T, "checkpoint_every": every, "dt": asc["dt"], "pcg_tol": 1e-12,
+                   "initial": "16-mode Fourier field, amplitude 1",
+                   "timing": "CUDA events on the handle's stream, inputs resident on the device, after one untimed "
+                             "pair, mean of 3; backward includes recomputing the checkpointed segments"}
+        grads = {}
+        for prec in ("mixed", "fp64"):
+            asim = fs2d.FluidSim2D(asc, seed=1, precision=prec, pcg_tol=1e-12, pcg_max_iters=2000, device=local)
+            asim.set_stream(stream.cuda_stream)
+            asim.forward(T, *ptrs)                      # warm-up pair
+            asim.backward(gdu.data_ptr(), gdv.data_ptr())
+            fwd_ms, bwd_ms, reps = 0.0, 0.0, 3
+            l0 = asim.launch_count()
+            for _ in range(reps):
+                torch.cuda.synchronize()
+                e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+                e0.record(stream)
+                loss = asim.forward(T, *ptrs)
+                e1.record(stream)
+                asim.backward(gdu.data_ptr(), gdv.data_ptr())
+                e2.record(stream)
+                torch.cuda.synchronize()
+                fwd_ms += e0.elapsed_time(e1)
+                bwd_ms += e1.elapsed_time(e2)
+            grads[prec] = torch.cat([gdu, gdv]).cpu().numpy()
+            adjoint[prec] = {"loss": loss, "forward_ms": fwd_ms / reps, "backward_ms": bwd_ms / reps,
+                             "backward_over_forward": bwd_ms / fwd_ms,
+                             "cell_steps_per_s_forward": n * n * T / (fwd_ms / reps / 1000.0),
+                             "gpu_launches_per_pair": (asim.launch_count() - l0) // reps}
+            asim.close()
+        adjoint["backward_over_forward"] = adjoint["mixed"]["backward_over_forward"]
+        adjoint["max_rel_diff_grad_mixed_vs_fp64"] = float(np.abs(grads["mixed"] - grads["fp64"]).max() /
+                                                           np.abs(grads["fp64"]).max())
 
     # ---- batch: independent PIC/FLIP dam breaks of uneven sizes ----
     batch = None

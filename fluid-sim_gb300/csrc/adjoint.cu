@@ -5,7 +5,8 @@
 // Forward step k (the reference's SL-mode stages without the level set and
 // particles): u* = SL(u_k) (applySemiLagrangianAdvection, src/FluidSim2D.cpp:
 // 206-235, double-buffered), + dt g (applyGravity), p = A^-1 b(u*)
-// (applyProjection :252-467), u_{k+1} = E(W(u*, p)) (updateVelocity :469-550:
+// (applyProjection :252-467, FP64 PCG or FP32 PCG inside FP64 refinement,
+// solved to the handle's tolerance), u_{k+1} = E(W(u*, p)) (updateVelocity :469-550:
 // W zeroes the faces next to a solid cell, subtracts dt/(rho dx) grad p on
 // fluid-fluid faces and keeps u* on the faces the loop never visits; E is
 // Array2D::extrapolate of the faces without a fluid side).
@@ -17,7 +18,7 @@
 //   W^T     u*bar = mu on fluid-fluid and never-visited faces, 0 on faces
 //           next to a solid; pbar = -dt/(rho dx) G^T mu on fluid-fluid faces;
 //   A^-T    bbar = A^-1 pbar (A is symmetric: a second Poisson solve with the
-//           same matrix and preconditioner);
+//           same matrix, preconditioner and precision);
 //   B^T     u*bar += the transposed divergence of the right-hand side
 //           (faces next to a solid do not enter it);
 //   SL^T    per face, the RK3 back-trace in reverse: the sampled value
@@ -322,14 +323,15 @@ int ro_alloc(double** p, size_t n) {
 }
 
 // One forward step of the rollout: the semi-Lagrangian frame's velocity
-// stages (applySemiLagrangianAdvection, applyGravity, applyProjection in
-// FP64, updateVelocity; src/FluidSim2D.cpp:100-113).  The labels are fixed,
-// so createWaterLevelSet and applyAdvection (particles) do not enter.
+// stages (applySemiLagrangianAdvection, applyGravity, applyProjection with
+// the handle's precision, updateVelocity; src/FluidSim2D.cpp:100-113).  The
+// labels are fixed, so createWaterLevelSet and applyAdvection (particles)
+// do not enter.
 int forward_step(Sim* s) {
     int rc = sl_advect(s);
     if (!rc) rc = apply_gravity(s);
     int status = 0;
-    if (!rc) rc = projection(s, &status);
+    if (!rc) rc = s->opt.precision == FS2D_PRECISION_MIXED ? projection_mixed(s, &status) : projection(s, &status);
     if (!rc) rc = update_velocity(s);
     if (!rc && status) {
         set_error("rollout: the pressure solve hit its iteration cap");

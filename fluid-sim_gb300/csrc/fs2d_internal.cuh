@@ -248,7 +248,9 @@ int apply_gravity(Sim* s);                // applyGravity
 int projection(Sim* s, int* status);      // applyProjection, FP64
 int projection_mixed(Sim* s, int* status);  // applyProjection, FP32 PCG in FP64 refinement
 int projection_build(Sim* s);             // FP64 matrix, rhs, p = 0, r = rhs, ||rhs||
-int projection_solve_custom(Sim* s, const double* b, int* status);  // A p = b (device b), FP64 PCG
+int projection_set_rhs(Sim* s, const double* b);   // after projection_build: rhs = r = b, p = 0
+int projection_solve_custom(Sim* s, const double* b, int* status);  // A p = b (device b), handle's precision
+int projection_mixed_rhs(Sim* s, const double* b, int* status);     // mixed solve; b == nullptr: physical rhs
 int mixed_setup_maps(Sim* s);             // TMA descriptors of the FP32 MIC(0) sweeps
 int cp_setup_maps(Sim* s);                // TMA descriptors of the closest-point sweeps
 int update_velocity(Sim* s);              // updateVelocity

@@ -434,13 +434,22 @@ int projection(Sim* s, int* status) {
     return projection_pcg(s, status);
 }
 
-// A p = b for a caller-supplied device array b (the matrix of the current
-// labels and level set); the solution is left in s->p.
-int projection_solve_custom(Sim* s, const double* b, int* status) {
-    int rc0 = projection_build(s);
-    if (rc0) return rc0;
+// Replaces the built right-hand side by a caller-supplied device array b
+// (fluid cells; 0 elsewhere), with r = b, p = 0 and the solver scalars reset.
+int projection_set_rhs(Sim* s, const double* b) {
     FS2D_LAUNCH(s, k_custom_rhs, blocks_for(s->N, kT), kT, 0, s->cell, b, s->rhs, s->r, s->p, s->N, s->partial,
                 s->pcg, s->opt.pcg_tol);
+    return 0;
+}
+
+// A p = b for a caller-supplied device array b (the matrix of the current
+// labels and level set), with the handle's precision; the solution is left
+// in s->p.
+int projection_solve_custom(Sim* s, const double* b, int* status) {
+    if (s->opt.precision == FS2D_PRECISION_MIXED) return projection_mixed_rhs(s, b, status);
+    int rc0 = projection_build(s);
+    if (rc0) return rc0;
+    if ((rc0 = projection_set_rhs(s, b))) return rc0;
     return projection_pcg(s, status);
 }
 

@@ -358,7 +358,11 @@ int mixed_setup_maps(Sim* s) {
     return 0;
 }
 
-int projection_mixed(Sim* s, int* status) {
+int projection_mixed(Sim* s, int* status) { return projection_mixed_rhs(s, nullptr, status); }
+
+// b == nullptr: the physical right-hand side; otherwise A p = b for a device
+// array b on the fluid cells.
+int projection_mixed_rhs(Sim* s, const double* b, int* status) {
     const int NX = s->NX, NY = s->NY, P = s->P;
     const size_t N = s->N;
     const unsigned nb = blocks_for(N, kT);
@@ -366,6 +370,7 @@ int projection_mixed(Sim* s, int* status) {
     // the FP64 matrix, rhs, ||b||inf, p = 0, r = b (exactly the reference's)
     int rc = projection_build(s);
     if (rc) return rc;
+    if (b && (rc = projection_set_rhs(s, b))) return rc;
     FS2D_LAUNCH(s, k_mixed_matrix, nb, kT, 0, s->Adiag, s->Ax, s->Ay, m.a0, m.ax, m.ay, NX, P, N);
     {
         MicFactor32 op{{m.a0, m.ax - 1, m.ay - 1, m.ay - P, m.ax - P}, m.pc, P, (float)s->opt.mic_tau,

@@ -182,8 +182,9 @@ int fs2d_solve_pressure(fs2d_sim* sim, const uint8_t* cell, const double* phi, c
 
 /* Differentiable rollout.  No reference counterpart: the reference has no
  * derivatives.  The forward pass is the semi-Lagrangian frame's velocity
- * stages (applySemiLagrangianAdvection, applyGravity, applyProjection in
- * FP64, updateVelocity; src/FluidSim2D.cpp:100-113) repeated `steps` times
+ * stages (applySemiLagrangianAdvection, applyGravity, applyProjection with
+ * the handle's precision and tolerance, updateVelocity;
+ * src/FluidSim2D.cpp:100-113) repeated `steps` times
  * from the face velocities (u0, v0), on the handle's fixed labels, which may
  * hold no EMPTY cell (a closed box: the projection is then a fixed linear
  * map).  The loss is the L2 distance sqrt(sum (u_T - uTarget)^2 +

@@ -8,6 +8,8 @@ fluid: semi-Lagrangian advection, projection and the velocity update, FP64.
   1, checkpoints every sqrt(T) = 8 steps: the hand-written adjoint against
   FP64 central differences of the GPU forward along 8 seeded random
   directions (eps = 1e-4 per face), within 1e-4 relative;
+* both with the FP64 projection and with the mixed one (FP32 MIC(0)-PCG in
+  FP64 refinement), each solved to 1e-12;
 * the gradient does not depend on the checkpoint spacing, and device
   pointers work like host ones;
 * scenes the rollout does not cover are refused.
@@ -32,11 +34,12 @@ def make(nx, **kw):
     return sc, fs2d.FluidSim2D(sc, seed=1, **opts)
 
 
-def test_adjoint_matches_cpu_reverse_mode():
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_adjoint_matches_cpu_reverse_mode(precision):
     torch = pytest.importorskip("torch")
     RA = pytest.importorskip("rollout_autograd")
     nx, steps = 32, 8
-    sc, sim = make(nx)
+    sc, sim = make(nx, precision=precision)
     u0, v0 = scenes.fourier_faces(nx, nx, seed=11)
     ut, vt = scenes.fourier_faces(nx, nx, seed=12)
     loss = sim.forward(steps, u0, v0, ut, vt, checkpoint_every=3)
@@ -49,9 +52,10 @@ def test_adjoint_matches_cpu_reverse_mode():
     assert np.abs(g - r).max() <= CPU_GRAD_REL * np.abs(r).max()
 
 
-def test_adjoint_finite_differences_128():
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_adjoint_finite_differences_128(precision):
     nx, steps = 128, 64
-    sc, sim = make(nx)
+    sc, sim = make(nx, precision=precision)
     u0, v0 = scenes.fourier_faces(nx, nx, seed=1)
     ut, vt = scenes.fourier_faces(nx, nx, seed=2)
     sim.forward(steps, u0, v0, ut, vt)
