@@ -22,6 +22,7 @@ replicas (the step does not shard); value = total cell-steps / max time.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -66,6 +67,8 @@ def parse():
     ap.add_argument("--adjoint-steps", type=int, default=64)
     ap.add_argument("--batch-scenes", type=int, default=256, help="batched dam breaks (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--batch-adjoint-scenes", type=int, default=32, help="batched closed-box rollouts (0: skip)")
+    ap.add_argument("--batch-adjoint-steps", type=int, default=16)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
@@ -482,6 +485,51 @@ def main():
                            "sequential = the same batch with one worker, one step"}
         bt.close()
 
+    # ---- batched rollouts: closed boxes of uneven sizes, forward and adjoint ----
+    batch_adjoint = None
+    if args.batch_adjoint_scenes > 0:
+        import scenes
+        T = args.batch_adjoint_steps
+        cscs = scenes.batch_closed_boxes(args.batch_adjoint_scenes, seed=SEED)
+        ccells = sum(sc["sizeX"] * sc["sizeY"] for sc in cscs)
+        ins = [scenes.fourier_faces(sc["sizeX"], sc["sizeY"], seed=1 + k) for k, sc in enumerate(cscs)]
+        tgs = [scenes.fourier_faces(sc["sizeX"], sc["sizeY"], seed=1000 + k) for k, sc in enumerate(cscs)]
+        dins = [[torch.tensor(a, device=f"cuda:{local}") for a in pair] for pair in ins]
+        dtgs = [[torch.tensor(a, device=f"cuda:{local}") for a in pair] for pair in tgs]
+        grads = [[torch.empty_like(p[0]), torch.empty_like(p[1])] for p in dins]
+        ba = fs2d.Batch(cscs, workers=8, seed=SEED, precision="mixed", pcg_tol=1e-12, pcg_max_iters=2000,
+                        device=local)
+        u0p = [p[0].data_ptr() for p in dins]
+        v0p = [p[1].data_ptr() for p in dins]
+        utp = [p[0].data_ptr() for p in dtgs]
+        vtp = [p[1].data_ptr() for p in dtgs]
+        gup = (ctypes.c_void_p * len(cscs))(*[g[0].data_ptr() for g in grads])
+        gvp = (ctypes.c_void_p * len(cscs))(*[g[1].data_ptr() for g in grads])
+
+        def bwd():
+            fs2d._check(fs2d.load().fs2d_batch_backward(ba.h, ctypes.cast(gup, ctypes.c_void_p),
+                                                        ctypes.cast(gvp, ctypes.c_void_p)))
+
+        ba.forward(T, u0p, v0p, utp, vtp)           # warm-up pair
+        bwd()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ba.forward(T, u0p, v0p, utp, vtp)
+        torch.cuda.synchronize()
+        f_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        bwd()
+        torch.cuda.synchronize()
+        b_s = time.perf_counter() - t0
+        sides = sorted(sc["sizeX"] for sc in cscs)
+        batch_adjoint = {"scenes": len(cscs), "cells": ccells, "side_min": sides[0], "side_max": sides[-1],
+                         "steps": T, "checkpoint_every": int(np.ceil(np.sqrt(T))), "workers": 8, "precision": "mixed",
+                         "pcg_tol": 1e-12, "forward_s": f_s, "backward_s": b_s, "backward_over_forward": b_s / f_s,
+                         "forward_cell_steps_per_s": ccells * T / f_s,
+                         "timing": "host wall clock around fs2d_batch_forward / fs2d_batch_backward (each returns after "
+                                   "its device work), inputs resident on the device, after one untimed pair"}
+        ba.close()
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -493,6 +541,7 @@ def main():
         "pressure_solve": pressure,
         "adjoint": adjoint,
         "batch": batch,
+        "batch_adjoint": batch_adjoint,
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,

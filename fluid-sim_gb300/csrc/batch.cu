@@ -10,7 +10,8 @@
 // polls, the extrapolation depth) block only the worker that issued it.
 //
 // Scenes go to workers longest-first onto the least-loaded worker (load =
-// cells), which balances uneven grid sizes.  With workers = 0 the first
+// cells), which balances uneven grid sizes.  The differentiable rollout
+// (fs2d_forward / fs2d_backward) of every scene runs the same way.  With workers = 0 the first
 // frames of fs2d_batch_step pick the worker count: candidate counts are
 // timed on one frame each and the fastest is kept.  Those frames are real
 // frames: a scene's results do not depend on the worker count, as every
@@ -80,10 +81,67 @@ int run(fs2d_batch* b, int w, int nframes) {
     return 0;
 }
 
+// Runs fn(k) for every scene with `w` workers (scenes longest-first onto the
+// least-loaded worker); returns the first error.
+template <typename F>
+int run_each(fs2d_batch* b, int w, F fn) {
+    auto parts = assign(b, w);
+    std::vector<int> rc(w, 0);
+    auto body = [&](int t) {
+        cudaSetDevice(b->device);
+        for (int k : parts[t]) {
+            int r = fn(k);
+            if (r) {
+                rc[t] = r;
+                return;
+            }
+        }
+    };
+    if (w == 1) {
+        body(0);
+    } else {
+        std::vector<std::thread> th;
+        th.reserve(w);
+        for (int t = 0; t < w; t++) th.emplace_back(body, t);
+        for (auto& x : th) x.join();
+    }
+    for (int r : rc)
+        if (r) return r;
+    return 0;
+}
+
+int workers_for(const fs2d_batch* b) {
+    if (b->workers > 0) return b->workers;
+    const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+    return std::max(1, std::min({(int)b->sims.size(), hw, 16}));
+}
+
 }  // namespace
 }  // namespace fs2d
 
 extern "C" {
+
+int fs2d_batch_forward(fs2d_batch* b, int steps, int checkpointEvery, const double* const* u0, const double* const* v0,
+                       const double* const* uTarget, const double* const* vTarget, double* losses) {
+    using namespace fs2d;
+    if (!b || !u0 || !v0 || !uTarget || !vTarget || !losses) {
+        set_error("fs2d_batch_forward: per-scene arrays and losses are required");
+        return FS2D_ERR_INVALID;
+    }
+    return run_each(b, workers_for(b), [&](int k) {
+        return fs2d_forward(b->sims[k], steps, checkpointEvery, u0[k], v0[k], uTarget[k], vTarget[k], &losses[k]);
+    });
+}
+
+int fs2d_batch_backward(fs2d_batch* b, double* const* gradU0, double* const* gradV0) {
+    using namespace fs2d;
+    if (!b || !gradU0 || !gradV0) {
+        set_error("fs2d_batch_backward: per-scene gradient arrays are required");
+        return FS2D_ERR_INVALID;
+    }
+    return run_each(b, workers_for(b), [&](int k) { return fs2d_backward(b->sims[k], gradU0[k], gradV0[k]); });
+}
+
 
 int fs2d_batch_create(const fs2d_config* cfgs, int n, const fs2d_options* opt, int workers, fs2d_batch** out) {
     using namespace fs2d;

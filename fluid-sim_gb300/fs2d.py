@@ -97,6 +97,9 @@ SIGNATURES = {
     "fs2d_batch_scene": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
     "fs2d_batch_workers": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "fs2d_batch_set_workers": (C.c_int, [C.c_void_p, C.c_int]),
+    "fs2d_batch_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_void_p]),
+    "fs2d_batch_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fs2d_batch_destroy": (C.c_int, [C.c_void_p]),
     "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
     "fs2d_save_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
@@ -442,6 +445,38 @@ class Batch:
     @workers.setter
     def workers(self, w):
         _check(load().fs2d_batch_set_workers(self.h, int(w)))
+
+    def _ptrs(self, arrays, sizes, keep):
+        out = (C.c_void_p * len(self.scenes))()
+        for k, a in enumerate(arrays):
+            if isinstance(a, int):
+                out[k] = a
+            else:
+                a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+                assert a.size == sizes[k]
+                keep.append(a)
+                out[k] = a.ctypes.data
+        return out
+
+    def forward(self, steps, u0s, v0s, u_targets, v_targets, checkpoint_every=0):
+        """fs2d_batch_forward: every scene's rollout; returns the losses."""
+        nu = [(sc["sizeX"] + 1) * sc["sizeY"] for sc in self.scenes]
+        nv = [sc["sizeX"] * (sc["sizeY"] + 1) for sc in self.scenes]
+        keep = []
+        args = [self._ptrs(a, n, keep) for a, n in ((u0s, nu), (v0s, nv), (u_targets, nu), (v_targets, nv))]
+        losses = np.zeros(len(self.scenes))
+        _check(load().fs2d_batch_forward(self.h, int(steps), int(checkpoint_every), *(C.cast(a, C.c_void_p) for a in args),
+                                         losses.ctypes.data))
+        return losses
+
+    def backward(self):
+        """fs2d_batch_backward into host arrays: [(dL/du0, dL/dv0) per scene]."""
+        gus = [np.empty((sc["sizeX"] + 1) * sc["sizeY"]) for sc in self.scenes]
+        gvs = [np.empty(sc["sizeX"] * (sc["sizeY"] + 1)) for sc in self.scenes]
+        pu = (C.c_void_p * len(gus))(*[g.ctypes.data for g in gus])
+        pv = (C.c_void_p * len(gvs))(*[g.ctypes.data for g in gvs])
+        _check(load().fs2d_batch_backward(self.h, C.cast(pu, C.c_void_p), C.cast(pv, C.c_void_p)))
+        return list(zip(gus, gvs))
 
     def close(self):
         if getattr(self, "h", None):

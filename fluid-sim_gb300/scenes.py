@@ -147,3 +147,10 @@ def batch_dam_breaks(count, seed=0, lo=64, hi=512):
         ex, ey = rng.uniform(0.2, 0.6, 2)
         out.append(dam_break(n, mode=PICFLIP, dt=(1.0 / 240) * (256.0 / n), extent=(ex, ey), pic_flip_alpha=0.05))
     return out
+
+
+def batch_closed_boxes(count, seed=0, lo=64, hi=512, dt=1.0 / 60):
+    """Closed boxes of fluid with sides drawn log-uniformly from [lo, hi]
+    (the differentiable rollout's scenes, in a batch)."""
+    rng = np.random.default_rng(seed)
+    return [closed_box(int(round(np.exp(rng.uniform(np.log(lo), np.log(hi))))), dt=dt) for _ in range(count)]

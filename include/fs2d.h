@@ -224,6 +224,15 @@ int fs2d_batch_scene(fs2d_batch* batch, int k, fs2d_sim** sim);
 int fs2d_batch_workers(fs2d_batch* batch, int* workers);   /* 0 until chosen */
 int fs2d_batch_set_workers(fs2d_batch* batch, int workers); /* 0: choose again on the next frames */
 int fs2d_batch_destroy(fs2d_batch* batch);
+/* fs2d_forward / fs2d_backward for every scene of a batch (each a closed box:
+ * no EMPTY cell, semi-Lagrangian mode), scenes issued concurrently by the
+ * batch's workers (all hardware threads up to 16 while the count is not
+ * chosen).  Arrays of per-scene pointers (host or device memory, scene k's
+ * face grids); losses[k] receives scene k's loss.  Returns the first error. */
+int fs2d_batch_forward(fs2d_batch* batch, int steps, int checkpointEvery, const double* const* u0,
+                       const double* const* v0, const double* const* uTarget, const double* const* vTarget,
+                       double* losses);
+int fs2d_batch_backward(fs2d_batch* batch, double* const* gradU0, double* const* gradV0);
 
 /* Runs `nframes` frames back to back without host synchronisation between them
  * (except the pressure solver's convergence polls). */

@@ -61,3 +61,23 @@ def test_batch_rejects_bad_arguments():
     with pytest.raises(fs2d.FS2DError):
         b.scene(2)
     b.close()
+
+
+def test_batch_rollout_matches_scenes_alone():
+    scs = scenes.batch_closed_boxes(4, seed=3, lo=24, hi=48)
+    fields = [scenes.fourier_faces(sc["sizeX"], sc["sizeY"], seed=10 + k) for k, sc in enumerate(scs)]
+    targets = [scenes.fourier_faces(sc["sizeX"], sc["sizeY"], seed=20 + k) for k, sc in enumerate(scs)]
+    opts = dict(precision="mixed", pcg_tol=1e-12, pcg_max_iters=2000)
+    b = fs2d.Batch(scs, workers=3, seed=1, **opts)
+    losses = b.forward(6, [f[0] for f in fields], [f[1] for f in fields], [t[0] for t in targets],
+                       [t[1] for t in targets], checkpoint_every=2)
+    grads = b.backward()
+    b.close()
+    for k, sc in enumerate(scs):
+        sim = fs2d.FluidSim2D(sc, seed=1 + k, **opts)
+        L = sim.forward(6, fields[k][0], fields[k][1], targets[k][0], targets[k][1], checkpoint_every=2)
+        gu, gv = sim.backward()
+        sim.close()
+        assert L == losses[k]
+        g, r = np.concatenate(grads[k]), np.concatenate([gu, gv])
+        assert np.abs(g - r).max() <= 1e-12 * np.abs(r).max()
