@@ -47,7 +47,7 @@ FLUSH_BYTES = 256 << 20          # > 129 MB L2
 #   eik_sweep: read phi (8 B) and the changeability byte, write phi: 17 B
 #   cp_sweep: read the closest-particle index (4 B) and its 16-byte
 #            position pair, write the index: 24 B
-KERNEL_BYTES_PER_CELL = {"mic32_forward": 16, "mic32_backward": 16, "wave2_MicForward64": 40,
+KERNEL_BYTES_PER_CELL = {"mic32": 16, "mic32_forward": 16, "mic32_backward": 16, "wave2_MicForward64": 40,
                          "wave2_MicBackward64": 40, "eik_sweep": 17, "cp_sweep": 24}
 DOMINANT = tuple(KERNEL_BYTES_PER_CELL)
 
@@ -68,6 +68,7 @@ def parse():
     ap.add_argument("--batch-scenes", type=int, default=256, help="batched dam breaks (0: skip)")
     ap.add_argument("--batch-steps", type=int, default=5)
     ap.add_argument("--batch-adjoint-scenes", type=int, default=32, help="batched closed-box rollouts (0: skip)")
+    ap.add_argument("--sl-steps", type=int, default=10, help="steps of the semi-Lagrangian 1024^2 variant (0: skip)")
     ap.add_argument("--batch-adjoint-steps", type=int, default=16)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--e2e-steps", type=int, default=5)
@@ -257,7 +258,7 @@ def main():
     clocks.start()
     time.sleep(0.3)
     l0 = sim.launch_count()
-    iters = []
+    iters, outers = [], []
     barrier()
     torch.cuda.synchronize()
     evs = []
@@ -269,7 +270,9 @@ def main():
         sim.runFrame()
         e1.record(stream)
         evs.append((e0, e1))
-        iters.append(sim.stats()["pcgIterations"])
+        st_ = sim.stats()
+        iters.append(st_["pcgIterations"])
+        outers.append(st_["irOuterIterations"])
     torch.cuda.synchronize()
     barrier()
     total_ms = sum(a.elapsed_time(b) for a, b in evs)
@@ -301,7 +304,13 @@ def main():
     value = cells * args.steps * world / (total_ms / 1000.0)
 
     # ---- roofline of the dominant kernel ----
-    dom = max((k for k in ktimes if k in DOMINANT), key=lambda k: ktimes[k][1], default=None)
+    # the FP32 MIC(0) forward and backward sweeps are one kernel template with
+    # the same bytes per cell: reported together as "mic32"
+    if "mic32_forward" in ktimes and "mic32_backward" in ktimes:
+        nf, mf = ktimes.pop("mic32_forward")
+        nb_, mb = ktimes.pop("mic32_backward")
+        ktimes["mic32"] = (nf + nb_, mf + mb)
+    dom = max((k for k in ktimes if k in KERNEL_BYTES_PER_CELL), key=lambda k: ktimes[k][1], default=None)
     roofline = None
     if dom is not None:
         n_launch, ms = ktimes[dom]
@@ -327,6 +336,26 @@ def main():
                     "share_of_step": round(ktimes[dom][1] / kt_total, 3),
                     "kernel_ms_per_step": {k: round(v[1] / kt_steps, 3) for k, v in sorted(ktimes.items())},
                     "timed_over": f"{kt_steps} extra steps with per-launch events"}
+
+    # ---- whole-step roofline: compulsory bytes of every stage per step ----
+    # per cell: PCG 24 b per inner iteration (b = 4 for the mixed inner solve,
+    # 8 for FP64), 48 B per FP64 refinement residual, matrix + rhs build 73 B,
+    # MIC(0) factor 4 b, velocity update 49 B, level set (16 closest-point
+    # sweeps x 24 B, 16 Eikonal sweeps x 16 B, seeding 12 B, smoothing 32 B),
+    # grid side of P2G / G2P / particle advection (32 + 32 + 16 B); per
+    # particle: P2G 28 B, G2P 24 B, advection 16 B, level-set seeding 8 B.
+    # Extrapolation faces are not counted (data dependent, a few % of cells).
+    b = 4 if args.precision == "mixed" else 8
+    it_mean = float(np.mean(iters))
+    out_mean = float(np.mean(outers)) if args.precision == "mixed" else 0.0
+    per_cell = 24 * b * it_mean + 48 * out_mean + 73 + 4 * b + 49 + (16 * 24 + 16 * 16 + 12 + 32) + (32 + 32 + 16)
+    step_bytes = per_cell * cells + (28 + 24 + 16 + 8) * n_particles
+    step_achieved = step_bytes / (total_ms / args.steps / 1000.0) / 1e9
+    step_roofline = {"bound": "hbm", "algorithmic_bytes_per_step": int(step_bytes),
+                     "achieved": round(step_achieved, 1), "peak": roofline["peak"] if roofline else 6800.0,
+                     "unit": "GB/s", "frac": round(step_achieved / (roofline["peak"] if roofline else 6800.0), 4),
+                     "pcg_iterations_per_step": it_mean, "refinement_sweeps_per_step": out_mean,
+                     "formula": "sum of the stages' compulsory bytes per step / measured step time"}
 
     # ---- e2e: through the C ABI with host buffers (upload + frame + download) ----
     e2e = None
@@ -371,6 +400,32 @@ def main():
                      "stage_ms_last_step": [round(x, 3) for x in sim64.stage_times()],
                      "pcg_iterations_last_step": sim64.stats()["pcgIterations"]}
         sim64.close()
+
+    # ---- semi-Lagrangian variant of the plain dam break at the same size ----
+    sl_path = None
+    if args.sl_steps > 0:
+        import scenes
+        ssc = scenes.sl_dam_break(args.size, dt=(1.0 / 120) * (64.0 / args.size))
+        ssim = fs2d.FluidSim2D(ssc, seed=SEED, **opts)
+        ssim.set_stream(stream.cuda_stream)
+        for _ in range(3):
+            ssim.runFrame()
+        torch.cuda.synchronize()
+        sms = 0.0
+        for _ in range(args.sl_steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            ssim.runFrame()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            sms += e0.elapsed_time(e1)
+        sl_path = {"scene": f"semi-Lagrangian dam break x<0.4, y<0.6, {args.size}^2, dt 1/120 scaled by 64/{args.size}",
+                   "value": cells * args.sl_steps / (sms / 1000.0), "unit": UNIT,
+                   "ms_per_step": sms / args.sl_steps, "steps": args.sl_steps, "precision": args.precision,
+                   "stage_ms_last_step": [round(x, 3) for x in ssim.stage_times()]}
+        ssim.close()
 
     # ---- standalone pressure solve: random disks, N(0,1) velocities, 1e-10 ----
     pressure = None
@@ -453,8 +508,12 @@ def main():
     batch = None
     if args.batch_scenes > 0:
         import scenes
-        bscs = scenes.batch_dam_breaks(args.batch_scenes, seed=SEED)
-        bcells = sum(sc["sizeX"] * sc["sizeY"] for sc in bscs)
+        import shard
+        all_b = scenes.batch_dam_breaks(args.batch_scenes, seed=SEED)
+        bcells = sum(sc["sizeX"] * sc["sizeY"] for sc in all_b)
+        # several GPUs: the scenes are split over the ranks (no exchange during the steps)
+        bparts = shard.partition([sc["sizeX"] * sc["sizeY"] for sc in all_b], world)
+        bscs = [all_b[k] for k in bparts[rank]]
         bt = fs2d.Batch(bscs, workers=0, seed=SEED, precision="mixed", pcg_tol=args.tol, pcg_max_iters=200,
                         device=local)
         t0 = time.perf_counter()
@@ -466,6 +525,10 @@ def main():
         bt.step(args.batch_steps)
         torch.cuda.synchronize()
         conc_s = time.perf_counter() - t0
+        if world > 1:
+            t = torch.tensor([conc_s], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            conc_s = float(t.item())
         l1 = sum(bt.scene(k).launch_count() for k in range(len(bscs)))
         workers = bt.workers
         bt.workers = 1
@@ -473,16 +536,17 @@ def main():
         bt.step(1)
         torch.cuda.synchronize()
         seq_s = time.perf_counter() - t0
-        sides = sorted(sc["sizeX"] for sc in bscs)
-        batch = {"scenes": len(bscs), "cells": bcells, "side_min": sides[0], "side_median": sides[len(sides) // 2],
+        sides = sorted(sc["sizeX"] for sc in all_b)
+        batch = {"scenes": len(all_b), "scenes_per_rank": [len(p) for p in bparts], "cells": bcells, "side_min": sides[0], "side_median": sides[len(sides) // 2],
                  "side_max": sides[-1], "steps": args.batch_steps, "workers": workers,
                  "value": bcells * args.batch_steps / conc_s, "unit": UNIT,
                  "ms_per_batch_step": 1000.0 * conc_s / args.batch_steps,
-                 "sequential_value": bcells / seq_s, "concurrency_speedup": seq_s / (conc_s / args.batch_steps),
+                 "sequential_value_rank0": sum(sc["sizeX"] * sc["sizeY"] for sc in bscs) / seq_s,
+                 "concurrency_speedup_rank0": seq_s / (conc_s / args.batch_steps),
                  "gpu_launches_per_batch_step": (l1 - l0) // max(args.batch_steps, 1),
                  "warmup_s": warm_s,
-                 "timing": "host wall clock around fs2d_batch_step (each frame returns after its device work); "
-                           "sequential = the same batch with one worker, one step"}
+                 "timing": "host wall clock around fs2d_batch_step (each frame returns after its device work), "
+                           "max over ranks; sequential = rank 0's scenes with one worker, one step"}
         bt.close()
 
     # ---- batched rollouts: closed boxes of uneven sizes, forward and adjoint ----
@@ -490,10 +554,13 @@ def main():
     if args.batch_adjoint_scenes > 0:
         import scenes
         T = args.batch_adjoint_steps
-        cscs = scenes.batch_closed_boxes(args.batch_adjoint_scenes, seed=SEED)
-        ccells = sum(sc["sizeX"] * sc["sizeY"] for sc in cscs)
-        ins = [scenes.fourier_faces(sc["sizeX"], sc["sizeY"], seed=1 + k) for k, sc in enumerate(cscs)]
-        tgs = [scenes.fourier_faces(sc["sizeX"], sc["sizeY"], seed=1000 + k) for k, sc in enumerate(cscs)]
+        import shard
+        all_c = scenes.batch_closed_boxes(args.batch_adjoint_scenes, seed=SEED)
+        ccells = sum(sc["sizeX"] * sc["sizeY"] for sc in all_c)
+        cparts = shard.partition([sc["sizeX"] * sc["sizeY"] for sc in all_c], world)
+        cscs = [all_c[k] for k in cparts[rank]]
+        ins = [scenes.fourier_faces(sc["sizeX"], sc["sizeY"], seed=1 + k) for k, sc in zip(cparts[rank], cscs)]
+        tgs = [scenes.fourier_faces(sc["sizeX"], sc["sizeY"], seed=1000 + k) for k, sc in zip(cparts[rank], cscs)]
         dins = [[torch.tensor(a, device=f"cuda:{local}") for a in pair] for pair in ins]
         dtgs = [[torch.tensor(a, device=f"cuda:{local}") for a in pair] for pair in tgs]
         grads = [[torch.empty_like(p[0]), torch.empty_like(p[1])] for p in dins]
@@ -514,20 +581,28 @@ def main():
         bwd()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        ba.forward(T, u0p, v0p, utp, vtp)
+        my_losses = ba.forward(T, u0p, v0p, utp, vtp)
         torch.cuda.synchronize()
         f_s = time.perf_counter() - t0
         t0 = time.perf_counter()
         bwd()
         torch.cuda.synchronize()
         b_s = time.perf_counter() - t0
-        sides = sorted(sc["sizeX"] for sc in cscs)
-        batch_adjoint = {"scenes": len(cscs), "cells": ccells, "side_min": sides[0], "side_max": sides[-1],
+        if world > 1:
+            t = torch.tensor([f_s, b_s], device="cuda", dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            f_s, b_s = (float(x) for x in t.tolist())
+        # host gather of the per-scene losses (the batch's only exchange)
+        losses_all = shard.gather(dict(zip(cparts[rank], my_losses.tolist())), cparts, rank, world)
+        sides = sorted(sc["sizeX"] for sc in all_c)
+        batch_adjoint = {"scenes": len(all_c), "scenes_per_rank": [len(p) for p in cparts], "cells": ccells,
+                         "loss_sum": float(sum(losses_all)), "side_min": sides[0], "side_max": sides[-1],
                          "steps": T, "checkpoint_every": int(np.ceil(np.sqrt(T))), "workers": 8, "precision": "mixed",
                          "pcg_tol": 1e-12, "forward_s": f_s, "backward_s": b_s, "backward_over_forward": b_s / f_s,
                          "forward_cell_steps_per_s": ccells * T / f_s,
                          "timing": "host wall clock around fs2d_batch_forward / fs2d_batch_backward (each returns after "
-                                   "its device work), inputs resident on the device, after one untimed pair"}
+                                   "its device work), max over ranks, inputs resident on the device, after one untimed "
+                                   "pair"}
         ba.close()
 
     line = {
@@ -538,6 +613,7 @@ def main():
         "config": config_dict(args, n_particles, {"pcg_iterations_per_step": iters}),
         "stage_ms_last_step": stage_ms,
         "fp64_path": fp64_path,
+        "sl_path": sl_path,
         "pressure_solve": pressure,
         "adjoint": adjoint,
         "batch": batch,
@@ -545,6 +621,7 @@ def main():
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,
+        "step_roofline": step_roofline,
         "e2e": e2e,
     }
     if rank == 0 and not args.no_cpu_baseline:
