@@ -311,6 +311,8 @@ int alloc_all(Sim* s) {
         A(m32.s1, N);
         A(m32.e, N);
         A(pcg32, 1);
+        A(m32_gbase, 1);
+        A(m32_gprogress, (size_t)s->progress_cap);
         (void)m;
         s->m32maps = new (std::nothrow) Mic32MapsHost();
         if (!s->m32maps) {
@@ -333,13 +335,15 @@ int alloc_all(Sim* s) {
 
 void free_all(Sim* s) {
     rollout_free(s);
+    if (s->m32_graph) cudaGraphExecDestroy(s->m32_graph);
     void* ptrs[] = {s->cell, s->phi, s->p, s->u, s->v, s->nu, s->nv, s->pos, s->vel, s->t, s->seed_key,
                     s->phi_tmp, s->surface, s->u0, s->v0, s->udiv, s->vdiv, s->mask_u, s->mask_v, s->cnt_u,
                     s->cnt_v, s->fill_u, s->fill_v, s->ent_u, s->ent_v, s->scan_tmp, s->tile_range, s->max_layer,
                     s->Adiag, s->Ax, s->Ay, s->rhs, s->precon, s->cfx, s->cfy, s->cbx, s->cby, s->r, s->z, s->q, s->w, s->s0,
                     s->s1, s->partial, s->pcg, s->progress, s->stats, s->err, s->m32.a0, s->m32.ax, s->m32.ay,
                     s->m32.pc, s->m32.fa, s->m32.fb, s->m32.fc, s->m32.fd, s->m32.r, s->m32.rp, s->m32.q,
-                    s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32, s->pos_df,
+                    s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32, s->m32_gbase, s->m32_gprogress,
+                    s->pos_df,
                     s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p, s->phi_p, s->emask};
     for (void* p : ptrs)
         if (p) cudaFree(p);

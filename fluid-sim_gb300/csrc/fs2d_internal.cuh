@@ -144,6 +144,13 @@ struct Sim {
     int m32_cluster = 0;                             // cluster size of the FP32 MIC(0) sweeps (0: not chosen)
     PcgScalars* pcg32 = nullptr;                     // inner FP32 solve scalars
     PcgScalars* pcg32_host = nullptr;
+    // the inner PCG loop replayed as a CUDA graph of kM32GraphIters iterations
+    unsigned long long* m32_gbase = nullptr;         // device progress base of graph-replayed sweeps
+    unsigned long long* m32_gprogress = nullptr;     // their progress counters (progress_cap)
+    cudaGraphExec_t m32_graph = nullptr;
+    const void* m32_graph_key = nullptr;             // s->partial when the graph was captured
+    unsigned long long m32_graph_launches = 0;       // kernels per replay
+    int m32_graph_state = 0;                         // 0 not tried, 1 ready, -1 unavailable (direct launches)
 
     // wavefront progress flags (monotonic, 64-bit, never reset)
     unsigned long long* progress = nullptr;

@@ -78,10 +78,14 @@ __device__ __forceinline__ float m32_entry_value(unsigned long long e) { return 
 // Block of 64 threads: warp 0 computes, warp 1 moves the strip boundaries
 // (so no remote write, release or L2 round trip stalls the compute warp).
 template <bool FWD>
+// base_dev: when non-null, the launch's progress base is read from device
+// memory (launches replayed from a CUDA graph, each preceded by a bump of
+// that counter) instead of the by-value `base_host`.
 __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32Maps maps, float* out, int P, int NY,
-                                                   unsigned long long* progress, unsigned long long base, int* err,
-                                                   const int* skip) {
+                                                   unsigned long long* progress, unsigned long long base_host,
+                                                   const unsigned long long* base_dev, int* err, const int* skip) {
     if (skip != nullptr && *skip) return;
+    const unsigned long long base = base_dev != nullptr ? *base_dev : base_host;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* ring = reinterpret_cast<float*>(smem_raw);
     // row below the strip, kM32BndRing columns of tagged entries
@@ -395,8 +399,17 @@ int mic32_make_map(CUtensorMap* map, float* base, int P, int NY, int box_rows);
 // Launches one sweep: cooperative (every strip co-resident, so the waits
 // between strips always make progress) and, where the device can hold them,
 // in clusters of up to 8 strips that hand rows over in shared memory.
+// Advances the device-side progress base of graph-replayed sweeps.
+__global__ void k_wave_bump(unsigned long long* base) { *base += 1ull << 24; }
+
+// Launches one sweep: cooperative (every strip co-resident, so the waits
+// between strips always make progress) and, where the device can hold them,
+// in clusters of up to 8 strips that hand rows over in shared memory.
+// graph = true: for stream capture; the sweep uses its own progress counters
+// and a base in device memory, bumped by a preceding kernel, so that every
+// replay of the captured launch gets a fresh base.
 template <bool FWD>
-int launch_mic32(Sim* s, const Mic32Maps& maps, float* out, const int* skip) {
+int launch_mic32(Sim* s, const Mic32Maps& maps, float* out, const int* skip, bool graph = false) {
     const int nstrips = (s->NY + kM32Rows - 1) / kM32Rows;
     if (nstrips > s->progress_cap) {
         set_error("mic32: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
@@ -404,17 +417,26 @@ int launch_mic32(Sim* s, const Mic32Maps& maps, float* out, const int* skip) {
     }
     static std::atomic<unsigned long long> configured{0};
     if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)mic32_kernel<FWD>, (int)kM32Smem)) return rc0;
-    unsigned long long base = wave_begin(s);
+    unsigned long long base = 0;
+    const unsigned long long* base_dev = nullptr;
+    unsigned long long* progress = s->progress;
+    if (graph) {
+        FS2D_LAUNCH(s, k_wave_bump, 1, 1, 0, s->m32_gbase);
+        base_dev = s->m32_gbase;
+        progress = s->m32_gprogress;
+    } else {
+        base = wave_begin(s);
+    }
     int P = s->P, NY = s->NY;
-    void* args[] = {(void*)&maps, (void*)&out, (void*)&P, (void*)&NY, (void*)&s->progress, (void*)&base,
-                    (void*)&s->err, (void*)&skip};
+    void* args[] = {(void*)&maps, (void*)&out, (void*)&P, (void*)&NY, (void*)&progress, (void*)&base,
+                    (void*)&base_dev, (void*)&s->err, (void*)&skip};
     s->launches++;
     const char* name = FWD ? "mic32_forward" : "mic32_backward";
     long long kt = ktimer_begin(s, name);
     int& cs = s->m32_cluster;   // 0: not chosen yet
     if (cs == 0) cs = choose_cluster((const void*)mic32_kernel<FWD>, nstrips, 64, kM32Smem);
     cudaError_t e = launch_clustered((const void*)mic32_kernel<FWD>, nstrips, cs, 64, kM32Smem, s->stream, args);
-    if (e != cudaSuccess && cs > 1) {   // clusters refused: plain cooperative launch
+    if (e != cudaSuccess && cs > 1 && !graph) {   // clusters refused: plain cooperative launch
         (void)cudaGetLastError();
         cs = 1;
         e = launch_clustered((const void*)mic32_kernel<FWD>, nstrips, 1, 64, kM32Smem, s->stream, args);

@@ -146,7 +146,7 @@ __global__ void k_resid64(const uint8_t* __restrict__ cell, const double* __rest
 // Start of an inner solve: r32 = r64 / ||r64||inf, r*pc^2, e = 0, scalars reset.
 __global__ void k_inner_init(const double* __restrict__ r64, const PcgScalars* __restrict__ outer,
                              const float* __restrict__ pc, float* r32, float* rp32, float* e32, int NX, int P,
-                             size_t N, PcgScalars* inner) {
+                             size_t N, PcgScalars* inner, double inner_tol) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     const double rn = outer->r_norm;
     const double scale = rn > 0 ? 1.0 / rn : 0.0;
@@ -165,6 +165,7 @@ __global__ void k_inner_init(const double* __restrict__ r64, const PcgScalars* _
         inner->sigma = inner->alpha = inner->beta = 0;
         inner->rhs_norm = 1.0;
         inner->r_norm = 1.0;
+        inner->tol_abs = inner_tol;   // read by k_axpy32 (device memory, so a captured loop can replay it)
     }
 }
 
@@ -289,10 +290,11 @@ __global__ void __launch_bounds__(kRT) k_spmv32(const uint8_t* __restrict__ cell
     }
 }
 
-// e += alpha s, r -= alpha w, rp = r pc^2, ||r||inf (stop when below inner_tol).
+// e += alpha s, r -= alpha w, rp = r pc^2, ||r||inf (stop when below the
+// inner tolerance, pcg->tol_abs).
 __global__ void __launch_bounds__(kRT) k_axpy32(float* e, float* r, float* rp, const float* __restrict__ pc,
                                                 const float* __restrict__ s, const float* __restrict__ w, int NX,
-                                                int NY, int P, float* partial, PcgScalars* pcg, double inner_tol) {
+                                                int NY, int P, float* partial, PcgScalars* pcg) {
     __shared__ float sh[32];
     if (pcg->done) return;
     const float alpha = (float)pcg->alpha;
@@ -318,7 +320,7 @@ __global__ void __launch_bounds__(kRT) k_axpy32(float* e, float* r, float* rp, c
         mm = block_max_f(mm, sh);
         if (threadIdx.x == 0) {
             pcg->r_norm = mm;
-            if (mm <= inner_tol) pcg->done = 1;
+            if (mm <= pcg->tol_abs) pcg->done = 1;
         }
     }
 }
@@ -357,6 +359,8 @@ int mixed_setup_maps(Sim* s) {
     memcpy(s->m32maps->bwd, &b, sizeof(b));
     return 0;
 }
+
+constexpr int kM32GraphIters = 4;   // inner iterations per graph replay (even: the search-direction ping-pong)
 
 int projection_mixed(Sim* s, int* status) { return projection_mixed_rhs(s, nullptr, status); }
 
@@ -406,30 +410,88 @@ int projection_mixed_rhs(Sim* s, const double* b, int* status) {
             // by tol_abs / ||r||inf (with a factor 2 of margin for the FP32
             // recurrence), but never asks for more than ir_inner_tol
             const double inner_tol = std::max(s->opt.ir_inner_tol, 0.5 * tol_abs / r_norm);
-            FS2D_LAUNCH(s, k_inner_init, nb, kT, 0, s->r, outer, m.pc, m.r, m.rp, m.e, NX, P, N, inner);
+            FS2D_LAUNCH(s, k_inner_init, nb, kT, 0, s->r, outer, m.pc, m.r, m.rp, m.e, NX, P, N, inner, inner_tol);
             rc = launch_mic32<true>(s, fmaps, m.q, done);
             if (rc) return rc;
             rc = launch_mic32<false>(s, bmaps, m.z, done);
             if (rc) return rc;
             FS2D_LAUNCH(s, k_dot32, rg, kRT, 0, m.z, m.r, NX, NY, P, part2, inner, 1, max_iters);
-            float* sbuf[2] = {m.s0, m.s1};
-            for (int it = 0; it < max_iters; it++) {
+            // one inner iteration; graph = true inside a stream capture
+            auto iteration = [&](int it, bool graph) -> int {
+                float* sbuf[2] = {m.s0, m.s1};
                 float* s_old = sbuf[it & 1];
                 float* s_new = sbuf[(it + 1) & 1];
                 FS2D_LAUNCH(s, k_spmv32, rg, kRT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, NY, P,
                             part2, inner);
-                FS2D_LAUNCH(s, k_axpy32, rg, kRT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, NX, NY, P, partf, inner,
-                            inner_tol);
-                rc = launch_mic32<true>(s, fmaps, m.q, done);
-                if (rc) return rc;
-                rc = launch_mic32<false>(s, bmaps, m.z, done);
-                if (rc) return rc;
+                FS2D_LAUNCH(s, k_axpy32, rg, kRT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, NX, NY, P, partf, inner);
+                int rc1 = launch_mic32<true>(s, fmaps, m.q, done, graph);
+                if (rc1) return rc1;
+                rc1 = launch_mic32<false>(s, bmaps, m.z, done, graph);
+                if (rc1) return rc1;
                 FS2D_LAUNCH(s, k_dot32, rg, kRT, 0, m.z, m.r, NX, NY, P, part2, inner, 0, max_iters);
+                return 0;
+            };
+            auto poll_done = [&]() -> int {
+                FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
+                                          s->stream));
+                FS2D_CUDA(cudaStreamSynchronize(s->stream));
+                return s->pcg32_host->done;
+            };
+            // Captures kM32GraphIters iterations as a CUDA graph (once per handle,
+            // again whenever the reduction scratch moved); false: launch directly
+            // (per-kernel timing is on, or capture is not available here).
+            auto ensure_graph = [&]() -> bool {
+                if (!s->kt_patterns.empty() || s->m32_graph_state < 0) return false;
+                if (s->m32_graph_state == 1 && s->m32_graph_key == (const void*)s->partial) return true;
+                if (s->m32_graph) {
+                    cudaGraphExecDestroy(s->m32_graph);
+                    s->m32_graph = nullptr;
+                }
+                s->m32_graph_state = -1;   // until the capture below succeeds
+                const unsigned long long l0 = s->launches;
+                if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    return false;
+                }
+                int rc1 = 0;
+                for (int k = 0; k < kM32GraphIters && !rc1; k++) rc1 = iteration(k, true);
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+                s->m32_graph_launches = s->launches - l0;
+                s->launches = l0;   // captured, not run
+                if (rc1 || e != cudaSuccess || g == nullptr) {
+                    if (g) cudaGraphDestroy(g);
+                    (void)cudaGetLastError();
+                    return false;
+                }
+                e = cudaGraphInstantiate(&s->m32_graph, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    s->m32_graph = nullptr;
+                    return false;
+                }
+                s->m32_graph_key = s->partial;
+                s->m32_graph_state = 1;
+                return true;
+            };
+            int it = 0;
+            if (ensure_graph()) {
+                // whole batches of iterations from the captured graph (kernels
+                // after convergence return at once on the done flag)
+                for (; it + kM32GraphIters <= max_iters; it += kM32GraphIters) {
+                    FS2D_CUDA(cudaGraphLaunch(s->m32_graph, s->stream));
+                    s->launches += s->m32_graph_launches;
+                    if (poll_done()) {
+                        it = max_iters;
+                        break;
+                    }
+                }
+            }
+            for (; it < max_iters; it++) {
+                if ((rc = iteration(it, false))) return rc;
                 if ((it + 1) % batch == 0 || it + 1 == max_iters) {
-                    FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
-                                              s->stream));
-                    FS2D_CUDA(cudaStreamSynchronize(s->stream));
-                    if (s->pcg32_host->done) break;
+                    if (poll_done()) break;
                 }
             }
             FS2D_LAUNCH(s, k_update64, nb, kT, 0, s->p, m.e, outer, NX, P, N);
