@@ -412,6 +412,21 @@ int check_scene(Sim* s) {
 
 }  // namespace
 
+// E^T of one face grid, in place: the layers as the last extrapolation left
+// them in `layer`, deepest first, layers above `lim` (a band limit) left out.
+int extrap_adjoint(Sim* s, double* mu, const uint32_t* layer, int W, int H, uint32_t lim) {
+    const size_t n = (size_t)W * H;
+    unsigned int* d = s->max_layer + 10;
+    FS2D_CUDA(cudaMemsetAsync(d, 0, sizeof(unsigned int), s->stream));
+    FS2D_LAUNCH(s, k_max_layer, blocks_for(n, kAT), kAT, 0, layer, n, d);
+    unsigned int h = 0;
+    FS2D_CUDA(cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    for (uint32_t L = h < lim ? h : lim; L >= 1; L--)
+        FS2D_LAUNCH(s, k_extrap_adjoint, dim3(blocks_for(W, 128), H), 128, 0, mu, layer, W, H, L);
+    return 0;
+}
+
 void rollout_free(Sim* s) {
     Rollout* ro = s->ro;
     if (!ro) return;

@@ -420,6 +420,24 @@ int finish(Host* h) {
     return 0;
 }
 
+// Device scratch of the transfer transposes, freed when the call returns.
+struct DevScratch {
+    std::vector<void*> ptrs;
+    ~DevScratch() {
+        for (void* p : ptrs) cudaFree(p);
+    }
+    template <typename T>
+    T* get(size_t n) {
+        void* p = nullptr;
+        if (cudaMalloc(&p, (n ? n : 1) * sizeof(T)) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return nullptr;
+        }
+        ptrs.push_back(p);
+        return static_cast<T*>(p);
+    }
+};
+
 Host* H(fs2d_sim* p) { return reinterpret_cast<Host*>(p); }
 
 }  // namespace
@@ -626,6 +644,62 @@ int fs2d_forward(fs2d_sim* p, int steps, int checkpointEvery, const double* u0, 
     int rc = rollout_forward(&h->sim, steps, checkpointEvery, u0, v0, uTarget, vTarget, loss);
     int rc2 = finish(h);
     return rc ? rc : rc2;
+}
+
+
+int fs2d_p2g_adjoint(fs2d_sim* p, const double* uBar, const double* vBar, double* particleVelsBar) {
+    if (!p || !uBar || !vBar || !particleVelsBar) {
+        set_error("fs2d_p2g_adjoint: uBar, vBar and particleVelsBar are required");
+        return FS2D_ERR_INVALID;
+    }
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    DevScratch sc;
+    double *mu = sc.get<double>(s->NU), *mv = sc.get<double>(s->NV), *wu = sc.get<double>(s->NU),
+           *wv = sc.get<double>(s->NV);
+    double2* vb = sc.get<double2>(s->np);
+    if (!mu || !mv || !wu || !wv || !vb) {
+        set_error("fs2d_p2g_adjoint: device scratch allocation failed");
+        return FS2D_ERR_ALLOC;
+    }
+    FS2D_CUDA(cudaMemcpyAsync(mu, uBar, s->NU * sizeof(double), cudaMemcpyDefault, s->stream));
+    FS2D_CUDA(cudaMemcpyAsync(mv, vBar, s->NV * sizeof(double), cudaMemcpyDefault, s->stream));
+    int rc = p2g_adjoint(s, mu, mv, wu, wv, vb);
+    if (rc) return rc;
+    if (s->np > 0)
+        FS2D_CUDA(cudaMemcpyAsync(particleVelsBar, vb, s->np * sizeof(double2), cudaMemcpyDefault, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    return finish(h);
+}
+
+int fs2d_g2p_adjoint(fs2d_sim* p, const double* particleVelsBar, double* newUBar, double* newVBar, double* uBar,
+                     double* vBar, double* particleVelsInBar) {
+    if (!p || !particleVelsBar || !newUBar || !newVBar || !uBar || !vBar || !particleVelsInBar) {
+        set_error("fs2d_g2p_adjoint: every array is required");
+        return FS2D_ERR_INVALID;
+    }
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    DevScratch sc;
+    double *nub = sc.get<double>(s->NU), *nvb = sc.get<double>(s->NV), *ub = sc.get<double>(s->NU),
+           *vb = sc.get<double>(s->NV);
+    double2 *gb = sc.get<double2>(s->np), *ib = sc.get<double2>(s->np);
+    if (!nub || !nvb || !ub || !vb || !gb || !ib) {
+        set_error("fs2d_g2p_adjoint: device scratch allocation failed");
+        return FS2D_ERR_ALLOC;
+    }
+    if (s->np > 0)
+        FS2D_CUDA(cudaMemcpyAsync(gb, particleVelsBar, s->np * sizeof(double2), cudaMemcpyDefault, s->stream));
+    int rc = g2p_adjoint(s, gb, nub, nvb, ub, vb, ib);
+    if (rc) return rc;
+    FS2D_CUDA(cudaMemcpyAsync(newUBar, nub, s->NU * sizeof(double), cudaMemcpyDefault, s->stream));
+    FS2D_CUDA(cudaMemcpyAsync(newVBar, nvb, s->NV * sizeof(double), cudaMemcpyDefault, s->stream));
+    FS2D_CUDA(cudaMemcpyAsync(uBar, ub, s->NU * sizeof(double), cudaMemcpyDefault, s->stream));
+    FS2D_CUDA(cudaMemcpyAsync(vBar, vb, s->NV * sizeof(double), cudaMemcpyDefault, s->stream));
+    if (s->np > 0)
+        FS2D_CUDA(cudaMemcpyAsync(particleVelsInBar, ib, s->np * sizeof(double2), cudaMemcpyDefault, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    return finish(h);
 }
 
 int fs2d_backward(fs2d_sim* p, double* gradU0, double* gradV0) {

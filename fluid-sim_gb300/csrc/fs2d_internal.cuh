@@ -278,6 +278,10 @@ int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double
                      const int W[2], const int H[2], int band);
 int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n);
 
+// ---- transposes of the particle transfers (transfer.cu) ----
+int p2g_adjoint(Sim* s, double* ubar, double* vbar, double* wu, double* wv, double2* velbar);
+int g2p_adjoint(Sim* s, const double2* velbar, double* nub, double* nvb, double* ub, double* vb, double2* vinb);
+
 // ---- differentiable rollout (adjoint.cu) ----
 int rollout_forward(Sim* s, int steps, int every, const double* u0, const double* v0, const double* ut,
                     const double* vt, double* loss);

@@ -210,6 +210,77 @@ __global__ void k_g2p(const double2* __restrict__ pos, double2* vel, size_t np, 
     vel[e] = make_double2(alpha * picx + (1 - alpha) * flipx, alpha * picy + (1 - alpha) * flipy);
 }
 
+// ---- transposes of the particle transfers (fixed particle positions) ----
+
+// Sum of the bilinear weights per face (linearDistribute's weight splat).
+__global__ void k_p2g_weights(const double2* __restrict__ pos, size_t np, double dx, int NX, int NY, double* wu,
+                              double* wv) {
+    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    double2 p = pos[e];
+    double x, y;
+    upos(p, dx, x, y);
+    Bilinear bu(x, y, NX + 1, NY);
+    vpos(p, dx, x, y);
+    Bilinear bv(x, y, NX, NY + 1);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        atomicAdd(wu + bu.face(k, NX + 1), bu.contrib(k, 1.0));
+        atomicAdd(wv + bv.face(k, NX), bv.contrib(k, 1.0));
+    }
+}
+
+// P2G^T after E^T: a particle's velocity adjoint gathers, over its corners
+// whose face kept its splatted value (mask 0), weight * mu / (sum of weights).
+__global__ void k_p2g_adjoint(const double2* __restrict__ pos, size_t np, double dx, int NX, int NY,
+                              const double* __restrict__ mu, const double* __restrict__ mv,
+                              const double* __restrict__ wu, const double* __restrict__ wv,
+                              const uint32_t* __restrict__ mask_u, const uint32_t* __restrict__ mask_v,
+                              double2* velbar) {
+    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    double2 p = pos[e];
+    double x, y;
+    upos(p, dx, x, y);
+    Bilinear bu(x, y, NX + 1, NY);
+    vpos(p, dx, x, y);
+    Bilinear bv(x, y, NX, NY + 1);
+    double gx = 0.0, gy = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int fu = bu.face(k, NX + 1), fv = bv.face(k, NX);
+        if (mask_u[fu] == 0 && wu[fu] > 0) gx += bu.contrib(k, 1.0) * mu[fu] / wu[fu];
+        if (mask_v[fv] == 0 && wv[fv] > 0) gy += bv.contrib(k, 1.0) * mv[fv] / wv[fv];
+    }
+    velbar[e] = make_double2(gx, gy);
+}
+
+// G2P^T: v_new = alpha pic + (1 - alpha)(v + flip delta), pic = G newMac,
+// delta = G (newMac - mac), so newMac^bar += G^T vbar, mac^bar -= (1 - alpha)
+// G^T vbar, v^bar = (1 - alpha) vbar.
+__global__ void k_g2p_adjoint(const double2* __restrict__ pos, const double2* __restrict__ vbar, size_t np, double dx,
+                              int NX, int NY, double alpha, double* nub, double* nvb, double* ub, double* vb,
+                              double2* vinb) {
+    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    double2 p = pos[e], g = vbar[e];
+    double x, y;
+    upos(p, dx, x, y);
+    Bilinear bu(x, y, NX + 1, NY);
+    vpos(p, dx, x, y);
+    Bilinear bv(x, y, NX, NY + 1);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int fu = bu.face(k, NX + 1), fv = bv.face(k, NX);
+        const double au = bu.contrib(k, 1.0) * g.x, av = bv.contrib(k, 1.0) * g.y;
+        atomicAdd(nub + fu, au);
+        atomicAdd(ub + fu, -(1 - alpha) * au);
+        atomicAdd(nvb + fv, av);
+        atomicAdd(vb + fv, -(1 - alpha) * av);
+    }
+    vinb[e] = make_double2((1 - alpha) * g.x, (1 - alpha) * g.y);
+}
+
 // ---- extrapolation ----
 
 // Column pass of the L1 distance transform: vertical distance to the nearest
@@ -619,6 +690,38 @@ int p2g(Sim* s) {
                     s->ent_v, NV, s->v, s->mask_v);
     }
     return extrapolate(s, s->u, s->mask_u, NX + 1, NY, s->v, s->mask_v, NX, NY + 1);
+}
+
+int extrap_adjoint(Sim* s, double* mu, const uint32_t* layer, int W, int H, uint32_t lim);
+
+// P2G^T at the current particle positions and the masks of the last P2G:
+// (ubar, vbar) face adjoints (device, overwritten by E^T) -> velbar.
+int p2g_adjoint(Sim* s, double* ubar, double* vbar, double* wu, double* wv, double2* velbar) {
+    const int NX = s->NX, NY = s->NY, T = 256;
+    const uint32_t lim = s->opt.extrapolate_band > 0 ? (uint32_t)s->opt.extrapolate_band : 0xFFFFFFFEu;
+    int rc = extrap_adjoint(s, ubar, s->mask_u, NX + 1, NY, lim);
+    if (!rc) rc = extrap_adjoint(s, vbar, s->mask_v, NX, NY + 1, lim);
+    if (rc) return rc;
+    FS2D_CUDA(cudaMemsetAsync(wu, 0, s->NU * sizeof(double), s->stream));
+    FS2D_CUDA(cudaMemsetAsync(wv, 0, s->NV * sizeof(double), s->stream));
+    if (s->np == 0) return 0;
+    FS2D_LAUNCH(s, k_p2g_weights, blocks_for(s->np, T), T, 0, s->pos, s->np, s->dx, NX, NY, wu, wv);
+    FS2D_LAUNCH(s, k_p2g_adjoint, blocks_for(s->np, T), T, 0, s->pos, s->np, s->dx, NX, NY, ubar, vbar, wu, wv,
+                s->mask_u, s->mask_v, velbar);
+    return 0;
+}
+
+// G2P^T at the current particle positions: velbar -> (newMac, mac, vel) adjoints (zeroed first).
+int g2p_adjoint(Sim* s, const double2* velbar, double* nub, double* nvb, double* ub, double* vb, double2* vinb) {
+    const int T = 256;
+    FS2D_CUDA(cudaMemsetAsync(nub, 0, s->NU * sizeof(double), s->stream));
+    FS2D_CUDA(cudaMemsetAsync(nvb, 0, s->NV * sizeof(double), s->stream));
+    FS2D_CUDA(cudaMemsetAsync(ub, 0, s->NU * sizeof(double), s->stream));
+    FS2D_CUDA(cudaMemsetAsync(vb, 0, s->NV * sizeof(double), s->stream));
+    if (s->np == 0) return 0;
+    FS2D_LAUNCH(s, k_g2p_adjoint, blocks_for(s->np, T), T, 0, s->pos, velbar, s->np, s->dx, s->NX, s->NY, s->alpha,
+                nub, nvb, ub, vb, vinb);
+    return 0;
 }
 
 int g2p(Sim* s) {

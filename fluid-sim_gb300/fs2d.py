@@ -91,6 +91,9 @@ SIGNATURES = {
     "fs2d_forward": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.POINTER(C.c_double)]),
     "fs2d_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fs2d_p2g_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "fs2d_g2p_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p]),
     "fs2d_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.POINTER(C.c_void_p)]),
     "fs2d_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
     "fs2d_batch_size": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
@@ -300,6 +303,31 @@ class FluidSim2D:
         gu, gv = np.empty((NX + 1) * NY), np.empty(NX * (NY + 1))
         _check(load().fs2d_backward(self.h, gu.ctypes.data, gv.ctypes.data))
         return gu, gv
+
+    def p2g_adjoint(self, u_bar, v_bar):
+        """Transpose of transferVelocityToGrid at the current particle
+        positions (after that stage ran): face adjoints -> particle velocity
+        adjoints (2 per particle)."""
+        NX, NY = self.nx, self.ny
+        ub = np.ascontiguousarray(u_bar, dtype=np.float64).reshape(-1)
+        vb = np.ascontiguousarray(v_bar, dtype=np.float64).reshape(-1)
+        assert ub.size == (NX + 1) * NY and vb.size == NX * (NY + 1)
+        out = np.zeros(2 * self.num_particles())
+        _check(load().fs2d_p2g_adjoint(self.h, ub.ctypes.data, vb.ctypes.data, out.ctypes.data))
+        return out
+
+    def g2p_adjoint(self, vel_bar):
+        """Transpose of updateParticleVelocities: adjoint of the new particle
+        velocities -> adjoints of (newU, newV, u, v, old velocities)."""
+        NX, NY = self.nx, self.ny
+        gb = np.ascontiguousarray(vel_bar, dtype=np.float64).reshape(-1)
+        assert gb.size == 2 * self.num_particles()
+        nub, ub = np.zeros((NX + 1) * NY), np.zeros((NX + 1) * NY)
+        nvb, vb = np.zeros(NX * (NY + 1)), np.zeros(NX * (NY + 1))
+        ib = np.zeros_like(gb)
+        _check(load().fs2d_g2p_adjoint(self.h, gb.ctypes.data, nub.ctypes.data, nvb.ctypes.data, ub.ctypes.data,
+                                       vb.ctypes.data, ib.ctypes.data))
+        return nub, nvb, ub, vb, ib
 
     def render_export(self, buffers, caps):
         """fs2d_render_export into device buffers: `buffers` maps field names

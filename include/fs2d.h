@@ -201,6 +201,28 @@ int fs2d_forward(fs2d_sim* sim, int steps, int checkpointEvery, const double* u0
                  const double* uTarget, const double* vTarget, double* loss);
 int fs2d_backward(fs2d_sim* sim, double* gradU0, double* gradV0);
 
+/* Transposes of the particle transfers, for reverse-mode use with the
+ * particle positions held fixed (no reference counterpart).  Both act at the
+ * handle's current particle positions.
+ *
+ * fs2d_p2g_adjoint: transferVelocityToGrid (src/FluidSim2D.cpp:144-204) maps
+ * the particle velocities linearly to the face velocities (bilinear splat,
+ * division by the summed weights, extrapolation of the unknown faces).  Call
+ * it after that stage ran on the current positions (it uses the stage's
+ * known/unknown masks); (uBar, vBar), adjoints of the face grids, give
+ * particleVelsBar (2 per particle, interleaved).
+ *
+ * fs2d_g2p_adjoint: updateParticleVelocities (:552-568) maps (newMac, mac,
+ * particle velocities) linearly to the new particle velocities; the adjoint
+ * of the new velocities gives the adjoints of newMac (newUBar, newVBar), of
+ * mac (uBar, vBar) and of the old velocities (particleVelsInBar).
+ *
+ * Pointers may be host or device memory; scratch is allocated with
+ * cudaMalloc for the duration of the call. */
+int fs2d_p2g_adjoint(fs2d_sim* sim, const double* uBar, const double* vBar, double* particleVelsBar);
+int fs2d_g2p_adjoint(fs2d_sim* sim, const double* particleVelsBar, double* newUBar, double* newVBar, double* uBar,
+                     double* vBar, double* particleVelsInBar);
+
 /* Batches of independent scenes.  No reference counterpart (the reference
  * runs one scene per process).  fs2d_batch_create makes one handle per
  * scene (cfgs[k], all with the options `opt`, which may be NULL; with
