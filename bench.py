@@ -192,7 +192,7 @@ def reference_arm(args):
     sc = workload(args.size)
     sim = oracle_py.OracleSim(sc, seed=SEED, omp=True, sl_inplace=0, pcg_tol=args.tol, pcg_max_iters=200)
     n_particles = sim.num_particles()
-    warm = min(args.warmup, 2)
+    warm = min(args.warmup, 5)   # about a second per frame on 16 Grace cores
     for _ in range(warm):
         sim.frame()
     frames, t0 = 0, time.perf_counter()
