@@ -8,6 +8,8 @@
 // grids of a batch fill the 152 SMs together instead of one after another.
 // A frame's few host synchronisations (the pressure solver's convergence
 // polls, the extrapolation depth) block only the worker that issued it.
+// (Blocking-sync events instead of spinning waits, with up to twice as many
+// workers as cores, measured slightly slower on the 256-scene batch.)
 //
 // Scenes go to workers longest-first onto the least-loaded worker (load =
 // cells), which balances uneven grid sizes.  The differentiable rollout

@@ -388,7 +388,7 @@ int finish(Host* h) {
     Sim* s = &h->sim;
     FS2D_CUDA(cudaMemcpyAsync(s->err_host, s->err, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
     FS2D_CUDA(cudaMemcpyAsync(s->stats_host, s->stats, sizeof(FrameStats), cudaMemcpyDeviceToHost, s->stream));
-    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    if (int rcw = wait_stream(s, s->stream)) return rcw;
     ktimer_collect(s);
     if (h->stats_pending) {
         if (s->hist_n == s->hist_cap) {
@@ -879,7 +879,7 @@ static int run_diag(fs2d_sim* p) {
     int rc = diagnostics(s);
     if (rc) return rc;
     FS2D_CUDA(cudaMemcpyAsync(s->stats_host, s->stats, sizeof(FrameStats), cudaMemcpyDeviceToHost, s->stream));
-    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    if (int rcw = wait_stream(s, s->stream)) return rcw;
     return FS2D_OK;
 }
 

@@ -245,6 +245,9 @@ inline int ensure_smem_attr(std::atomic<unsigned long long>& done, int device, c
     return rc;
 }
 
+// Waits for the work queued on `st` (the handle's stream) to finish.
+inline int wait_stream(Sim*, cudaStream_t st) { return check_cuda(cudaStreamSynchronize(st), "cudaStreamSynchronize"); }
+
 inline unsigned int blocks_for(size_t n, int threads) { return (unsigned int)((n + threads - 1) / threads); }
 
 // ---- stage entry points (implemented in the per-stage .cu files) ----

@@ -493,12 +493,12 @@ static int projection_pcg(Sim* s, int* status) {
         FS2D_LAUNCH(s, k_dot_zr, nb, kT, 0, s->z, s->r, N, s->partial, s->pcg, 0, max_iters);
         if ((it + 1) % batch == 0 || it + 1 == max_iters) {
             FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, s->pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
-            FS2D_CUDA(cudaStreamSynchronize(s->stream));
+            if (int rcw = wait_stream(s, s->stream)) return rcw;
             if (s->pcg_host->done) break;
         }
     }
     FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, s->pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
-    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    if (int rcw = wait_stream(s, s->stream)) return rcw;
     const PcgScalars& h = *s->pcg_host;
     s->last_iters = h.iter;
     s->last_outer = 0;

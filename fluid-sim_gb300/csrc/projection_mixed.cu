@@ -399,7 +399,7 @@ int projection_mixed_rhs(Sim* s, const double* b, int* status) {
     int total_iters = 0, outer_iters = 0, status_out = 0;
 
     FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, outer, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
-    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    if (int rcw = wait_stream(s, s->stream)) return rcw;
     const double rhs_norm = s->pcg_host->rhs_norm;
     const double tol_abs = s->pcg_host->tol_abs;
     double r_norm = rhs_norm;
@@ -431,11 +431,15 @@ int projection_mixed_rhs(Sim* s, const double* b, int* status) {
                 FS2D_LAUNCH(s, k_dot32, rg, kRT, 0, m.z, m.r, NX, NY, P, part2, inner, 0, max_iters);
                 return 0;
             };
-            auto poll_done = [&]() -> int {
-                FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost,
-                                          s->stream));
-                FS2D_CUDA(cudaStreamSynchronize(s->stream));
-                return s->pcg32_host->done;
+            // true once the inner solve stopped; a failed copy or wait also
+            // stops it and leaves its status in rc_poll
+            int rc_poll = 0;
+            auto poll_done = [&]() -> bool {
+                rc_poll = check_cuda(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars),
+                                                     cudaMemcpyDeviceToHost, s->stream),
+                                     "cudaMemcpyAsync");
+                if (!rc_poll) rc_poll = wait_stream(s, s->stream);
+                return rc_poll != 0 || s->pcg32_host->done != 0;
             };
             // Captures kM32GraphIters iterations as a CUDA graph (once per handle,
             // again whenever the reduction scratch moved); false: launch directly
@@ -494,12 +498,13 @@ int projection_mixed_rhs(Sim* s, const double* b, int* status) {
                     if (poll_done()) break;
                 }
             }
+            if (rc_poll) return rc_poll;
             FS2D_LAUNCH(s, k_update64, nb, kT, 0, s->p, m.e, outer, NX, P, N);
             FS2D_LAUNCH(s, k_resid64, nb, kT, 0, s->cell, s->Adiag, s->Ax, s->Ay, s->rhs, s->p, s->r, NX, N,
                         s->partial, outer);
             FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
             FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, outer, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
-            FS2D_CUDA(cudaStreamSynchronize(s->stream));
+            if (int rcw = wait_stream(s, s->stream)) return rcw;
             total_iters += s->pcg32_host->iter;
             r_norm = s->pcg_host->r_norm;
         }

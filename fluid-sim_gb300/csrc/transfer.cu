@@ -633,7 +633,7 @@ int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double
     }
     unsigned int hmax[2] = {0, 0};
     FS2D_CUDA(cudaMemcpyAsync(hmax, x.max_layer, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
-    FS2D_CUDA(cudaStreamSynchronize(stream));
+    if (int rcw = wait_stream(s, stream)) return rcw;
     for (int gi = 0; gi < ng; gi++) {
         int maxL = (int)std::min<unsigned int>(hmax[gi], (unsigned int)band_limit);
         for (int lo = 1; lo <= maxL; lo += kBand) {
