@@ -47,8 +47,14 @@ FLUSH_BYTES = 256 << 20          # > 129 MB L2
 #   eik_sweep: read phi (8 B) and the changeability byte, write phi: 17 B
 #   cp_sweep: read the closest-particle index (4 B) and its 16-byte
 #            position pair, write the index: 24 B
+#   k_spmv32: s = z + beta s_old, w = A s, s.w: reads label (1 B), three
+#            matrix arrays, z and s_old, writes s and w: 29 B
+#   k_axpy32: e += alpha s, r -= alpha w, r pc^2, ||r||inf: reads e, s, r, w,
+#            pc, writes e, r, r pc^2: 32 B
+#   k_dot32: z.r: 8 B
 KERNEL_BYTES_PER_CELL = {"mic32": 16, "mic32_forward": 16, "mic32_backward": 16, "wave2_MicForward64": 40,
-                         "wave2_MicBackward64": 40, "eik_sweep": 17, "cp_sweep": 24}
+                         "wave2_MicBackward64": 40, "eik_sweep": 17, "cp_sweep": 24, "k_spmv32": 29,
+                         "k_axpy32": 32, "k_dot32": 8}
 DOMINANT = tuple(KERNEL_BYTES_PER_CELL)
 
 
@@ -328,13 +334,20 @@ def main():
             for line in open(tf):
                 parts = line.split()
                 if len(parts) >= 3 and parts[0] == dom and parts[1] == args.precision:
-                    traffic = float(parts[2])
+                    # measured per launch at 1024^2; a launch reads each cell's operands once
+                    traffic = float(parts[2]) * cells / (1024 * 1024)
         roofline = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                     "frac": round(achieved / peak, 4), "peak_source": peak_src,
                     "traffic": traffic, "launches": n_launch, "avg_launch_us": round(1000 * ms / n_launch, 2),
                     "algorithmic_bytes_per_launch": alg_bytes,
                     "share_of_step": round(ktimes[dom][1] / kt_total, 3),
                     "kernel_ms_per_step": {k: round(v[1] / kt_steps, 3) for k, v in sorted(ktimes.items())},
+                    "kernels": {k: {"launches_per_step": v[0] / kt_steps, "ms_per_step": round(v[1] / kt_steps, 3),
+                                    "achieved_gbs": round(KERNEL_BYTES_PER_CELL[k] * cells * v[0] / (v[1] / 1000.0)
+                                                          / 1e9, 1),
+                                    "frac": round(KERNEL_BYTES_PER_CELL[k] * cells * v[0] / (v[1] / 1000.0) / 1e9
+                                                  / peak, 4)}
+                                for k, v in sorted(ktimes.items()) if k in KERNEL_BYTES_PER_CELL and v[1] > 0},
                     "timed_over": f"{kt_steps} extra steps with per-launch events"}
 
     # ---- whole-step roofline: compulsory bytes of every stage per step ----
