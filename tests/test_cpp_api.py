@@ -41,3 +41,33 @@ def test_cpp_api_runs(tmp_path, mode):
     exe = build(tmp_path)
     r = subprocess.run([exe, mode], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout + r.stderr
+
+
+C_SRC = os.path.join(ROOT, "tests", "cpp", "capi_rollout_batch_test.c")
+
+
+def build_c(tmp_path):
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    if not os.path.exists(os.path.join(LIBDIR, "libfs2d.so")):
+        pytest.skip("libfs2d.so not built")
+    exe = str(tmp_path / "capi_rollout_batch_test")
+    cmd = [gcc, "-std=c11", "-D_DEFAULT_SOURCE", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"),
+           C_SRC, "-o", exe, "-L", LIBDIR, "-lfs2d", "-Wl,-rpath," + LIBDIR, "-lm"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "warning" not in r.stderr, r.stderr
+    return exe
+
+
+def test_c_abi_program_builds(tmp_path):
+    """fs2d.h compiles as C11; the rollout, transfer and batch entry points link."""
+    build_c(tmp_path)
+
+
+@pytest.mark.gpu
+def test_c_abi_rollout_and_batch_run(tmp_path):
+    exe = build_c(tmp_path)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout + r.stderr
