@@ -53,8 +53,11 @@ constexpr int kCpSlots = 8;
 constexpr int kCpAhead = 4;        // tiles requested ahead
 constexpr int kCpD = 8;            // gather distance (columns)
 constexpr int kCpR = 16;           // gather ring slots per row (power of two > kCpD + 1)
-constexpr int kCpCH = 16;          // chunk of the row below
-constexpr int kCpBndChunks = 8;
+// Chunk of the row below (columns per arrival check): smaller chunks shorten
+// the strip-to-strip lag (measured at 1024^2: 16 and 8 columns gave 9.8 and
+// 8.9 ms of sweeps per frame, 4 columns no better than 8).
+constexpr int kCpCH = 8;
+constexpr int kCpBndChunks = 128 / kCpCH;
 constexpr int kCpTopRing = 256;
 constexpr int kCpTileInts = kCpBoxRows * kCpCols;
 constexpr unsigned kCpTileBytes = kCpTileInts * 4;

@@ -40,8 +40,13 @@ constexpr int kEkCols = 32;
 constexpr int kEkRows = 32;
 constexpr int kEkSlots = 8;
 constexpr int kEkAhead = 4;
-constexpr int kEkCH = 16;          // columns per arrival check / flow-control chunk
-constexpr int kEkRingChunks = 16;
+// Columns per arrival check / flow-control chunk.  A strip waits for whole
+// chunks of the row below, so the chunk adds to the strip-to-strip lag; an
+// Eikonal step is long (dependent FP64 updates), so a check every 4 columns
+// costs little (measured at 1024^2: chunks of 16, 8, 4, 2 columns gave
+// 14.8, 13.6, 13.2, 13.5 ms of sweeps per frame).
+constexpr int kEkCH = 4;
+constexpr int kEkRingChunks = 256 / kEkCH;
 constexpr int kEkRing = kEkRingChunks * kEkCH;   // boundary ring, columns
 constexpr int kEkTopRing = 256;
 constexpr unsigned kEkTileBytes = kEkCols * kEkRows * 8;
@@ -177,8 +182,9 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         while (hb < P || tc < tend || ts < nt) {
             bool moved = false;
             // row below from global memory (the previous strip is in another cluster)
-            if (hb < P && hb < (*bnd_used + kEkRingChunks - 2) * kEkCH) {
-                const int n = min(32, P - hb);
+            const int hb_lim = (*bnd_used + kEkRingChunks - 2) * kEkCH;   // slots consumed two chunks ago
+            if (hb < P && hb < hb_lim) {
+                const int n = min(min(32, P - hb), hb_lim - hb);
                 const unsigned long long need = a.base + (unsigned long long)(hb + n);
                 if (gavail < need) {
                     unsigned long long v = 0;

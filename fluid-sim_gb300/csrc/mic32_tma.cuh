@@ -145,8 +145,9 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
         while (hb < ncols || tc < tend || ts < nt) {
             bool moved = false;
             // row below from global memory (the previous strip is in another cluster)
-            if (hb < ncols && hb < (*bnd_used + kM32BndChunks - 2) * kM32CH) {
-                const int n = min(32, ncols - hb);
+            const int hb_lim = (*bnd_used + kM32BndChunks - 2) * kM32CH;   // slots consumed two chunks ago
+            if (hb < ncols && hb < hb_lim) {
+                const int n = min(min(32, ncols - hb), hb_lim - hb);
                 const unsigned long long need = base + (unsigned long long)(hb + n);
                 if (gavail < need) {
                     unsigned long long v = 0;
