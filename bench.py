@@ -18,6 +18,21 @@ stopping test); the all-FP64 GPU path is measured beside it ("fp64_path").
 
 One JSON line is printed by rank 0.  Multi-GPU runs are independent
 replicas (the step does not shard); value = total cell-steps / max time.
+Besides the headline keys the line carries:
+  roofline        the dominant kernel (and every timed kernel with a known
+                  byte count) against the measured HBM copy peak;
+  step_roofline   the compulsory bytes of every stage of a step / step time;
+  fp64_path       the all-FP64 GPU step on the same workload;
+  sl_path         the semi-Lagrangian dam break at the same size;
+  pressure_solve  the standalone 2048^2 solve to 1e-10, FP64 vs mixed;
+  adjoint         the differentiable 128^2 closed-box rollout (64 steps):
+                  forward and backward times in both precisions;
+  batch           256 dam breaks of uneven sizes advanced together (split
+                  over the ranks when N > 1);
+  batch_adjoint   the rollouts of 32 closed boxes of uneven sizes;
+  e2e             the headline through the C ABI with host buffers;
+  cpu_baseline    the CPU oracle port timed on the host's cores.
+Each extra line has a flag that switches it off (e.g. --adjoint-size 0).
 """
 from __future__ import annotations
 
