@@ -78,14 +78,15 @@ __device__ __forceinline__ float m32_entry_value(unsigned long long e) { return 
 // Block of 64 threads: warp 0 computes, warp 1 moves the strip boundaries
 // (so no remote write, release or L2 round trip stalls the compute warp).
 template <bool FWD>
-// base_dev: when non-null, the launch's progress base is read from device
-// memory (launches replayed from a CUDA graph, each preceded by a bump of
-// that counter) instead of the by-value `base_host`.
+// base_dev: when non-null, the launch's progress base is the device-memory
+// value plus `base_host` (launches replayed from a CUDA graph: one bump of
+// that counter per replay, and a fixed offset per sweep of the replay);
+// otherwise `base_host` alone.
 __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32Maps maps, float* out, int P, int NY,
                                                    unsigned long long* progress, unsigned long long base_host,
                                                    const unsigned long long* base_dev, int* err, const int* skip) {
     if (skip != nullptr && *skip) return;
-    const unsigned long long base = base_dev != nullptr ? *base_dev : base_host;
+    const unsigned long long base = base_dev != nullptr ? *base_dev + base_host : base_host;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* ring = reinterpret_cast<float*>(smem_raw);
     // row below the strip, kM32BndRing columns of tagged entries
@@ -400,17 +401,21 @@ int mic32_make_map(CUtensorMap* map, float* base, int P, int NY, int box_rows);
 // Launches one sweep: cooperative (every strip co-resident, so the waits
 // between strips always make progress) and, where the device can hold them,
 // in clusters of up to 8 strips that hand rows over in shared memory.
-// Advances the device-side progress base of graph-replayed sweeps.
-__global__ void k_wave_bump(unsigned long long* base) { *base += 1ull << 24; }
+// Advances the device-side progress base of graph-replayed sweeps by `n`
+// sweeps' worth.
+__global__ void k_wave_bump(unsigned long long* base, unsigned long long n) { *base += n << 24; }
 
 // Launches one sweep: cooperative (every strip co-resident, so the waits
 // between strips always make progress) and, where the device can hold them,
 // in clusters of up to 8 strips that hand rows over in shared memory.
-// graph = true: for stream capture; the sweep uses its own progress counters
-// and a base in device memory, bumped by a preceding kernel, so that every
-// replay of the captured launch gets a fresh base.
+// graph_slot >= 0: for stream capture; the sweep is number graph_slot of the
+// graph_sweeps sweeps of one replay, uses its own progress counters and the
+// device-memory base plus graph_slot sweeps; slot 0 first advances that base
+// by graph_sweeps, so that every replay gets fresh bases.
 template <bool FWD>
-int launch_mic32(Sim* s, const Mic32Maps& maps, float* out, const int* skip, bool graph = false) {
+int launch_mic32(Sim* s, const Mic32Maps& maps, float* out, const int* skip, int graph_slot = -1,
+                 int graph_sweeps = 0) {
+    const bool graph = graph_slot >= 0;
     const int nstrips = (s->NY + kM32Rows - 1) / kM32Rows;
     if (nstrips > s->progress_cap) {
         set_error("mic32: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
@@ -422,7 +427,8 @@ int launch_mic32(Sim* s, const Mic32Maps& maps, float* out, const int* skip, boo
     const unsigned long long* base_dev = nullptr;
     unsigned long long* progress = s->progress;
     if (graph) {
-        FS2D_LAUNCH(s, k_wave_bump, 1, 1, 0, s->m32_gbase);
+        if (graph_slot == 0) FS2D_LAUNCH(s, k_wave_bump, 1, 1, 0, s->m32_gbase, (unsigned long long)graph_sweeps);
+        base = (unsigned long long)graph_slot << 24;
         base_dev = s->m32_gbase;
         progress = s->m32_gprogress;
     } else {

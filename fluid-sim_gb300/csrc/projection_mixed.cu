@@ -424,9 +424,10 @@ int projection_mixed_rhs(Sim* s, const double* b, int* status) {
                 FS2D_LAUNCH(s, k_spmv32, rg, kRT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, NY, P,
                             part2, inner);
                 FS2D_LAUNCH(s, k_axpy32, rg, kRT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, NX, NY, P, partf, inner);
-                int rc1 = launch_mic32<true>(s, fmaps, m.q, done, graph);
+                const int slot = graph ? 2 * (it % kM32GraphIters) : -1;   // sweeps of one replay
+                int rc1 = launch_mic32<true>(s, fmaps, m.q, done, slot, 2 * kM32GraphIters);
                 if (rc1) return rc1;
-                rc1 = launch_mic32<false>(s, bmaps, m.z, done, graph);
+                rc1 = launch_mic32<false>(s, bmaps, m.z, done, graph ? slot + 1 : -1, 2 * kM32GraphIters);
                 if (rc1) return rc1;
                 FS2D_LAUNCH(s, k_dot32, rg, kRT, 0, m.z, m.r, NX, NY, P, part2, inner, 0, max_iters);
                 return 0;
