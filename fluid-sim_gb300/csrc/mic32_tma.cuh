@@ -301,11 +301,17 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 pn = cell_ptr(c0 < 0 ? 0 : c0);
                 load_next(pn);
             }
+            // one chunk of the row below per group: a rolled loop of two
+            // groups with the chunk's steps unrolled measured 2-6 % faster
+            // than the whole tile unrolled
+#pragma unroll 1
+            for (int g = 0; g < kM32Cols; g += kM32CH) {
 #pragma unroll
-            for (int u = 0; u < kM32Cols; u++) {
+            for (int u8 = 0; u8 < kM32CH; u8++) {
+                const int u = g + u8;
                 const int s = t * kM32Cols + u;
                 const int c = s - lane;
-                if (below_in_grid && (u % kM32CH) == 0 && (!check || s < ncols)) {
+                if (below_in_grid && u8 == 0 && (!check || s < ncols)) {
                     // lane 0 enters a chunk of the row below: every column of
                     // it must have arrived (one entry per lane, one vote)
                     const int cc = s + (lane & (kM32CH - 1));
@@ -341,7 +347,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 float below = __shfl_up_sync(0xffffffffu, o[3], 1);
                 const float b0 = below_in_grid ? m32_entry_value(bn) : 0.0f;
                 // next step's entry (same chunk; a new chunk is read after its check)
-                if (((s + 1) % kM32CH) != 0) bn = bnd_p[(s + 1) % kM32BndRing];
+                if (u8 + 1 != kM32CH) bn = bnd_p[(s + 1) % kM32BndRing];
                 if (lane == 0) below = b0;
                 if (!check || (c >= 0 && c < ncols)) {
                     float r[4];
@@ -357,6 +363,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                     }
                     if (has_next && lane == 31) top_p[c % kM32TopRing] = m32_entry(c, o[3]);
                 }
+            }
             }
         };
 
