@@ -27,6 +27,13 @@
 //           of the weights; zero where a position was clamped) flows back
 //           through k3, k2, k1, each of which scatters into u and v with the
 //           weights at its own point (atomic adds).
+//
+// The host driver (rollout_forward / rollout_backward) keeps the state before
+// every `every`-th step (default ceil(sqrt(T))), and in reverse recomputes
+// each segment from its checkpoint before walking it backwards; the forward
+// pass already leaves the last segment's states in the segment buffer.
+// extrap_adjoint (E^T of one face grid) is shared with the particle-transfer
+// transposes in transfer.cu.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <algorithm>
