@@ -360,7 +360,7 @@ int mixed_setup_maps(Sim* s) {
     return 0;
 }
 
-constexpr int kM32GraphIters = 4;   // inner iterations per graph replay (even: the search-direction ping-pong)
+constexpr int kM32GraphIters = 8;   // inner iterations per graph replay (even: the search-direction ping-pong)
 
 int projection_mixed(Sim* s, int* status) { return projection_mixed_rhs(s, nullptr, status); }
 
