@@ -10,8 +10,9 @@ Two kinds of artefacts:
   (``src/FluidSim2D.cpp``, ``src/PerformanceCounter.cpp``), compiled in
   place from the reference checkout together with the compatibility shim
   (``oracle/shim``) and a C wrapper (``oracle/ref_capi.cpp``).  Only built
-  when the reference checkout exists (``FS2D_REFERENCE_DIR``, default
-  ``/root/reference``).  Variants:
+  when the location of a reference checkout is given, as the argument of
+  ``build_reference`` or in the environment variable ``FS2D_REFERENCE_DIR``
+  (there is no default location).  Variants:
     - ``libfs2d_ref.so``      scalar path (USE_AVX off), serial,
                               ``-O2 -ffp-contract=off`` — the parity build;
     - ``libfs2d_ref_avx.so``  the reference's Release configuration on x86:
@@ -29,7 +30,6 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE_DIR = os.environ.get("FS2D_REFERENCE_DIR", "/root/reference")
 
 
 def _run(cmd):
@@ -63,22 +63,32 @@ def build_restatement(force=False):
     return plain
 
 
-def reference_available():
-    return os.path.exists(os.path.join(REFERENCE_DIR, "src", "FluidSim2D.cpp"))
+def reference_dir(path=None):
+    """The reference checkout: `path`, else $FS2D_REFERENCE_DIR; None when
+    neither names a directory holding src/FluidSim2D.cpp."""
+    path = path or os.environ.get("FS2D_REFERENCE_DIR")
+    if path and os.path.exists(os.path.join(path, "src", "FluidSim2D.cpp")):
+        return path
+    return None
 
 
-def build_reference(force=False):
+def reference_available(path=None):
+    return reference_dir(path) is not None
+
+
+def build_reference(force=False, path=None):
     """Compile the reference in place; returns the list of built libraries
-    (empty when the reference checkout is absent)."""
-    if not reference_available():
+    (empty when no reference checkout is given)."""
+    ref_dir = reference_dir(path)
+    if ref_dir is None:
         return []
     os.makedirs(REF_OUT, exist_ok=True)
-    srcs = [os.path.join(REFERENCE_DIR, "src", "FluidSim2D.cpp"),
-            os.path.join(REFERENCE_DIR, "src", "PerformanceCounter.cpp"),
+    srcs = [os.path.join(ref_dir, "src", "FluidSim2D.cpp"),
+            os.path.join(ref_dir, "src", "PerformanceCounter.cpp"),
             os.path.join(HERE, "ref_capi.cpp")]
     shim = os.path.join(HERE, "shim", "altlib")
     noavx = os.path.join(HERE, "shim", "noavx")
-    inc = os.path.join(REFERENCE_DIR, "include")
+    inc = os.path.join(ref_dir, "include")
     deps = srcs + [os.path.join(shim, f) for f in os.listdir(shim)] + \
         [os.path.join(inc, f) for f in os.listdir(inc)]
     base = ["g++", "-std=gnu++14", "-fPIC", "-shared", "-Wno-format", "-I", shim, "-I", inc]
@@ -102,5 +112,7 @@ def build_reference(force=False):
 
 
 if __name__ == "__main__":
+    # python oracle/build_oracle.py [-f] [REFERENCE_DIR]
+    rest = [a for a in sys.argv[1:] if a != "-f"]
     print(build_restatement(force="-f" in sys.argv))
-    print(build_reference(force="-f" in sys.argv))
+    print(build_reference(force="-f" in sys.argv, path=rest[0] if rest else None))
