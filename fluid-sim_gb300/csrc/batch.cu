@@ -21,6 +21,7 @@
 #include <algorithm>
 #include <chrono>
 #include <numeric>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -32,6 +33,7 @@ struct fs2d_batch {
     int workers = 0;          // 0: not tuned yet
     int device = 0;
     std::vector<int> status;  // last frame's status per scene
+    std::vector<std::string> status_msg;  // message of a scene's last NOT_CONVERGED frame
     std::vector<double> tuning_ms;
 };
 
@@ -53,21 +55,43 @@ std::vector<std::vector<int>> assign(const fs2d_batch* b, int w) {
     return out;
 }
 
+// The error message of a failing call lives in its worker thread
+// (fs2d_last_error is per thread): each worker keeps the message of its
+// first error, and the calling thread re-raises the first failing worker's
+// code and message.
+struct WorkerStatus {
+    int rc = 0;
+    std::string msg;
+    void fail(int r) {
+        rc = r;
+        msg = fs2d_last_error();
+    }
+};
+int first_error(const std::vector<WorkerStatus>& ws) {
+    for (const WorkerStatus& w : ws)
+        if (w.rc) {
+            set_error("%s", w.msg.c_str());
+            return w.rc;
+        }
+    return 0;
+}
+
 // Runs `nframes` frames of every scene with `w` workers; returns the first
 // hard error (NOT_CONVERGED is recorded per scene, as fs2d_step does).
 int run(fs2d_batch* b, int w, int nframes) {
     auto parts = assign(b, w);
-    std::vector<int> rc(w, 0);
+    std::vector<WorkerStatus> ws(w);
     auto body = [&](int t) {
         cudaSetDevice(b->device);
-        for (int f = 0; f < nframes && rc[t] == 0; f++)
+        for (int f = 0; f < nframes && ws[t].rc == 0; f++)
             for (int k : parts[t]) {
                 int r = fs2d_run_frame(b->sims[k]);
                 b->status[k] = r;
                 if (r && r != FS2D_ERR_NOT_CONVERGED) {
-                    rc[t] = r;
+                    ws[t].fail(r);
                     break;
                 }
+                if (r) b->status_msg[k] = fs2d_last_error();
             }
     };
     if (w == 1) {
@@ -78,9 +102,7 @@ int run(fs2d_batch* b, int w, int nframes) {
         for (int t = 0; t < w; t++) th.emplace_back(body, t);
         for (auto& x : th) x.join();
     }
-    for (int r : rc)
-        if (r) return r;
-    return 0;
+    return first_error(ws);
 }
 
 // Runs fn(k) for every scene with `w` workers (scenes longest-first onto the
@@ -88,13 +110,13 @@ int run(fs2d_batch* b, int w, int nframes) {
 template <typename F>
 int run_each(fs2d_batch* b, int w, F fn) {
     auto parts = assign(b, w);
-    std::vector<int> rc(w, 0);
+    std::vector<WorkerStatus> ws(w);
     auto body = [&](int t) {
         cudaSetDevice(b->device);
         for (int k : parts[t]) {
             int r = fn(k);
             if (r) {
-                rc[t] = r;
+                ws[t].fail(r);
                 return;
             }
         }
@@ -107,9 +129,7 @@ int run_each(fs2d_batch* b, int w, F fn) {
         for (int t = 0; t < w; t++) th.emplace_back(body, t);
         for (auto& x : th) x.join();
     }
-    for (int r : rc)
-        if (r) return r;
-    return 0;
+    return first_error(ws);
 }
 
 int workers_for(const fs2d_batch* b) {
@@ -170,6 +190,7 @@ int fs2d_batch_create(const fs2d_config* cfgs, int n, const fs2d_options* opt, i
         b->cells.push_back((long long)cfgs[k].sizeX * cfgs[k].sizeY);
     }
     b->status.assign(n, 0);
+    b->status_msg.assign(n, std::string());
     b->workers = workers == 0 ? 0 : std::min({workers, n, 64});
     *out = b;
     return FS2D_OK;
@@ -205,8 +226,11 @@ int fs2d_batch_step(fs2d_batch* b, int nframes) {
     if (nframes == 0) return FS2D_OK;
     int rc = run(b, b->workers, nframes);
     if (rc) return rc;
-    for (int s : b->status)
-        if (s) return s;
+    for (size_t k = 0; k < b->status.size(); k++)
+        if (b->status[k]) {
+            set_error("scene %zu: %s", k, b->status_msg[k].c_str());
+            return b->status[k];
+        }
     return FS2D_OK;
 }
 
