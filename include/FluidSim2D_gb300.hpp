@@ -229,6 +229,73 @@ struct LevelSet {
     void free() { phi.free(); }
 };
 
+// PerformanceCounter (include/PerformanceCounter.h:11-35,
+// src/PerformanceCounter.cpp:9-74): the reference's per-stage timer ring with
+// the same public fields and the same averaging.  FluidSim2D::runFrame feeds
+// it each frame's stage times (CUDA events around each stage on the device,
+// in ms) where the reference feeds host clock readings: endStage(ms) stores
+// one stage's time for the current frame, endFrame() averages the last
+// SampleCount frames once that many were sampled (sampleFinished), sums the
+// averages into avgTimePerFrame and appends them to averageStore, and
+// saveToFile writes perf.csv from averageStore in the reference's format.
+struct PerformanceCounter {
+    static constexpr int SampleCount = 30;
+    int currentStage = 0;
+    int currentFrame = 0;
+    Vec<float[SampleCount]> samples = {};
+    Vec<float> average = {};
+    float avgTimePerFrame = 0.0f;
+    bool sampleFinished = false;
+    Vec<float> averageStore = {};
+
+    static PerformanceCounter create(int numStages) {
+        PerformanceCounter counter = {};
+        counter.samples.resize(numStages);
+        counter.average.resize(numStages);
+        return counter;
+    }
+    void endStage(float ms) {
+        samples[currentStage][currentFrame] = ms;
+        currentStage++;
+    }
+    void endFrame() {
+        if (sampleFinished) {
+            for (size_t i = 0; i < (size_t)samples.size; i++) {
+                average[i] = 0.0f;
+                for (int k = 0; k < SampleCount; k++) average[i] += samples[i][k];
+                average[i] /= SampleCount;
+            }
+        }
+        currentStage = 0;
+        if (currentFrame == SampleCount - 1) sampleFinished = true;
+        currentFrame = (currentFrame + 1) % SampleCount;
+        avgTimePerFrame = 0.0f;
+        for (size_t i = 0; i < (size_t)average.size; i++) {
+            averageStore.push(average[i]);
+            avgTimePerFrame += average[i];
+        }
+    }
+    // perf.csv rows from frame SampleCount on: each stage's average, then ','.
+    void saveToFile(const char* filename) {
+        std::FILE* fp = std::fopen(filename, "w+");
+        if (!fp) {
+            std::fprintf(stderr, "fs2d: cannot open %s\n", filename);
+            std::exit(EXIT_FAILURE);
+        }
+        const size_t numStages = (size_t)average.size;
+        for (size_t i = SampleCount; numStages && i < (size_t)averageStore.size / numStages; i++) {
+            for (size_t j = 0; j < numStages; j++) std::fprintf(fp, "%f,", (double)averageStore[numStages * i + j]);
+            std::fputc('\n', fp);
+        }
+        std::fclose(fp);
+    }
+    void free() {
+        samples.free();
+        average.free();
+        averageStore.free();
+    }
+};
+
 enum FluidSimMode { FS_SEMILAGRANGIAN, FS_PICFLIP };
 enum FluidCellType : uint8_t { FS_EMPTY, FS_FLUID, FS_SOLID };
 
@@ -264,6 +331,7 @@ struct FluidSim2D {
     Vec<vec2d> particleVels = {};
 
     LevelSet waterLevelSet;
+    PerformanceCounter perfCounter;
 
     vec2d gravity = {0, -9.81};
     vec2d origGravity = {0, -9.81};
@@ -320,6 +388,7 @@ struct FluidSim2D {
         s.p = Array2D<double>::create(s.sizeX, s.sizeY);
         s.cell = Array2D<FluidCellType>::create(s.sizeX, s.sizeY);
         s.waterLevelSet = LevelSet::create(s.sizeX, s.sizeY, s.dx);
+        s.perfCounter = PerformanceCounter::create(s.numStages);
         s.check(fs2d_create(reinterpret_cast<const fs2d_config*>(&config), opt, &s.device), "create");
         s.syncToHost();
         return s;
@@ -335,6 +404,7 @@ struct FluidSim2D {
         particles.free();
         particleVels.free();
         waterLevelSet.free();
+        perfCounter.free();
         waterVolumeData.free();
         totalEnergyData.free();
         particleTotalEnergyData.free();
@@ -343,6 +413,11 @@ struct FluidSim2D {
     void runFrame() {
         pushParams();
         check(fs2d_run_frame(device), "runFrame");
+        float ms[16];
+        int n = 0;
+        check(fs2d_get_stage_times(device, ms, 16, &n), "get_stage_times");
+        for (int k = 0; k < n && k < numStages; k++) perfCounter.endStage(ms[k]);
+        perfCounter.endFrame();
         afterDeviceWork();
     }
     void update() { runFrame(); }

@@ -196,6 +196,10 @@ def get_reference_lib(variant=""):
         lib = _load(path, "ref_")
         lib.ref_create.argtypes = [C.POINTER(Config), C.c_int, C.c_uint]
         lib.ref_set_gravity.argtypes = [C.c_void_p, C.c_double, C.c_double]
+        lib.ref_save_stats.argtypes = [C.c_void_p]
+        lib.ref_num_stages.argtypes = [C.c_void_p]
+        lib.ref_feed_stats.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int]
         _libs[key] = lib
     return _libs[key]
 
@@ -252,6 +256,27 @@ class RefSim(_SimBase):
     def frame(self):
         self.lib.ref_run_frame(self.h)
         return 0
+
+    def save_stats_of(self, stage_ms, vol, en, pen, directory):
+        """The reference's own saveStats (perf.csv, conservation.csv written
+        into `directory`) after feeding it the given series: `stage_ms`
+        (frames x stages, float32) through PerformanceCounter::endFrame and
+        the three conservation series; returns the two files' bytes."""
+        stage_ms = np.ascontiguousarray(stage_ms, dtype=np.float32)
+        assert stage_ms.shape[1] == self.lib.ref_num_stages(self.h)
+        vol, en, pen = (np.ascontiguousarray(a, dtype=np.float64) for a in (vol, en, pen))
+        fp = C.POINTER(C.c_float)
+        dp = C.POINTER(C.c_double)
+        self.lib.ref_feed_stats(self.h, stage_ms.ctypes.data_as(fp), stage_ms.shape[0], vol.ctypes.data_as(dp),
+                                en.ctypes.data_as(dp), pen.ctypes.data_as(dp), len(vol))
+        cwd = os.getcwd()
+        os.chdir(directory)
+        try:
+            self.lib.ref_save_stats(self.h)   # writes ./perf.csv and ./conservation.csv
+        finally:
+            os.chdir(cwd)
+        return (open(os.path.join(directory, "perf.csv"), "rb").read(),
+                open(os.path.join(directory, "conservation.csv"), "rb").read())
 
 
 def tricubic(data, nx, ny, px, py):

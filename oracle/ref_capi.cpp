@@ -119,4 +119,28 @@ void ref_set_gravity(void* h, double gx, double gy) { ((FluidSim2D*)h)->gravity 
 
 void ref_save_stats(void* h) { ((FluidSim2D*)h)->saveStats(); }
 
+// Feeds given series through the reference's own statistics code: each of
+// `nframes` rows of stage times goes into perfCounter.samples for the
+// current frame followed by PerformanceCounter::endFrame
+// (src/PerformanceCounter.cpp:39-56), and the conservation series are
+// appended to waterVolumeData / totalEnergyData / particleTotalEnergyData,
+// so that ref_save_stats then writes what the reference writes for them.
+void ref_feed_stats(void* h, const float* stage_ms, int nframes, const double* vol, const double* en,
+                    const double* pen, int n) {
+    FluidSim2D* s = (FluidSim2D*)h;
+    PerformanceCounter& pc = s->perfCounter;
+    const int ns = (int)pc.samples.size;
+    for (int f = 0; f < nframes; f++) {
+        for (int k = 0; k < ns; k++) pc.samples[k][pc.currentFrame] = stage_ms[(size_t)f * ns + k];
+        pc.endFrame();
+    }
+    for (int k = 0; k < n; k++) {
+        s->waterVolumeData.push(vol[k]);
+        s->totalEnergyData.push(en[k]);
+        s->particleTotalEnergyData.push(pen[k]);
+    }
+}
+
+int ref_num_stages(void* h) { return (int)((FluidSim2D*)h)->perfCounter.samples.size; }
+
 }  // extern "C"

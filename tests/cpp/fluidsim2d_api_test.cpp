@@ -2,10 +2,12 @@
 // break advanced with runFrame() and, in a second instance, with the stage
 // methods called one by one in runFrame's order (src/FluidSim2D.cpp:94-138),
 // must give bit-identical host mirrors; diagnostics and the host-side MAC
-// helpers must be usable on the mirrored fields.
+// helpers must be usable on the mirrored fields; perfCounter must fill as
+// the reference's does and save the same perf.csv as the library.
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "FluidSim2D_gb300.hpp"
@@ -81,6 +83,53 @@ int main(int argc, char** argv) {
             std::printf("FAIL syncToDevice\n");
             return 1;
         }
+    // the Performance panel of the reference's UI (demo/FluidRenderer2D.cpp:421-430)
+    // reads perfCounter.sampleFinished, average and avgTimePerFrame
+    a.sync = FS2D_SYNC_ON_DEMAND;
+    if (a.perfCounter.sampleFinished) {
+        std::printf("FAIL perfCounter finished after 5 frames\n");
+        return 1;
+    }
+    for (int f = 5; f < 32; f++) a.runFrame();
+    FluidSim2D* sim = &a;
+    float sum = 0.0f;
+    if (sim->perfCounter.sampleFinished) {
+        for (int i = 0; i < (int)sim->perfCounter.average.size; i++) {
+            if (!(sim->perfCounter.average[i] >= 0.0f)) {
+                std::printf("FAIL stage %d: %f ms\n", i, sim->perfCounter.average[i]);
+                return 1;
+            }
+            sum += sim->perfCounter.average[i];
+        }
+    }
+    if (!sim->perfCounter.sampleFinished || (int)sim->perfCounter.average.size != a.numStages ||
+        !(sim->perfCounter.avgTimePerFrame > 0.0f) || sum != sim->perfCounter.avgTimePerFrame) {
+        std::printf("FAIL perfCounter finished %d stages %d avg %f\n", (int)sim->perfCounter.sampleFinished,
+                    (int)sim->perfCounter.average.size, sim->perfCounter.avgTimePerFrame);
+        return 1;
+    }
+    // the mirror's PerformanceCounter and the library's perf.csv writer agree byte for byte
+    if (argc > 2) {
+        const std::string dir = argv[2];
+        const std::string p1 = dir + "/mirror_perf.csv", p2 = dir + "/lib_perf.csv";
+        a.perfCounter.saveToFile(p1.c_str());
+        if (fs2d_save_stats(a.device, p2.c_str(), nullptr) != FS2D_OK) {
+            std::printf("FAIL fs2d_save_stats\n");
+            return 1;
+        }
+        std::FILE* f1 = std::fopen(p1.c_str(), "rb");
+        std::FILE* f2 = std::fopen(p2.c_str(), "rb");
+        std::string b1, b2;
+        for (int ch; f1 && (ch = std::fgetc(f1)) != EOF;) b1 += (char)ch;
+        for (int ch; f2 && (ch = std::fgetc(f2)) != EOF;) b2 += (char)ch;
+        if (f1) std::fclose(f1);
+        if (f2) std::fclose(f2);
+        if (b1.empty() || b1 != b2) {
+            std::printf("FAIL perf.csv of the mirror (%zu bytes) and the library (%zu bytes) differ\n", b1.size(),
+                        b2.size());
+            return 1;
+        }
+    }
     a.free();
     b.free();
     std::printf("OK %s fluid=%d particles=%zu maxVelocity=%.6g\n", mode == FS_PICFLIP ? "pic" : "sl", fluid,

@@ -12,8 +12,12 @@ serial, -ffp-contract=off) on small seeded scenes and stores, per scene:
 * ``stats_f{n}``      waterVolume, totalEnergy, particleTotalEnergy,
                       avgPressure, avgPressureInFluid, maxVelocity.
 
-Usage (needs the reference checkout, so it runs only where that exists):
-    python tests/golden/make_golden.py
+* ``stats_csv.npz``  the reference's saveStats output for seeded series
+                      (see generate_stats_csv).
+
+Usage (needs the reference checkout, named by FS2D_REFERENCE_DIR, so it runs
+only where that exists; "stats" regenerates stats_csv.npz alone):
+    FS2D_REFERENCE_DIR=<checkout> python tests/golden/make_golden.py [stats]
 """
 from __future__ import annotations
 
@@ -87,13 +91,46 @@ def generate(name, scene):
     np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
 
 
+STATS_FRAMES = 45
+STATS_SEED = 4242
+
+
+def generate_stats_csv():
+    """stats_csv.npz: the reference's own saveStats output (perf.csv and
+    conservation.csv, src/FluidSim2D.cpp:738-750 and
+    src/PerformanceCounter.cpp:39-74) for seeded series fed through its
+    PerformanceCounter, for both modes (7 and 8 stages), with the inputs."""
+    import tempfile
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import golden_util
+
+    out = {}
+    for tag, scene in (("sl", scenes.sl_dam_break(16)), ("pic", scenes.pic_dam_break_disk(16))):
+        stages = 7 if tag == "sl" else 8
+        ms, vol, en, pen = golden_util.stats_series(STATS_SEED + stages, STATS_FRAMES, stages)
+        sim = O.RefSim(scene, seed=1)
+        with tempfile.TemporaryDirectory() as d:
+            perf, cons = sim.save_stats_of(ms, vol, en, pen, d)
+        sim.close()
+        out.update({f"{tag}_stage_ms": ms, f"{tag}_vol": vol, f"{tag}_en": en, f"{tag}_pen": pen,
+                    f"{tag}_perf": np.frombuffer(perf, np.uint8), f"{tag}_cons": np.frombuffer(cons, np.uint8)})
+    np.savez_compressed(os.path.join(HERE, "stats_csv.npz"), **out)
+
+
 def main():
     build_oracle.build_reference()
     if O.get_reference_lib() is None:
-        raise SystemExit("reference checkout not available; golden vectors cannot be regenerated")
+        raise SystemExit("reference checkout not available (set FS2D_REFERENCE_DIR); golden vectors cannot be "
+                         "regenerated")
+    if sys.argv[1:] == ["stats"]:
+        generate_stats_csv()
+        print("wrote stats_csv")
+        return
     for name, scene in golden_scenes().items():
         generate(name, scene)
         print("wrote", name)
+    generate_stats_csv()
+    print("wrote stats_csv")
 
 
 if __name__ == "__main__":

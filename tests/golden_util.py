@@ -36,3 +36,18 @@ def stage_order(sc):
 
 def pre_stage(g, k):
     return snapshot(g, "init_" if k == 0 else f"s{k - 1}_post_")
+
+
+def stats_series(seed, frames, stages):
+    """Seeded inputs of the statistics writers: per-frame stage times (ms,
+    float32, frames x stages, a few exact zeros) and the three conservation
+    series, spread over many magnitudes and with values at the rounding
+    boundary of the "%f" format."""
+    rng = np.random.default_rng(seed)
+    ms = rng.lognormal(mean=0.0, sigma=2.0, size=(frames, stages)).astype(np.float32)
+    ms[rng.random(ms.shape) < 0.05] = 0.0
+    vol = rng.uniform(0.05, 2.5, frames)
+    en = rng.normal(0.0, 1.0, frames) * 10.0 ** rng.integers(-3, 7, frames)
+    pen = -np.abs(rng.normal(0.0, 1.0, frames)) * 10.0 ** rng.integers(-3, 7, frames)
+    vol[0], en[1], pen[2] = 0.0000005, -0.0000005, 1234567.0000005
+    return ms, vol, en, pen

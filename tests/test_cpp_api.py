@@ -3,7 +3,8 @@
 CPU: the header compiles with g++ against the reference's usage and links
 against libfs2d.so.  GPU: the program runs a dam break through runFrame and
 through the stage methods one by one (bit-identical host mirrors), in both
-modes.
+modes, then fills the reference's perfCounter (32 frames) and checks its
+perf.csv against the library's.
 """
 import os
 import shutil
@@ -39,7 +40,7 @@ def test_cpp_api_builds(tmp_path):
 @pytest.mark.parametrize("mode", ["sl", "pic"])
 def test_cpp_api_runs(tmp_path, mode):
     exe = build(tmp_path)
-    r = subprocess.run([exe, mode], capture_output=True, text=True, timeout=300)
+    r = subprocess.run([exe, mode, str(tmp_path)], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout + r.stderr
 
 
