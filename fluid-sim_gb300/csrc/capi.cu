@@ -227,6 +227,16 @@ int alloc_particles(Sim* s, size_t cap) {
     return 0;
 }
 
+// Writes the wait controls that follow the device error word (kErrWords).
+int set_wave_controls(Sim* s, long long polls, int kinds, int strip) {
+    int w[kErrWords] = {0};
+    w[1] = kinds;
+    w[2] = strip;
+    memcpy(&w[4], &polls, sizeof(polls));
+    FS2D_CUDA(cudaMemcpyAsync(s->err + 1, w + 1, (kErrWords - 1) * sizeof(int), cudaMemcpyHostToDevice, s->stream));
+    return wait_stream(s, s->stream);
+}
+
 int alloc_all(Sim* s) {
     int rc;
     const size_t N = s->N, NU = s->NU, NV = s->NV;
@@ -290,10 +300,13 @@ int alloc_all(Sim* s) {
     }
     if ((rc = cp_setup_maps(s))) return rc;
     A(stats, 1);
-    A(err, 1);
+    A(err, kErrWords);
+    if ((rc = set_wave_controls(s, kWaveSpinLimit, 0, -1))) return rc;
     if (s->opt.precision == FS2D_PRECISION_MIXED) {
         Mixed32& m = s->m32;
-        const size_t N = (size_t)s->P * s->NY;  // pitched FP32 arrays
+        s->P32 = (s->NX + 127) / 128 * 128;
+        s->NY32 = (s->NY + 31) / 32 * 32;
+        const size_t N = (size_t)s->P32 * s->NY32;  // pitched, padded FP32 arrays
         A(m32.a0, N);
         A(m32.ax, N);
         A(m32.ay, N);
@@ -622,6 +635,7 @@ int fs2d_solve_pressure(fs2d_sim* p, const uint8_t* cell, const double* phi, con
     int rc = fs2d_upload_state(p, &in);
     if (rc) return rc;
     const int status = fs2d_run_stage(p, FS2D_STAGE_APPLY_PROJECTION);
+    H(p)->sim.last_status = status;
     if (status && status != FS2D_ERR_NOT_CONVERGED) return status;
     fs2d_state out{};
     out.p = pressure;
@@ -911,20 +925,20 @@ int fs2d_get_stage_times(fs2d_sim* p, float* ms, int cap, int* n) {
 // stage times, averaged once the ring is full; saveToFile writes one row per
 // frame from frame 30 on, each stage's average followed by ','.  The
 // conservation file follows FluidSim2D::saveStats (src/FluidSim2D.cpp:738-750).
-int fs2d_save_stats(fs2d_sim* p, const char* perf_path, const char* cons_path) {
-    if (!p) return FS2D_ERR_INVALID;
-    Host* h = H(p);
-    Sim* s = &h->sim;
+int fs2d_write_stats(const float* stage_ms, int ns, size_t frames, const double* vol, const double* en,
+                     const double* pen, size_t n, const char* perf_path, const char* cons_path) {
+    if ((perf_path && (ns < 1 || (frames > 0 && !stage_ms))) || (cons_path && n > 0 && (!vol || !en || !pen))) {
+        set_error("fs2d_write_stats: missing series");
+        return FS2D_ERR_INVALID;
+    }
     if (perf_path) {
-        const int ns = num_stages(s);
         const int kSamples = 30;
         std::vector<float> ring((size_t)ns * kSamples, 0.0f), avg(ns, 0.0f);
         std::string buf;
         bool finished = false;
-        size_t frames = h->frame_stage_ms.size() / ns;
         for (size_t f = 0; f < frames; f++) {
             int slot = (int)(f % kSamples);
-            for (int k = 0; k < ns; k++) ring[(size_t)k * kSamples + slot] = h->frame_stage_ms[f * ns + k];
+            for (int k = 0; k < ns; k++) ring[(size_t)k * kSamples + slot] = stage_ms[f * ns + k];
             if (finished) {
                 for (int k = 0; k < ns; k++) {
                     float a = 0.0f;
@@ -956,11 +970,35 @@ int fs2d_save_stats(fs2d_sim* p, const char* perf_path, const char* cons_path) {
             return FS2D_ERR_INVALID;
         }
         fputs("Total Volume, Total Energy, Total Energy (Particle) \n", fp);
-        for (size_t k = 0; k < s->hist_n; k++)
-            fprintf(fp, "%f, %f, %f\n", s->hist[3 * k], s->hist[3 * k + 1], s->hist[3 * k + 2]);
+        for (size_t k = 0; k < n; k++) fprintf(fp, "%f, %f, %f\n", vol[k], en[k], pen[k]);
         fclose(fp);
     }
     return FS2D_OK;
+}
+
+int fs2d_save_stats(fs2d_sim* p, const char* perf_path, const char* cons_path) {
+    if (!p) return FS2D_ERR_INVALID;
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    const int ns = num_stages(s);
+    std::vector<double> vol(s->hist_n), en(s->hist_n), pen(s->hist_n);
+    for (size_t k = 0; k < s->hist_n; k++) {
+        vol[k] = s->hist[3 * k];
+        en[k] = s->hist[3 * k + 1];
+        pen[k] = s->hist[3 * k + 2];
+    }
+    return fs2d_write_stats(h->frame_stage_ms.data(), ns, h->frame_stage_ms.size() / ns, vol.data(), en.data(),
+                            pen.data(), s->hist_n, perf_path, cons_path);
+}
+
+int fs2d_debug_wavefront(fs2d_sim* p, long long polls, int holdKinds, int holdStrip) {
+    if (!p || holdKinds < 0 || holdKinds > 15) {
+        set_error("fs2d_debug_wavefront: invalid arguments");
+        return FS2D_ERR_INVALID;
+    }
+    Sim* s = &H(p)->sim;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    return set_wave_controls(s, polls > 0 ? polls : kWaveSpinLimit, holdKinds, holdKinds ? holdStrip : -1);
 }
 
 int fs2d_set_stream(fs2d_sim* p, void* stream) {

@@ -264,6 +264,9 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
     const int nt = P / kCpCols;
     const int nchunks = P / kCpCH;
     const bool has_next = strip + 1 < nstrips;
+    // this strip hands its top row to the next one (unless the test hook holds it back)
+    const bool publishes = has_next && !wave_held(a.err, kWaveKindCp, strip);
+    const long long spin = wave_spin(a.err);
     const bool below_in_grid = strip > 0;
     const int y0 = SY > 0 ? 32 * strip : NY - 33 - 32 * strip;   // memory row of box row 0
 
@@ -278,11 +281,14 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
         *tiles_done = 0;
         *tiles_freed = 0;
     }
-    if (!below_in_grid) {
-        for (int k = threadIdx.x; k < kCpBndChunks * kCpCH; k += blockDim.x) {
-            bnd_t[k] = -1;
-            bnd_p[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-        }
+    // the row below starts as "no particle" in every strip: the first strip
+    // keeps it (the reference's border), the others overwrite it with the
+    // previous strip's row; a strip whose wait gave up reads -1, never a
+    // stale shared-memory word, so every index it stores stays a particle
+    // index or -1
+    for (int k = threadIdx.x; k < kCpBndChunks * kCpCH; k += blockDim.x) {
+        bnd_t[k] = -1;
+        bnd_p[k] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
 
@@ -291,7 +297,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
         const unsigned long long* gprev = below_in_grid ? a.progress + (strip - 1) : nullptr;
         int hbk = below_in_grid ? 0 : nchunks;
         int tc = 0;
-        const int tend = has_next ? P : 0;
+        const int tend = publishes ? P : 0;
         int ts = 0;
         unsigned long long gavail = 0;
         long long idle = 0;
@@ -360,7 +366,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
             }
             if (moved) {
                 idle = 0;
-            } else if (++idle > 16 * kWaveSpinLimit || *quit || ((idle & 1023) == 0 && *(volatile int*)a.err)) {
+            } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(a.err))) {
                 if (lane == 0) atomicOr(a.err, 1);
                 break;
             }
@@ -383,6 +389,10 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
         const int bc = SX > 0 ? (c & 31) : 31 - (c & 31);
         return tile_base(c >> 5)[r * kCpCols + bc];
     };
+    // Tiles keep being loaded after a failed wait (the loads complete on
+    // their own and are all waited for below): every slot then holds indices
+    // read from t, so whatever this strip computes stays a particle index or
+    // -1, never a stale shared-memory word.
     auto issue = [&](int t) {
         if (lane == 0 && t < nt) {
             unsigned long long* bar = bars + (t % kCpSlots);
@@ -407,7 +417,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
         if (failed) return;
         long long polls = 0;
         while (*flag < need) {
-            if (++polls > 16 * kWaveSpinLimit) {
+            if (++polls > 16 * spin) {
                 failed = true;
                 atomicOr(a.err, 1);
                 *quit = 1;
@@ -500,7 +510,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
             } else {
                 o_t = -1;
             }
-            if (has_next && lane == 31 && cin) {
+            if (publishes && lane == 31 && cin) {
                 top_t[c % kCpTopRing] = o_t;
                 top_p[c % kCpTopRing] = o_p;
                 if (((c + 1) % 8) == 0 || c == P - 1) {
@@ -514,7 +524,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
     const int nsteps = P + 31;
     for (int t = 0; t * kCpCols < nsteps; t++) {
         if (t + 1 < nt) wait_tile(t + 1);
-        if (has_next && t * kCpCols - 31 - *top_done > kCpTopRing / 2)
+        if (publishes && t * kCpCols - 31 - *top_done > kCpTopRing / 2)
             spin_ge(top_done, t * kCpCols - 31 - kCpTopRing / 2);
         __syncwarp();
         if (t == 0 || t >= nt - 1)
@@ -536,6 +546,8 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
     }
     cp_async_wait<0>();
     __syncwarp();
+    // every issued tile was waited for in the loop (wait_tile(t + 1) for each
+    // t + 1 < nt), so no TMA load is in flight when the CTA exits
     if (lane == 0) *tiles_done = nt;
     (void)failed;
 }

@@ -147,11 +147,14 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
     const int nstrips = (NY + kEkRows - 1) / kEkRows;
     const int nt = P / kEkCols;
     const bool has_next = strip + 1 < nstrips;
+    // this strip hands its top row to the next one (unless the test hook holds it back)
+    const bool publishes = has_next && !wave_held(a.err, kWaveKindEik, strip);
+    const long long spin = wave_spin(a.err);
     const bool below_in_grid = strip > 0;
     const bool active = strip < nstrips;                       // the grid is rounded up to whole clusters
     const unsigned crank = cluster_ctarank(), csize = cluster_nctarank();
     const bool prev_local = below_in_grid && crank > 0;        // the previous strip fills this ring
-    const bool next_local = has_next && crank + 1 < csize;     // this strip fills the next strip's ring
+    const bool next_local = publishes && crank + 1 < csize;    // this strip fills the next strip's ring
     const int y0 = SY > 0 ? kEkRows * strip : NY - kEkRows - kEkRows * strip;   // memory row of box row 0
 
     if (threadIdx.x == 0) {
@@ -172,7 +175,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         const unsigned long long* gprev = below_in_grid ? a.progress + (strip - 1) : nullptr;
         int hb = (below_in_grid && !prev_local) ? 0 : P;   // next column of the row below to fetch
         int tc = 0;                                        // top-row columns forwarded
-        const int tend = has_next ? P : 0;
+        const int tend = publishes ? P : 0;
         int rused = 0;                                     // last seen chunk position of the consumer
         const unsigned r_bnd = next_local ? mapa_shared((const void*)bnd, crank + 1) : 0u;
         const unsigned r_used = next_local ? mapa_shared((const void*)bnd_used, crank + 1) : 0u;
@@ -265,7 +268,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
             }
             if (moved) {
                 idle = 0;
-            } else if (++idle > 16 * kWaveSpinLimit || *quit || ((idle & 1023) == 0 && *(volatile int*)a.err)) {
+            } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(a.err))) {
                 if (lane == 0) atomicOr(a.err, 1);
                 break;
             }
@@ -305,7 +308,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
             if (failed) return;
             long long polls = 0;
             while (*flag < need) {
-                if (++polls > 16 * kWaveSpinLimit) {
+                if (++polls > 16 * spin) {
                     failed = true;
                     atomicOr(a.err, 1);
                     *quit = 1;
@@ -340,7 +343,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                         while (!ok && !failed) {
                             const unsigned long long w = bnd[wi];
                             ok = (lane >> 4) ? ek_w1_is(w, cc) : ek_w0_is(w, cc);
-                            if (!ok && ++polls > 16 * kWaveSpinLimit) {
+                            if (!ok && (++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(a.err)))) {
                                 failed = true;
                                 atomicOr(a.err, 1);
                                 *quit = 1;
@@ -384,7 +387,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                 }
                 o_v = out;
                 o_c = chg;
-                if (has_next && lane == 31 && cin) {
+                if (publishes && lane == 31 && cin) {
                     top_p[2 * (c % kEkTopRing)] = ek_w0(c, out);
                     top_p[2 * (c % kEkTopRing) + 1] = ek_w1(c, out, chg);
                 }
@@ -394,7 +397,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         const int nsteps = P + 31;
         for (int t = 0; t * kEkCols < nsteps; t++) {
             if (t < nt) wait_tile(t);
-            if (has_next && t * kEkCols - 31 - *top_done > kEkTopRing / 2)
+            if (publishes && t * kEkCols - 31 - *top_done > kEkTopRing / 2)
                 spin_ge(top_done, t * kEkCols - 31 - kEkTopRing / 2);
             __syncwarp();
             if (t == 0 || t >= nt)

@@ -153,129 +153,16 @@ struct WaveGeom {
     int i_lo, i_hi, j_lo, j_hi;
 };
 
-constexpr int kWavePublish = 8;                 // columns per progress publication
-constexpr long long kWaveSpinLimit = 1ll << 22; // polls before giving up (~0.5 s)
-constexpr int kWavePrefetch = 32;               // columns of look-ahead for the L1 prefetch
-constexpr int kWaveQueue = 4;                   // lane 0: below-row values loaded ahead
-
-__device__ __forceinline__ void prefetch_l1(const void* p) {
-    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+// Controls of the bounded waits (see kErrWords): polls before a wait between
+// strips gives up, and whether the test hook holds back `strip`'s hand-off
+// in sweeps of `kind`.
+__device__ __forceinline__ long long wave_spin(const int* err) {
+    return *reinterpret_cast<const volatile long long*>(err + 4);
 }
-
-// Strip wavefront: block k (32 threads) owns rows 32k .. 32k+31 in sweep
-// order, lane l one row.  At step s lane l visits column c = s - l, so the
-// warp forms a diagonal front; the value of the cell below (previous row in
-// sweep order) arrives by shuffle from lane l-1, the value of the previous
-// column stays in the lane's register.  Lane 0 reads the last row of strip
-// k-1 from L2 after waiting on that strip's progress counter, which lane 31
-// of strip k-1 publishes (release) every kWavePublish columns; it loads
-// those values kWaveQueue columns ahead of use so the L2 round trip stays
-// off the critical path.  Every lane prefetches its own row's operands into
-// L1 kWavePrefetch columns ahead.  The wait is bounded: on timeout bit 0 of
-// *err is set and the strip carries on (results are then invalid, but
-// nothing hangs).
-//
-// Op interface:
-//   typename Op::Carry;                       value handed to the next column / row
-//   Carry op.fetch(int i, int j, bool l2)     value of a cell outside this strip
-//   Carry op.update(int i, int j, Carry prev_x, Carry prev_y)
-//   void op.prefetch(int i, int j)            L1 prefetch of what update(i, j) reads
-//   static Carry Op::shfl_up(Carry c)         __shfl_up_sync by one lane
-template <class Op>
-__global__ void __launch_bounds__(32) wave_kernel(Op op, WaveGeom g, unsigned long long* progress,
-                                                  unsigned long long base, int* err, const int* skip) {
-    typedef typename Op::Carry Carry;
-    if (skip != nullptr && *skip) return;
-    const int lane = threadIdx.x;
-    const int k = blockIdx.x;
-    const int ncols = g.i_hi - g.i_lo + 1;
-    const int nrows = g.j_hi - g.j_lo + 1;
-    const int row = k * 32 + lane;
-    const bool valid = row < nrows;
-    const int j = g.sy > 0 ? g.j_lo + row : g.j_hi - row;
-    Carry out{};
-    const unsigned long long* prev = (k > 0) ? progress + (k - 1) : nullptr;
-    unsigned long long avail = 0;
-    bool gave_up = false;
-    const bool publisher = (lane == 31) && valid && (k * 32 + 32 < nrows);
-    auto col = [&](int c) { return g.sx > 0 ? g.i_lo + c : g.i_hi - c; };
-    // lane 0: below-row value of column cc, waiting for its publication first
-    auto below_of = [&](int cc) -> Carry {
-        if (prev != nullptr && !gave_up) {
-            unsigned long long need = base + (unsigned long long)min(((cc / kWavePublish) + 1) * kWavePublish, ncols);
-            if (avail < need) {
-                long long polls = 0;
-                unsigned long long v;
-                while ((v = ld_acquire(prev)) < need) {
-                    if (++polls > kWaveSpinLimit || *(volatile int*)err) {
-                        atomicOr(err, 1);
-                        gave_up = true;
-                        break;
-                    }
-                    __nanosleep(32);
-                }
-                avail = v;
-            }
-        }
-        return op.fetch(col(cc), j - g.sy, prev != nullptr);
-    };
-    Carry bq[kWaveQueue];
-    if (lane == 0 && valid) {
-#pragma unroll
-        for (int q = 0; q < kWaveQueue; q++) bq[q] = (q < ncols) ? below_of(q) : Carry{};
-    }
-    if (valid) {
-        for (int c = 0; c < min(kWavePrefetch, ncols); c += 8) op.prefetch(col(c), j);
-    }
-    for (int s = 0; s < ncols + 31; ++s) {
-        const int c = s - lane;
-        Carry below = Op::shfl_up(out);
-        if (valid && c >= 0 && c < ncols) {
-            const int i = col(c);
-            if ((c & 7) == 0 && c + kWavePrefetch < ncols) op.prefetch(col(c + kWavePrefetch), j);
-            if (lane == 0) {
-                below = bq[0];
-#pragma unroll
-                for (int q = 0; q < kWaveQueue - 1; q++) bq[q] = bq[q + 1];
-                if (c + kWaveQueue < ncols) bq[kWaveQueue - 1] = below_of(c + kWaveQueue);
-            }
-            Carry left = (c > 0) ? out : op.fetch(i - g.sx, j, false);
-            out = op.update(i, j, left, below);
-            if (publisher && (((c + 1) % kWavePublish) == 0 || c == ncols - 1)) {
-                st_release(progress + k, base + (unsigned long long)(c + 1));
-            }
-        }
-        __syncwarp();
-    }
-}
-
-// Launches a wavefront sweep; blocks are co-resident (cooperative launch) so
-// the waits between strips always make progress.
-template <class Op>
-int launch_wave(Sim* s, const Op& op, WaveGeom g, const int* skip) {
-    int nrows = g.j_hi - g.j_lo + 1;
-    int ncols = g.i_hi - g.i_lo + 1;
-    if (nrows <= 0 || ncols <= 0) return 0;
-    int nstrips = (nrows + 31) / 32;
-    if (nstrips > s->progress_cap) {
-        set_error("wavefront: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
-        return FS2D_ERR_INVALID;
-    }
-    // One strip per SM: the strips of a sweep run concurrently and, on GB300,
-    // strips sharing an SM contend for its small FP64 pipe.  Reserving more
-    // than half of the SM's shared memory keeps every strip on its own SM.
-    const int kReserve = 120 * 1024;
-    static std::atomic<unsigned long long> configured{0};
-    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)wave_kernel<Op>, kReserve)) return rc0;
-    unsigned long long base = wave_begin(s);
-    void* args[] = {(void*)&op, (void*)&g, (void*)&s->progress, (void*)&base, (void*)&s->err, (void*)&skip};
-    s->launches++;
-    long long kt = ktimer_begin(s, Op::kName);
-    int rc = check_cuda(cudaLaunchCooperativeKernel((const void*)wave_kernel<Op>, dim3(nstrips), dim3(32), args,
-                                                    kReserve, s->stream),
-                        Op::kName);
-    ktimer_end(s, kt);
-    return rc;
+// A wait of some sweep already gave up (other waits then give up early).
+__device__ __forceinline__ bool wave_failed(const int* err) { return (*(const volatile int*)err & 1) != 0; }
+__device__ __forceinline__ bool wave_held(const int* err, int kind, int strip) {
+    return (err[1] & kind) != 0 && err[2] == strip;
 }
 
 }  // namespace fs2d

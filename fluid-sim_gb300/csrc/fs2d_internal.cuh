@@ -25,6 +25,22 @@ constexpr uint8_t kFluid = FS2D_FLUID;
 constexpr uint8_t kSolid = FS2D_SOLID;
 constexpr uint32_t kUnknown = 0xFFFFFFFFu;   // extrapolation mask of an unknown face
 
+// The device error word and the controls of the wavefront waits share one
+// allocation of kErrWords ints (Sim::err):
+//   err[0]      error bits: 1 a wait gave up (timeout), 2 a non-finite
+//               particle position, 4 a particle outside the grid;
+//   err[1]      kinds of sweep (kWaveKind*) in which strip err[2] withholds
+//               its hand-off to the next strip (0: none).  A test hook
+//               (fs2d_debug_wavefront): the next strip's wait then runs out
+//               and the sweep reports a timeout without any fault;
+//   err[4..5]   polls before a wait between strips gives up (a long long;
+//               kWaveSpinLimit unless a test shortened it).
+// Waits for a sweep's own TMA copies always use kWaveSpinLimit: those
+// copies complete whatever the other strips do.
+constexpr int kErrWords = 8;
+constexpr long long kWaveSpinLimit = 1ll << 22;   // polls before a wait gives up (~0.5 s), by default
+constexpr int kWaveKindCp = 1, kWaveKindEik = 2, kWaveKindWave2 = 4, kWaveKindMic32 = 8;
+
 // Scalars of one pressure solve, kept in device memory so that the PCG loop
 // runs without host round trips.  Finalised by the last block of each
 // reduction kernel.
@@ -54,8 +70,9 @@ struct FrameStats {
 };
 
 // FP32 arrays of the mixed-precision inner solver (projection_mixed.cu),
-// each P x NY with a row pitch of P = NX rounded up to 32 floats (tiles of
-// the TMA wavefront start on 128-byte boundaries); padding holds zeros.
+// each P32 x NY32: the row pitch P32 is NX rounded up to 128 floats and the
+// rows NY rounded up to 32, so that the FP32 MIC(0) sweeps work on whole
+// strips of 128 columns and tiles of 32 rows; padding holds zeros.
 struct Mixed32 {
     float *a0 = nullptr, *ax = nullptr, *ay = nullptr;             // matrix
     float *pc = nullptr, *fa = nullptr, *fb = nullptr, *fc = nullptr, *fd = nullptr;  // MIC(0), folded
@@ -64,8 +81,8 @@ struct Mixed32 {
 };
 // TMA descriptors of the two FP32 MIC(0) sweeps (see mic32_tma.cuh).
 struct Mic32MapsHost {
-    alignas(64) unsigned char fwd[4 * 128 + 128];
-    alignas(64) unsigned char bwd[4 * 128 + 128];
+    alignas(64) unsigned char fwd[4 * 128];
+    alignas(64) unsigned char bwd[4 * 128];
 };
 
 // TMA descriptors of the closest-point sweeps (see cp_sweep.cuh).
@@ -140,6 +157,7 @@ struct Sim {
     PcgScalars* pcg_host = nullptr;                  // pinned mirror for polling
     Mixed32 m32;                                     // MIXED precision only
     int P = 0;                                       // row pitch of the pitched arrays (NX rounded up to 32)
+    int P32 = 0, NY32 = 0;                           // pitch and rows of the FP32 solver arrays (Mixed32)
     Mic32MapsHost* m32maps = nullptr;
     int m32_cluster = 0;                             // cluster size of the FP32 MIC(0) sweeps (0: not chosen)
     PcgScalars* pcg32 = nullptr;                     // inner FP32 solve scalars
@@ -160,7 +178,7 @@ struct Sim {
     // frame statistics and errors
     FrameStats* stats = nullptr;
     FrameStats* stats_host = nullptr;
-    int* err = nullptr;            // device error word: bit 0 timeout, bit 1 non-finite
+    int* err = nullptr;            // device error word and wait controls (kErrWords ints)
     int* err_host = nullptr;
 
     // history of per-frame conservation values (host)

@@ -153,13 +153,13 @@ __global__ void k_cp_check(const int* __restrict__ t, const float4* __restrict__
 
 // phi = d(t) of every cell (HUGE_VAL without a particle), as the reference
 // stores it with t.
-__global__ void k_cp_phi(const int* __restrict__ t, const double2* __restrict__ pos, double* phi, int NX, int NY,
-                         int P, double dx, double dr) {
+__global__ void k_cp_phi(const int* __restrict__ t, const double2* __restrict__ pos, size_t np, double* phi, int NX,
+                         int NY, int P, double dx, double dr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= NX) return;
     const int e = t[(size_t)j * P + i];
-    phi[(size_t)j * NX + i] = e < 0 ? HUGE_VAL : corner_dist(pos[e], i, j, dx, dr);
+    phi[(size_t)j * NX + i] = (e < 0 || (size_t)e >= np) ? HUGE_VAL : corner_dist(pos[e], i, j, dx, dr);
 }
 
 // ---- redistance ----
@@ -449,7 +449,7 @@ int levelset_create(Sim* s) {
             if (rc) return rc;
         }
     }
-    FS2D_LAUNCH(s, k_cp_phi, g2, 128, 0, s->t, s->pos, s->phi, NX, NY, P, s->dx, s->dr);
+    FS2D_LAUNCH(s, k_cp_phi, g2, 128, 0, s->t, s->pos, s->np, s->phi, NX, NY, P, s->dx, s->dr);
 
     // redistance on the pitched copy phi_p
     FS2D_LAUNCH(s, k_surface, g2, 128, 0, s->phi, s->phi_p, NX, NY, P);

@@ -8,7 +8,7 @@
 // The matrix (ghost-fluid diagonal), right-hand side, MIC(0) factor and the
 // two triangular solves per iteration round exactly like the reference's
 // serial loops: the factor and the solves are Gauss-Seidel-ordered
-// recurrences and run as strip wavefronts (wave_kernel) that keep the
+// recurrences and run as strip wavefronts (wave2.cuh) that keep the
 // reference's dependency order.  Dot products and norms are tree reductions
 // (a different summation order than the reference's serial loop), so the
 // iterates agree with the reference to rounding, not bit for bit.

@@ -334,8 +334,8 @@ __global__ void k_update64(double* p, const float* __restrict__ e, const PcgScal
 
 }  // namespace
 
-int mic32_make_map(CUtensorMap* map, float* base, int P, int NY, int box_rows) {
-    return make_tensor_map_2d(map, base, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NY, P, kM32Cols, box_rows);
+int mic32_make_map(CUtensorMap* map, float* base, int P, int NR) {
+    return make_tensor_map_2d(map, base, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, P, NR, P, kM32Cols, kM32Rows);
 }
 
 static_assert(sizeof(Mic32Maps) <= sizeof(Mic32MapsHost::fwd), "tensor map storage");
@@ -344,16 +344,13 @@ static_assert(sizeof(Mic32Maps) <= sizeof(Mic32MapsHost::fwd), "tensor map stora
 int mixed_setup_maps(Sim* s) {
     Mixed32& m = s->m32;
     Mic32Maps f{}, b{};
-    const int tail = s->NY % kM32Rows;
     int rc = 0;
     float* fin[3] = {m.rp, m.fa, m.fb};
     float* bin[3] = {m.q, m.fc, m.fd};
-    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&f.in[a], fin[a], s->P, s->NY, kM32Rows);
-    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&b.in[a], bin[a], s->P, s->NY, kM32Rows);
-    if (!rc) rc = mic32_make_map(&f.out, m.q, s->P, s->NY, kM32Rows);
-    if (!rc) rc = mic32_make_map(&b.out, m.z, s->P, s->NY, kM32Rows);
-    if (!rc) rc = mic32_make_map(&f.out_tail, m.q, s->P, s->NY, tail > 0 ? tail : kM32Rows);
-    if (!rc) rc = mic32_make_map(&b.out_tail, m.z, s->P, s->NY, tail > 0 ? tail : kM32Rows);
+    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&f.in[a], fin[a], s->P32, s->NY32);
+    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&b.in[a], bin[a], s->P32, s->NY32);
+    if (!rc) rc = mic32_make_map(&f.out, m.q, s->P32, s->NY32);
+    if (!rc) rc = mic32_make_map(&b.out, m.z, s->P32, s->NY32);
     if (rc) return rc;
     memcpy(s->m32maps->fwd, &f, sizeof(f));
     memcpy(s->m32maps->bwd, &b, sizeof(b));
@@ -367,7 +364,7 @@ int projection_mixed(Sim* s, int* status) { return projection_mixed_rhs(s, nullp
 // b == nullptr: the physical right-hand side; otherwise A p = b for a device
 // array b on the fluid cells.
 int projection_mixed_rhs(Sim* s, const double* b, int* status) {
-    const int NX = s->NX, NY = s->NY, P = s->P;
+    const int NX = s->NX, NY = s->NY, P = s->P32;   // FP32 arrays: pitch P32
     const size_t N = s->N;
     const unsigned nb = blocks_for(N, kT);
     Mixed32& m = s->m32;

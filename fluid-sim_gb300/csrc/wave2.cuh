@@ -20,9 +20,10 @@
 //     warp 0 of the next CTA copies that row into shared memory in chunks of
 //     CH columns, two chunks ahead of use, through registers and L2-only
 //     loads (ld.global.cg), so the L2 round trip stays off the critical path.
-// Every wait is bounded (kWaveSpinLimit polls): on timeout bit 0 of *err is
-// set and the kernel carries on without the value (the result is then
-// invalid, nothing hangs).  CTAs are co-resident (cooperative launch).
+// Every wait is bounded (wave_spin(err) polls, times a fixed factor): on
+// timeout bit 0 of *err is set and the kernel carries on without the value
+// (the result is then invalid, nothing hangs).  CTAs are co-resident
+// (cooperative launch).
 //
 // Op interface:
 //   typedef T;  static constexpr int NA;   operand element type and count
@@ -71,10 +72,10 @@ __host__ __device__ constexpr size_t wave2_smem_bytes() {
 
 // Busy-wait on a shared-memory counter (no sleep: a consumer that slept
 // past the moment its data arrived would fall further behind at every chunk).
-__device__ __forceinline__ bool spin_until_smem(volatile int* flag, int need, int* err) {
+__device__ __forceinline__ bool spin_until_smem(volatile int* flag, int need, int* err, long long spin) {
     long long polls = 0;
     while (*flag < need) {
-        if (++polls > 64 * kWaveSpinLimit || ((polls & 1023) == 0 && *(volatile int*)err)) {
+        if (++polls > 64 * spin || ((polls & 1023) == 0 && wave_failed(err))) {
             atomicOr(err, 1);
             return false;
         }
@@ -126,7 +127,11 @@ __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsign
     const unsigned long long* gprev = from_global ? progress + (blockIdx.x - 1) : nullptr;
     const T* edge_in = from_edge ? edges + (size_t)(w - 1) * kW2EdgeRing : nullptr;
     T* edge_out = (!last_in_cta) ? edges + (size_t)w * kW2EdgeRing : nullptr;
-    const bool publish_global = last_in_cta && (strip + 1 < nstrips);
+    // the CTA's last warp hands its row to the next CTA (unless the test hook
+    // holds this CTA's hand-off back)
+    const bool publish_global =
+        last_in_cta && (strip + 1 < nstrips) && !wave_held(err, kWaveKindWave2, (int)blockIdx.x);
+    const long long spin = wave_spin(err);
 
     // ---- staging: tile t (32 columns) -> ring columns (t%3)*32 .. +31 ----
     auto issue_tile = [&](int t) {
@@ -159,7 +164,7 @@ __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsign
             long long polls = 0;
             unsigned long long v;
             while ((v = ld_acquire(gprev)) < need) {
-                if (++polls > 16 * kWaveSpinLimit || ((polls & 255) == 0 && *(volatile int*)err)) {
+                if (++polls > 16 * spin || ((polls & 255) == 0 && wave_failed(err))) {
                     atomicOr(err, 1);
                     v = need;
                     break;
@@ -218,7 +223,7 @@ __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsign
             // two chunks of slack: in steady state the consumer never catches up
             const int need = min(s0 + 2 * CH, ncols);
             if (edge_avail < need) {
-                if (lane == 0) spin_until_smem(eprog + (w - 1), need, err);
+                if (lane == 0) spin_until_smem(eprog + (w - 1), need, err, spin);
                 __syncwarp();
                 __threadfence_block();
                 edge_avail = need;
@@ -265,7 +270,7 @@ __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsign
                         if (c + 1 - eread[w + 1] > kW2EdgeRing - 64) {
                             long long polls = 0;
                             while (c + 1 - eread[w + 1] > kW2EdgeRing - 64) {
-                                if (++polls > kWaveSpinLimit || *(volatile int*)err) {
+                                if (++polls > spin || wave_failed(err)) {
                                     atomicOr(err, 1);
                                     break;
                                 }

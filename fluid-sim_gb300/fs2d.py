@@ -106,7 +106,10 @@ SIGNATURES = {
     "fs2d_batch_destroy": (C.c_int, [C.c_void_p]),
     "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
     "fs2d_save_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
+    "fs2d_write_stats": (C.c_int, [C.c_void_p, C.c_int, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
+                                   C.c_char_p, C.c_char_p]),
     "fs2d_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "fs2d_debug_wavefront": (C.c_int, [C.c_void_p, C.c_longlong, C.c_int, C.c_int]),
     "fs2d_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
     "fs2d_last_error": (C.c_char_p, []),
     "fs2d_set_kernel_timing": (C.c_int, [C.c_void_p, C.c_char_p]),

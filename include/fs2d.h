@@ -143,7 +143,7 @@ typedef struct fs2d_stats {
     int pcgIterations;           /* iterations of the last pressure solve (sum over refinement sweeps) */
     int irOuterIterations;       /* MIXED: refinement sweeps of the last solve; FP64: 0 */
     double pcgRelResidual;       /* ||r||inf / ||b||inf at exit of the last solve (FP64 residual) */
-    int lastStatus;              /* status of the last frame */
+    int lastStatus;              /* status of the last frame or standalone pressure solve */
 } fs2d_stats;
 
 typedef struct fs2d_sim fs2d_sim;
@@ -325,6 +325,17 @@ int fs2d_get_stage_times(fs2d_sim* sim, float* ms, int cap, int* n);
  * in the reference's formats.  Either path may be NULL to skip that file. */
 int fs2d_save_stats(fs2d_sim* sim, const char* perfPath, const char* conservationPath);
 
+/* The formatting of fs2d_save_stats applied to caller-supplied series, on
+ * the host only (no device work; usable without a GPU): `stageMs` holds
+ * `frames` rows of `numStages` stage times (ms), fed through the
+ * reference's 30-frame PerformanceCounter averaging
+ * (src/PerformanceCounter.cpp:39-56) into perfPath; `volume`, `energy`,
+ * `particleEnergy` hold `n` frames of the conservation series
+ * (src/FluidSim2D.cpp:709-731), written to conservationPath.  Either path
+ * may be NULL. */
+int fs2d_write_stats(const float* stageMs, int numStages, size_t frames, const double* volume, const double* energy,
+                     const double* particleEnergy, size_t n, const char* perfPath, const char* conservationPath);
+
 /* Headless render data: what the reference's renderer gathers each frame
  * (FluidRenderer2D::updateBuffers, demo/FluidRenderer2D.cpp:435-486),
  * computed on the device into caller-owned DEVICE buffers (float pairs).
@@ -347,6 +358,22 @@ typedef struct fs2d_render {
     float* phiValues;       /* sizeX*sizeY values sigmoid(100 phi) */
 } fs2d_render;
 int fs2d_render_export(fs2d_sim* sim, fs2d_render* r);
+
+/* Test hook of the failure path of the wavefront sweeps (no reference
+ * counterpart).  Every wait of a sweep on its neighbour strip is bounded: it
+ * gives up after `polls` polls (<= 0: the default, about half a second),
+ * the kernel then finishes without the value and the call returns
+ * FS2D_ERR_TIMEOUT.  With holdKinds != 0, strip `holdStrip` of every sweep
+ * of those kinds withholds its hand-off to the next strip, so that strip's
+ * wait runs out (kinds: 1 closest-point sweeps, 2 Eikonal sweeps, 4 FP64
+ * MIC(0) factor and solves, counted in blocks of their launch, 8 FP32
+ * MIC(0) solves); 0 turns the hold off.  Results of a frame that timed out
+ * are invalid; the handle stays usable. */
+#define FS2D_WAVE_CLOSEST_POINT 1
+#define FS2D_WAVE_EIKONAL       2
+#define FS2D_WAVE_MIC_FP64      4
+#define FS2D_WAVE_MIC_FP32      8
+int fs2d_debug_wavefront(fs2d_sim* sim, long long polls, int holdKinds, int holdStrip);
 
 /* Use `stream` (a cudaStream_t) for all subsequent work of this handle;
  * NULL restores the handle's own stream. */

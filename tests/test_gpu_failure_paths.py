@@ -1,8 +1,20 @@
-"""Failure paths that the reference only logs, made on the host (no GPU
-fault): a pressure solve capped below convergence returns
-FS2D_ERR_NOT_CONVERGED while the frame still completes (the reference logs
-"PCG did not converge" and continues, src/FluidSim2D.cpp:464-466), the status
-is reported by the statistics, and the next frames run normally."""
+"""Failure paths, made on the host or by a flag that nothing sets (no GPU
+fault, no trap, no hang):
+
+* a pressure solve capped below convergence returns FS2D_ERR_NOT_CONVERGED
+  while the frame still completes (the reference logs "PCG did not converge"
+  and continues, src/FluidSim2D.cpp:464-466), the status is reported by the
+  statistics, and the next frames run normally;
+* a wavefront sweep whose neighbour strip never hands its boundary over
+  (the test hook fs2d_debug_wavefront holds one strip's hand-off back, with a
+  short poll limit) gives up, the frame returns FS2D_ERR_TIMEOUT, and the
+  handle stays usable: the next frame from the same state is bit-identical
+  to a handle that never timed out;
+* a NaN particle velocity makes the frame return FS2D_ERR_NONFINITE (the
+  reference exits on a NaN position, src/FluidSim2D.cpp:598-601).
+"""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -11,6 +23,9 @@ scenes = pytest.importorskip("scenes")
 pytestmark = pytest.mark.gpu
 
 NOT_CONVERGED = 4
+NONFINITE = 5
+TIMEOUT = 6
+KINDS = {"closest_point": 1, "eikonal": 2, "mic_fp64": 4, "mic_fp32": 8}
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -34,6 +49,63 @@ def test_standalone_solve_reports_not_converged():
     sc, cell, phi, u, v = scenes.pressure_disks(96, 96, seed=9)
     sim = fs2d.FluidSim2D(sc, seed=1, precision="fp64", pcg_tol=1e-12, pcg_max_iters=2)
     p, st = sim.solve_pressure(cell, phi, u, v)
-    assert st["lastStatus"] == NOT_CONVERGED or st["pcgIterations"] == 2
+    assert st["lastStatus"] == NOT_CONVERGED
+    assert st["pcgIterations"] == 2
     assert st["pcgRelResidual"] > 1e-12 and np.isfinite(p).all()
+    sim.close()
+
+
+def _same(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint8), np.ascontiguousarray(b).view(np.uint8))
+
+
+@pytest.mark.parametrize("kind", list(KINDS))
+def test_wavefront_wait_runs_out_and_the_handle_recovers(kind):
+    """256 x 256 (at least two strips in every sweep), strip 0 of one kind of
+    sweep holds its hand-off back for one frame, 4096-poll limit."""
+    lib = fs2d.load()
+    prec = "mixed" if kind == "mic_fp32" else "fp64"
+    sc = scenes.pic_dam_break_disk(256)
+    opts = dict(precision=prec, pcg_tol=1e-6, pcg_max_iters=20, ir_max_outer=2)
+    a = fs2d.FluidSim2D(sc, seed=5, **opts)
+    b = fs2d.FluidSim2D(sc, seed=5, **opts)
+    assert a.runFrame() in (0, NOT_CONVERGED) and b.runFrame() in (0, NOT_CONVERGED)
+    saved = a.get_state()
+    assert lib.fs2d_debug_wavefront(a.h, C.c_longlong(1 << 12), KINDS[kind], 0) == 0
+    rc = lib.fs2d_run_frame(a.h)
+    assert rc == TIMEOUT, (kind, rc, lib.fs2d_last_error())
+    assert b"timed out" in lib.fs2d_last_error()
+    assert a.stats()["lastStatus"] == TIMEOUT
+    # hold off, default limit; the same frame again from the saved state
+    assert lib.fs2d_debug_wavefront(a.h, C.c_longlong(0), 0, 0) == 0
+    a.set_state(saved)
+    assert a.runFrame() in (0, NOT_CONVERGED)
+    assert b.runFrame() in (0, NOT_CONVERGED)
+    sa, sb = a.get_state(), b.get_state()
+    for k in sa:
+        assert _same(sa[k], sb[k]), (kind, k)
+    a.close()
+    b.close()
+
+
+def test_debug_wavefront_rejects_bad_arguments():
+    lib = fs2d.load()
+    sim = fs2d.FluidSim2D(scenes.pic_dam_break_disk(32), seed=1)
+    assert lib.fs2d_debug_wavefront(sim.h, C.c_longlong(0), 16, 0) == 1
+    assert lib.fs2d_debug_wavefront(None, C.c_longlong(0), 0, 0) == 1
+    sim.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nan_particle_velocity_reports_nonfinite(precision):
+    sc = scenes.pic_dam_break_disk(64)
+    sim = fs2d.FluidSim2D(sc, seed=4, precision=precision, pcg_tol=1e-6, pcg_max_iters=20, ir_max_outer=2)
+    assert sim.runFrame() in (0, NOT_CONVERGED)
+    st = sim.get_state(["particles", "particleVels"])
+    vel = st["particleVels"].copy()
+    vel[2 * (len(vel) // 4)] = np.nan
+    sim.set_state({"particles": st["particles"], "particleVels": vel})
+    rc = fs2d.load().fs2d_run_frame(sim.h)
+    assert rc == NONFINITE, (rc, fs2d.load().fs2d_last_error())
+    assert b"non-finite" in fs2d.load().fs2d_last_error()
     sim.close()
