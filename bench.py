@@ -23,6 +23,9 @@ Besides the headline keys the line carries:
                   byte count) against the measured HBM copy peak;
   step_roofline   the compulsory bytes of every stage of a step / step time;
   fp64_path       the all-FP64 GPU step on the same workload;
+  error_vs_oracle one projection of the workload by the mixed and FP64
+                  device paths at the bench tolerance: time, and error of
+                  p, u, v against the FP64 oracle solved to 1e-12;
   sl_path         the semi-Lagrangian dam break at the same size;
   pressure_solve  the standalone 2048^2 solve to 1e-10, FP64 vs mixed;
   adjoint         the differentiable 128^2 closed-box rollout (64 steps):
@@ -94,6 +97,8 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
+    ap.add_argument("--no-oracle-error", action="store_true",
+                    help="skip the accuracy comparison against the FP64 oracle (error_vs_oracle)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -244,6 +249,65 @@ def reference_arm(args):
 # ---------------------------------------------------------------- GPU arm
 def state_bytes(st):
     return sum(a.nbytes for a in st.values())
+
+
+def error_vs_oracle(args, sc, st, stream, local):
+    """Accuracy of the two device projections on one system of the headline
+    workload.  From the state `st` (a frame boundary of the headline run) the
+    oracle (the FP64 C restatement, OpenMP build) advances the stages before
+    applyProjection, which gives the pre-projection state S; the oracle then
+    solves S to a relative residual of 1e-12 (the FP64 oracle run) and
+    applies updateVelocity.  The mixed and the all-FP64 device paths solve S
+    at the bench's tolerance (CUDA events around the projection stage, after
+    one untimed solve of the same state) and apply updateVelocity; the line
+    reports their time and the max-norm relative error of p, u and v against
+    the oracle's."""
+    import numpy as np
+    import torch
+    import fs2d
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_py
+    t0 = time.perf_counter()
+    orc = oracle_py.OracleSim(sc, seed=SEED, omp=True, sl_inplace=0, pcg_tol=1e-12, pcg_max_iters=4000)
+    orc.set_state(st)
+    for stage in ("createWaterLevelSet", "transferVelocityToGrid", "applyGravity", "createSolidLevelSet"):
+        orc.stage(stage)
+    pre = orc.get_state()
+    orc.stage("applyProjection")
+    info = orc.solver_info()
+    orc.stage("updateVelocity")
+    ref = orc.get_state()
+    orc.close()
+    out = {"state": "frame boundary of the headline run, advanced to applyProjection by the oracle",
+           "oracle": {"pcg_tol": 1e-12, "pcg_iterations": info["iterations"], "rel_residual": info["rel_residual"],
+                      "wall_s": round(time.perf_counter() - t0, 1)},
+           "error": "max |x - x_oracle| / max |x_oracle| for x = p, u, v after applyProjection + updateVelocity"}
+
+    def rel(a, b):
+        return float(np.abs(a - b).max() / (np.abs(b).max() + 1e-300))
+
+    for prec in ("mixed", "fp64"):
+        g = fs2d.FluidSim2D(sc, seed=SEED, precision=prec, pcg_tol=args.tol, pcg_max_iters=200, device=local)
+        g.set_stream(stream.cuda_stream)
+        g.set_state(pre)
+        g.stage("applyProjection")
+        g.set_state(pre)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        g.stage("applyProjection")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        stt = g.stats()
+        g.stage("updateVelocity")
+        got = g.get_state(["p", "u", "v"])
+        out[prec] = {"pcg_tol": args.tol, "ms_to_tol": round(e0.elapsed_time(e1), 3),
+                     "pcg_iterations": stt["pcgIterations"], "refinement_sweeps": stt["irOuterIterations"],
+                     "rel_residual": stt["pcgRelResidual"], "p_rel_err": rel(got["p"], ref["p"]),
+                     "u_rel_err": rel(got["u"], ref["u"]), "v_rel_err": rel(got["v"], ref["v"])}
+        g.close()
+    out["fp64_over_mixed_time"] = out["fp64"]["ms_to_tol"] / out["mixed"]["ms_to_tol"]
+    return out
 
 
 def main():
@@ -404,6 +468,11 @@ def main():
         e2e = {"value": cells * args.e2e_steps * world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": args.e2e_steps,
                "path": "fs2d_upload_state + fs2d_run_frame + fs2d_download_state, full state, pinned host buffers"}
+
+    # ---- accuracy of the mixed and FP64 projections against the FP64 oracle ----
+    oracle_err = None
+    if rank == 0 and not args.no_oracle_error:
+        oracle_err = error_vs_oracle(args, sc, sim.get_state(), stream, local)
 
     # ---- the all-FP64 GPU path on the same workload (fewer steps) ----
     fp64_path = None
@@ -641,6 +710,7 @@ def main():
         "config": config_dict(args, n_particles, {"pcg_iterations_per_step": iters}),
         "stage_ms_last_step": stage_ms,
         "fp64_path": fp64_path,
+        "error_vs_oracle": oracle_err,
         "sl_path": sl_path,
         "pressure_solve": pressure,
         "adjoint": adjoint,
