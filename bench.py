@@ -617,7 +617,7 @@ def main():
         bt.step(max(args.warmup, 3))                 # the first frames choose the worker count
         warm_s = time.perf_counter() - t0
         torch.cuda.synchronize()
-        l0 = sum(bt.scene(k).launch_count() for k in range(len(bscs)))
+        l0 = bt.launch_count()
         t0 = time.perf_counter()
         bt.step(args.batch_steps)
         torch.cuda.synchronize()
@@ -626,7 +626,7 @@ def main():
             t = torch.tensor([conc_s], device="cuda", dtype=torch.float64)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
             conc_s = float(t.item())
-        l1 = sum(bt.scene(k).launch_count() for k in range(len(bscs)))
+        l1 = bt.launch_count()
         workers = bt.workers
         bt.workers = 1
         t0 = time.perf_counter()

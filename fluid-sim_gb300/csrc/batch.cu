@@ -18,6 +18,7 @@
 // timed on one frame each and the fastest is kept.  Those frames are real
 // frames: a scene's results do not depend on the worker count, as every
 // scene runs the same kernels on its own stream.
+#include <string.h>
 #include <algorithm>
 #include <chrono>
 #include <numeric>
@@ -35,6 +36,16 @@ struct fs2d_batch {
     std::vector<int> status;  // last frame's status per scene
     std::vector<std::string> status_msg;  // message of a scene's last NOT_CONVERGED frame
     std::vector<double> tuning_ms;
+    // mixed precision: every scene's pressure solve in one pack (one launch
+    // per kernel of the inner solve for all scenes) on the batch's stream
+    fs2d::Pack* pack = nullptr;
+    fs2d_options opt{};
+    cudaStream_t stream = nullptr;
+    std::vector<cudaEvent_t> ready;       // per scene: its solve's setup is queued
+    cudaEvent_t solved = nullptr;
+    int* err = nullptr;                   // error word and wait controls of the pack's sweeps
+    unsigned long long launches = 0;      // kernels of the pack solves
+    double sweep_us = 0;                  // the tuned persistent sweep's time (pack_tune)
 };
 
 namespace fs2d {
@@ -103,6 +114,80 @@ int run(fs2d_batch* b, int w, int nframes) {
         for (auto& x : th) x.join();
     }
     return first_error(ws);
+}
+
+// Runs fn(k) on the scenes of each worker, `w` workers in parallel; returns
+// the first error (with its message on the calling thread).
+template <typename F>
+int on_workers(const std::vector<std::vector<int>>& parts, int device, F fn) {
+    const int w = (int)parts.size();
+    std::vector<WorkerStatus> ws(w);
+    auto body = [&](int t) {
+        cudaSetDevice(device);
+        for (int k : parts[t]) {
+            int r = fn(k);
+            if (r) {
+                ws[t].fail(r);
+                return;
+            }
+        }
+    };
+    if (w == 1) {
+        body(0);
+    } else {
+        std::vector<std::thread> th;
+        th.reserve(w);
+        for (int t = 0; t < w; t++) th.emplace_back(body, t);
+        for (auto& x : th) x.join();
+    }
+    return first_error(ws);
+}
+
+// Frames of a mixed-precision batch: the workers queue every scene's stages
+// up to its pressure solve's setup; one pack solve then solves all scenes
+// together on the batch's stream (one launch per kernel of the inner solve
+// for every scene); the workers queue the remaining stages and finish each
+// scene's frame.  A scene computes exactly what it computes alone.
+int run_packed(fs2d_batch* b, int w, int nframes) {
+    auto parts = assign(b, w);
+    const int n = (int)b->sims.size();
+    std::vector<int> st(n, 0);
+    for (int f = 0; f < nframes; f++) {
+        int rc = on_workers(parts, b->device, [&](int k) {
+            st[k] = 0;
+            fs2d_sim* p = b->sims[k];
+            int r = frame_stages(p, 0, frame_solve_stage(p) + 1, &st[k], 1);
+            if (!r) r = check_cuda(cudaEventRecord(b->ready[k], sim_of(p)->stream), "cudaEventRecord");
+            return r;
+        });
+        if (rc) return rc;
+        for (int k = 0; k < n; k++) FS2D_CUDA(cudaStreamWaitEvent(b->stream, b->ready[k], 0));
+        rc = pack_solve(b->pack, b->opt, b->stream, &b->launches, b->err, b->device, nullptr);
+        if (rc) return rc;
+        int perr = 0;
+        FS2D_CUDA(cudaMemcpyAsync(&perr, b->err, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+        FS2D_CUDA(cudaStreamSynchronize(b->stream));
+        if (perr) {
+            FS2D_CUDA(cudaMemset(b->err, 0, sizeof(int)));
+            set_error("a wavefront sweep of the batch's pressure solve timed out");
+            return FS2D_ERR_TIMEOUT;
+        }
+        FS2D_CUDA(cudaEventRecord(b->solved, b->stream));
+        rc = on_workers(parts, b->device, [&](int k) {
+            fs2d_sim* p = b->sims[k];
+            int r = check_cuda(cudaStreamWaitEvent(sim_of(p)->stream, b->solved, 0), "cudaStreamWaitEvent");
+            if (!r) r = frame_stages(p, frame_solve_stage(p), -1, &st[k], 2);
+            r = frame_close(p, r, st[k]);
+            b->status[k] = r;
+            if (r == FS2D_ERR_NOT_CONVERGED) {
+                b->status_msg[k] = fs2d_last_error();
+                r = 0;
+            }
+            return r;
+        });
+        if (rc) return rc;
+    }
+    return 0;
 }
 
 // Runs fn(k) for every scene with `w` workers (scenes longest-first onto the
@@ -192,6 +277,30 @@ int fs2d_batch_create(const fs2d_config* cfgs, int n, const fs2d_options* opt, i
     b->status.assign(n, 0);
     b->status_msg.assign(n, std::string());
     b->workers = workers == 0 ? 0 : std::min({workers, n, 64});
+    b->opt = o;
+    if (o.precision == FS2D_PRECISION_MIXED) {
+        std::vector<Sim*> ss(n);
+        for (int k = 0; k < n; k++) ss[k] = sim_of(b->sims[k]);
+        int rc = pack_create_batch(ss.data(), n, &b->pack);
+        if (!rc) rc = check_cuda(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        b->ready.assign(n, nullptr);
+        for (int k = 0; k < n && !rc; k++)
+            rc = check_cuda(cudaEventCreateWithFlags(&b->ready[k], cudaEventDisableTiming), "cudaEventCreate");
+        if (!rc) rc = check_cuda(cudaEventCreateWithFlags(&b->solved, cudaEventDisableTiming), "cudaEventCreate");
+        if (!rc) rc = check_cuda(cudaMalloc((void**)&b->err, kErrWords * sizeof(int)), "cudaMalloc");
+        if (!rc) {
+            int wd[kErrWords] = {0};
+            wd[2] = -1;
+            const long long polls = kWaveSpinLimit;
+            memcpy(&wd[4], &polls, sizeof(polls));
+            rc = check_cuda(cudaMemcpy(b->err, wd, sizeof(wd), cudaMemcpyHostToDevice), "cudaMemcpy");
+        }
+        if (!rc) rc = pack_tune(b->pack, b->stream, b->err, b->device, &b->launches, &b->sweep_us);
+        if (rc) {
+            fs2d_batch_destroy(b);
+            return rc;
+        }
+    }
     *out = b;
     return FS2D_OK;
 }
@@ -211,7 +320,7 @@ int fs2d_batch_step(fs2d_batch* b, int nframes) {
         for (int w : cand) {
             if (nframes == 0) break;
             auto t0 = std::chrono::steady_clock::now();
-            int rc = run(b, w, 1);
+            int rc = b->pack ? run_packed(b, w, 1) : run(b, w, 1);
             if (rc) return rc;
             double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
             b->tuning_ms.push_back(ms);
@@ -224,7 +333,7 @@ int fs2d_batch_step(fs2d_batch* b, int nframes) {
         b->workers = best;
     }
     if (nframes == 0) return FS2D_OK;
-    int rc = run(b, b->workers, nframes);
+    int rc = b->pack ? run_packed(b, b->workers, nframes) : run(b, b->workers, nframes);
     if (rc) return rc;
     for (size_t k = 0; k < b->status.size(); k++)
         if (b->status[k]) {
@@ -263,8 +372,33 @@ int fs2d_batch_set_workers(fs2d_batch* b, int workers) {
 
 int fs2d_batch_destroy(fs2d_batch* b) {
     if (!b) return FS2D_OK;
+    if (b->stream) cudaStreamSynchronize(b->stream);
     for (fs2d_sim* s : b->sims) fs2d_destroy(s);
+    fs2d::pack_free(b->pack);
+    for (cudaEvent_t e : b->ready)
+        if (e) cudaEventDestroy(e);
+    if (b->solved) cudaEventDestroy(b->solved);
+    if (b->err) cudaFree(b->err);
+    if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
+    return FS2D_OK;
+}
+
+int fs2d_batch_sweep_schedule(fs2d_batch* b, int* schedule, int* ctas, int* items, double* sweep_us) {
+    if (!b) return FS2D_ERR_INVALID;
+    fs2d::Pack* pk = b->pack;
+    if (schedule) *schedule = pk ? pk->schedule : -1;
+    if (ctas) *ctas = pk ? pk->sweep_ctas : 0;
+    if (items) *items = pk ? pk->nitems : 0;
+    if (sweep_us) *sweep_us = pk ? b->sweep_us : 0.0;
+    return FS2D_OK;
+}
+
+int fs2d_batch_launch_count(fs2d_batch* b, unsigned long long* out) {
+    if (!b || !out) return FS2D_ERR_INVALID;
+    unsigned long long n = b->launches;
+    for (fs2d_sim* s : b->sims) n += fs2d::sim_of(s)->launches;
+    *out = n;
     return FS2D_OK;
 }
 

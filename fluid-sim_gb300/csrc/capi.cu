@@ -324,15 +324,9 @@ int alloc_all(Sim* s) {
         A(m32.s1, N);
         A(m32.e, N);
         A(pcg32, 1);
-        A(m32_gbase, 1);
-        A(m32_gprogress, (size_t)s->progress_cap);
         (void)m;
-        s->m32maps = new (std::nothrow) Mic32MapsHost();
-        if (!s->m32maps) {
-            set_error("out of host memory");
-            return FS2D_ERR_ALLOC;
-        }
-        if ((rc = mixed_setup_maps(s))) return rc;
+        s->m32_owned = true;
+        if ((rc = pack_create_single(s))) return rc;
     }
 #undef A
     if ((rc = check_cuda(cudaMallocHost((void**)&s->pcg_host, sizeof(PcgScalars)), "cudaMallocHost"))) return rc;
@@ -348,21 +342,22 @@ int alloc_all(Sim* s) {
 
 void free_all(Sim* s) {
     rollout_free(s);
-    if (s->m32_graph) cudaGraphExecDestroy(s->m32_graph);
+    pack_free(s->pack);
+    s->pack = nullptr;
+    if (!s->m32_owned) s->m32 = Mixed32();   // views into a batch's arrays, freed with the batch
     void* ptrs[] = {s->cell, s->phi, s->p, s->u, s->v, s->nu, s->nv, s->pos, s->vel, s->t, s->seed_key,
                     s->phi_tmp, s->surface, s->u0, s->v0, s->udiv, s->vdiv, s->mask_u, s->mask_v, s->cnt_u,
                     s->cnt_v, s->fill_u, s->fill_v, s->ent_u, s->ent_v, s->scan_tmp, s->tile_range, s->max_layer,
                     s->Adiag, s->Ax, s->Ay, s->rhs, s->precon, s->cfx, s->cfy, s->cbx, s->cby, s->r, s->z, s->q, s->w, s->s0,
                     s->s1, s->partial, s->pcg, s->progress, s->stats, s->err, s->m32.a0, s->m32.ax, s->m32.ay,
                     s->m32.pc, s->m32.fa, s->m32.fb, s->m32.fc, s->m32.fd, s->m32.r, s->m32.rp, s->m32.q,
-                    s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32, s->m32_gbase, s->m32_gprogress,
+                    s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32,
                     s->pos_df,
                     s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p, s->phi_p, s->emask};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->pcg_host) cudaFreeHost(s->pcg_host);
     if (s->pcg32_host) cudaFreeHost(s->pcg32_host);
-    delete s->m32maps;
     delete s->cpmaps;
     delete s->ekmaps;
     if (s->stats_host) cudaFreeHost(s->stats_host);
@@ -454,6 +449,70 @@ struct DevScratch {
 Host* H(fs2d_sim* p) { return reinterpret_cast<Host*>(p); }
 
 }  // namespace
+
+// Stages k0 .. k1-1 of runFrame's order (k1 < 0: to the end), each between
+// its two timing events.  With a pack solve in between (a batch), the
+// projection stage is split: `solve_part` 1 runs its FP64 build and FP32
+// setup and stops, 2 takes the finished solve's statistics and goes on.
+int frame_stages(fs2d_sim* p, int k0, int k1, int* status, int solve_part) {
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    const int n = num_stages(s);
+    const int* st = s->mode == FS2D_SEMILAGRANGIAN ? kSlStages : kPicStages;
+    if (k1 < 0) k1 = n;
+    for (int k = k0; k < k1; k++) {
+        const bool split = solve_part != 0 && st[k] == FS2D_STAGE_APPLY_PROJECTION;
+        if (!(split && solve_part == 2)) FS2D_CUDA(cudaEventRecord(s->ev[2 * k], s->stream));
+        int sst = 0;
+        int rc;
+        if (split && solve_part == 1) {
+            rc = projection_build(s);
+            if (!rc) rc = mixed_setup(s);
+            if (rc) return rc;
+            return 0;   // the pack solve follows
+        } else if (split) {
+            rc = mixed_finish(s, &sst);
+        } else {
+            rc = run_stage_impl(s, st[k], &sst);
+        }
+        if (rc) return rc;
+        if (sst) *status = sst;
+        FS2D_CUDA(cudaEventRecord(s->ev[2 * k + 1], s->stream));
+        if (st[k] == FS2D_STAGE_CREATE_WATER_LEVEL_SET) h->stats_pending = true;
+    }
+    return 0;
+}
+
+int frame_solve_stage(fs2d_sim* p) {
+    Sim* s = &H(p)->sim;
+    const int* st = s->mode == FS2D_SEMILAGRANGIAN ? kSlStages : kPicStages;
+    for (int k = 0; k < num_stages(s); k++)
+        if (st[k] == FS2D_STAGE_APPLY_PROJECTION) return k;
+    return -1;
+}
+
+// End of a frame: device error word, statistics, stage times, counters.
+int frame_close(fs2d_sim* p, int rc, int status) {
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    if (rc) return rc;
+    rc = finish(h);
+    const int n = num_stages(s);
+    for (int k = 0; k < n; k++) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, s->ev[2 * k], s->ev[2 * k + 1]);
+        s->stage_ms[k] = ms;
+        h->frame_stage_ms.push_back(ms);
+    }
+    s->n_stage_times = n;
+    s->current_time += s->dt;
+    s->frames++;
+    s->last_status = rc ? rc : status;
+    return s->last_status;
+}
+
+Sim* sim_of(fs2d_sim* p) { return &H(p)->sim; }
+
 }  // namespace fs2d
 
 using namespace fs2d;
@@ -726,32 +785,9 @@ int fs2d_backward(fs2d_sim* p, double* gradU0, double* gradV0) {
 
 int fs2d_run_frame(fs2d_sim* p) {
     if (!p) return FS2D_ERR_INVALID;
-    Host* h = H(p);
-    Sim* s = &h->sim;
-    const int n = num_stages(s);
-    const int* st = s->mode == FS2D_SEMILAGRANGIAN ? kSlStages : kPicStages;
     int status = 0;
-    for (int k = 0; k < n; k++) {
-        FS2D_CUDA(cudaEventRecord(s->ev[2 * k], s->stream));
-        int sst = 0;
-        int rc = run_stage_impl(s, st[k], &sst);
-        if (rc) return rc;
-        if (sst) status = sst;
-        FS2D_CUDA(cudaEventRecord(s->ev[2 * k + 1], s->stream));
-        if (st[k] == FS2D_STAGE_CREATE_WATER_LEVEL_SET) h->stats_pending = true;
-    }
-    int rc = finish(h);
-    for (int k = 0; k < n; k++) {
-        float ms = 0;
-        cudaEventElapsedTime(&ms, s->ev[2 * k], s->ev[2 * k + 1]);
-        s->stage_ms[k] = ms;
-        h->frame_stage_ms.push_back(ms);
-    }
-    s->n_stage_times = n;
-    s->current_time += s->dt;
-    s->frames++;
-    s->last_status = rc ? rc : status;
-    return s->last_status;
+    int rc = frame_stages(p, 0, -1, &status);
+    return frame_close(p, rc, status);
 }
 
 int fs2d_step(fs2d_sim* p, int nframes) {

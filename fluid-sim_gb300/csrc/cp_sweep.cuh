@@ -316,8 +316,11 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
                         tma_store_2d(&maps.st_tail, x, 0, src + (kCpBoxRows - tail) * kCpCols);
                     }
                     bulk_commit();
-                    bulk_wait_read<0>();
-                    *tiles_freed = ts + 1;
+                    // no wait for this store's own read: once every store but the
+                    // newest has read its tile, tiles < ts are free (the compute
+                    // warp reuses a slot kCpSlots tiles later)
+                    bulk_wait_read<1>();
+                    *tiles_freed = ts;
                 }
                 __syncwarp();
                 ts++;

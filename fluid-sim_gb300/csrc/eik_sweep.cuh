@@ -208,8 +208,9 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                     moved = true;
                 }
             }
-            // top row out: to the next strip's ring (same cluster) or to global memory
-            if (tc < tend) {
+            // top row out: to the next strip's ring (same cluster) or to global
+            // memory, every complete run of up to 128 columns at once
+            for (int rep = 0; rep < 4 && tc < tend; rep++) {
                 const int c = tc + lane;
                 unsigned long long w0 = 0ull, w1 = 0ull;
                 if (c < P) {
@@ -247,6 +248,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                     if (lane == 0) *top_done = tc;
                     moved = true;
                 }
+                if (n < 32) break;
             }
             if (ts < nt && *tiles_done > ts) {
                 if (lane == 0) {
@@ -259,8 +261,11 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                         tma_store_2d(&maps.st_tail, x, 0, src + (kEkRows - tail) * kEkCols);
                     }
                     bulk_commit();
-                    bulk_wait_read<0>();
-                    *tiles_freed = ts + 1;
+                    // no wait for this store's own read: once every store but the
+                    // newest has read its tile, tiles < ts are free (the compute
+                    // warp reuses a slot kEkSlots tiles later)
+                    bulk_wait_read<1>();
+                    *tiles_freed = ts;
                 }
                 __syncwarp();
                 ts++;

@@ -55,6 +55,13 @@ struct PcgScalars {
     int done;           // 1 once the solve stopped
     int first;          // 1 until the first search direction was formed
     unsigned int ticket[4];  // last-block-done counters, one per reduction kernel
+    // mixed precision: the FP64 refinement around the FP32 inner solves
+    // (kept in the handle's FP64 scalars) and whether an inner solve runs in
+    // the current refinement sweep (kept in the FP32 scalars)
+    int outer_iters;    // refinement sweeps done
+    int outer_done;     // 1 once the refinement stopped (converged, nothing to solve, or the sweep cap)
+    int inner_total;    // inner iterations summed over the sweeps
+    int active;         // FP32 scalars: 1 while this sweep solves the scene
 };
 
 // Scalars of the per-frame statistics (createWaterLevelSet, src/FluidSim2D.cpp:709-731).
@@ -79,6 +86,35 @@ struct Mixed32 {
     float *r = nullptr, *rp = nullptr, *q = nullptr, *z = nullptr, *w = nullptr;
     float *s0 = nullptr, *s1 = nullptr, *e = nullptr;
 };
+// One scene of a pack (below): where its padded FP32 region lies in the
+// pack's arrays, its block ranges in the pack's reduction launches, and the
+// handle arrays the FP64 refinement works on.
+struct PackScene {
+    int NX, NY;              // cells
+    int P32, NY32;           // padded extent (multiples of 128 columns and 32 rows)
+    long long off;           // pack offset of the scene's cell (0, 0): y0 * pitch + x0
+    int x0, y0;              // pack column and row of that cell
+    int gx, gy, blk0;        // FP32 reductions: gx x gy blocks of row segments, from block blk0
+    int nb64, blk64;         // FP64 refinement kernels: nb64 blocks of 256 cells, from block blk64
+    const uint8_t* cell;     // labels (NX x NY)
+    const double *A0, *Ax, *Ay, *rhs;
+    double *p, *r;           // FP64 pressure and residual
+    PcgScalars *outer;       // the handle's FP64 scalars (refinement)
+    PcgScalars *inner;       // the handle's FP32 scalars (inner solve)
+    float2* part;            // FP32 reduction partials (gx * gy), in the pack's buffer
+    double* part64;          // FP64 residual partials (nb64), in the pack's buffer
+};
+
+// Work item of a sweep over several scenes: one strip of 128 columns of one
+// scene; a scene's strips are consecutive items in sweep order.
+struct Mic32Item {
+    int scene;               // index in the pack's scene table
+    int strip;               // strip of the scene (0: first in sweep order)
+    int nstrips;             // strips of the scene
+    int x0, P32;             // the scene's pack column and padded width
+    int y0, NY32;            // the scene's pack row and padded rows
+};
+
 // TMA descriptors of the two FP32 MIC(0) sweeps (see mic32_tma.cuh).
 struct Mic32MapsHost {
     alignas(64) unsigned char fwd[4 * 128];
@@ -97,6 +133,48 @@ struct CpConst {
     float tiny_q;    // >= 2^-20 dr^2
     unsigned amax;   // bits of max |h| over particle coordinates (non-negative float)
     int fast;        // 0: dr or A not finite/representable, every decision is exact
+};
+
+// A pack: the FP32 solver arrays of one scene, or of several scenes side by
+// side in one set of pitched arrays (a batch), with everything one launch
+// per kernel of the inner solve needs: the scene table, the map from block to
+// scene of the reduction launches, the sweep work items and the counters the
+// host polls.  A mixed-precision handle owns a pack of its own scene; a batch
+// owns a pack of all its scenes, and each scene's handle then works on its
+// region of the batch's arrays (projection_mixed.cu).
+struct Pack {
+    int n = 0;                            // scenes
+    int pitch = 0, rows = 0;              // array extent: rows x pitch floats
+    Mixed32 m;                            // the arrays
+    bool owns_arrays = false;             // freed with the pack (a batch); else the handle's
+    std::vector<PackScene> scenes;        // scene table (host copy)
+    PackScene* d_scenes = nullptr;
+    float2* part = nullptr;               // FP32 reduction partials, one per block of nblk
+    double* part64 = nullptr;             // FP64 residual partials, one per block of nblk64
+    int* d_blk = nullptr;                 // scene of each block of the FP32 reduction launches
+    int nblk = 0;
+    int* d_blk64 = nullptr;               // scene of each block of the FP64 refinement launches
+    int nblk64 = 0;
+    Mic32Item* d_items = nullptr;         // sweep work items (several scenes only)
+    int nitems = 0;
+    // counters in device memory: [0] scenes whose inner solve is running,
+    // [1] scenes still refining, [2..5] work and exit counters of the two
+    // persistent sweeps; h_ctl is a pinned mirror for polling
+    int* d_ctl = nullptr;
+    int* h_ctl = nullptr;
+    unsigned long long* progress = nullptr;    // sweep progress (items), direct launches
+    unsigned long long* gprogress = nullptr;   // ... graph-replayed launches
+    unsigned long long* gbase = nullptr;       // device progress base of graph-replayed sweeps
+    int progress_cap = 0;
+    Mic32MapsHost* maps = nullptr;             // tensor maps of the pack's arrays
+    int cluster = 0;                           // cluster size of single-scene sweeps (0: not chosen)
+    int sweep_ctas = 0;                        // CTAs of persistent sweeps (several scenes)
+    int schedule = 0;                          // order of the scenes in the sweep's work list (pack_tune)
+    unsigned long long wave_launch = 0;        // progress bases of direct sweeps
+    cudaGraphExec_t graph = nullptr;           // inner iterations captured as a graph
+    const void* graph_key = nullptr;
+    unsigned long long graph_launches = 0;
+    int graph_state = 0;                       // 0 not tried, 1 ready, -1 unavailable (direct launches)
 };
 
 struct Sim {
@@ -155,20 +233,13 @@ struct Sim {
     size_t partial_cap = 0;
     PcgScalars* pcg = nullptr;
     PcgScalars* pcg_host = nullptr;                  // pinned mirror for polling
-    Mixed32 m32;                                     // MIXED precision only
+    Mixed32 m32;                                     // MIXED precision only: views into pack->m
     int P = 0;                                       // row pitch of the pitched arrays (NX rounded up to 32)
-    int P32 = 0, NY32 = 0;                           // pitch and rows of the FP32 solver arrays (Mixed32)
-    Mic32MapsHost* m32maps = nullptr;
-    int m32_cluster = 0;                             // cluster size of the FP32 MIC(0) sweeps (0: not chosen)
+    int P32 = 0, NY32 = 0;                           // pitch of the FP32 solver arrays, padded rows of the scene
     PcgScalars* pcg32 = nullptr;                     // inner FP32 solve scalars
     PcgScalars* pcg32_host = nullptr;
-    // the inner PCG loop replayed as a CUDA graph of kM32GraphIters iterations
-    unsigned long long* m32_gbase = nullptr;         // device progress base of graph-replayed sweeps
-    unsigned long long* m32_gprogress = nullptr;     // their progress counters (progress_cap)
-    cudaGraphExec_t m32_graph = nullptr;
-    const void* m32_graph_key = nullptr;             // s->partial when the graph was captured
-    unsigned long long m32_graph_launches = 0;       // kernels per replay
-    int m32_graph_state = 0;                         // 0 not tried, 1 ready, -1 unavailable (direct launches)
+    Pack* pack = nullptr;                            // MIXED: the pack of this scene alone
+    bool m32_owned = true;                           // m32 arrays allocated by this handle (not a batch's views)
 
     // wavefront progress flags (monotonic, 64-bit, never reset)
     unsigned long long* progress = nullptr;
@@ -279,7 +350,30 @@ int projection_build(Sim* s);             // FP64 matrix, rhs, p = 0, r = rhs, |
 int projection_set_rhs(Sim* s, const double* b);   // after projection_build: rhs = r = b, p = 0
 int projection_solve_custom(Sim* s, const double* b, int* status);  // A p = b (device b), handle's precision
 int projection_mixed_rhs(Sim* s, const double* b, int* status);     // mixed solve; b == nullptr: physical rhs
-int mixed_setup_maps(Sim* s);             // TMA descriptors of the FP32 MIC(0) sweeps
+// ---- packs of FP32 solver arrays (projection_mixed.cu) ----
+// The pack of a handle's own scene (its FP32 arrays at pitch s->P32).
+int pack_create_single(Sim* s);
+// A pack of several handles' scenes in new arrays; each scene's FP32 arrays
+// become views into them (their pitch becomes the pack's).
+int pack_create_batch(Sim* const* sims, int n, Pack** out);
+void pack_free(Pack* pk);
+// Device state of the handle's FP32 setup for a solve (matrix, MIC(0) factor,
+// folded coefficients) after projection_build / projection_set_rhs.
+int mixed_setup(Sim* s);
+// The refinement loop of every scene of the pack (each after mixed_setup),
+// on `stream`; returns after the work completed.
+// Kernels go on `stream`, count into *launches and report waits that gave up
+// in `err` (an error word with its wait controls); `timer` (may be null)
+// times the launches as fs2d_set_kernel_timing asks.
+int pack_solve(Pack* pk, const fs2d_options& opt, cudaStream_t stream, unsigned long long* launches, int* err,
+               int device, Sim* timer);
+// Chooses the persistent sweep's schedule and CTA count of a pack of several
+// scenes by timing forward sweeps of each candidate; *best_us (may be null)
+// receives the chosen sweep's time.
+int pack_tune(Pack* pk, cudaStream_t stream, int* err, int device, unsigned long long* launches, double* best_us);
+// Statistics of the handle's last mixed solve (from its scalars); *status =
+// FS2D_ERR_NOT_CONVERGED when it stopped short of its tolerance.
+int mixed_finish(Sim* s, int* status);
 int cp_setup_maps(Sim* s);                // TMA descriptors of the closest-point sweeps
 int update_velocity(Sim* s);              // updateVelocity
 int g2p(Sim* s);                          // updateParticleVelocities
@@ -308,6 +402,12 @@ int rollout_forward(Sim* s, int steps, int every, const double* u0, const double
                     const double* vt, double* loss);
 int rollout_backward(Sim* s, double* gu, double* gv);
 void rollout_free(Sim* s);
+
+// ---- frames in parts (capi.cu), for batches that solve their scenes together ----
+int frame_stages(fs2d_sim* p, int k0, int k1, int* status, int solve_part = 0);
+int frame_solve_stage(fs2d_sim* p);   // index of applyProjection in the frame's stage order
+int frame_close(fs2d_sim* p, int rc, int status);
+Sim* sim_of(fs2d_sim* p);
 
 // ---- wavefront plumbing ----
 // Reserves `n` progress counters and returns the base value for this launch.

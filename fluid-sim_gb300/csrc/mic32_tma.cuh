@@ -93,22 +93,41 @@ __device__ __forceinline__ float4 m32_pack(const float (&o)[4]) {
     return FWD ? make_float4(o[0], o[1], o[2], o[3]) : make_float4(o[3], o[2], o[1], o[0]);
 }
 
+// Arguments of one sweep.  One scene (SEVERAL = false): strip = block, the
+// scene's padded region is the whole pack (P32 x NY32 at the origin) and
+// `skip` (may be null) cancels the launch.  Several scenes (SEVERAL = true):
+// persistent CTAs take the work items in order from work[0] (work[1] counts
+// the CTAs that finished; the last one resets both for the next launch); an
+// item of a scene whose inner solve stopped is skipped.
+struct Mic32Args {
+    float* out;                          // result array (pack pitch)
+    int pitch;                           // pack pitch
+    int P32, NY32;                       // one scene: its padded extent
+    const int* skip;                     // one scene: cancel flag
+    const Mic32Item* items;              // several scenes
+    int nitems;
+    const PackScene* scenes;
+    int* work;
+    unsigned long long* progress;        // one counter per strip / item
+    unsigned long long base_host;
+    const unsigned long long* base_dev;  // graph-replayed launches: device-memory base (see launch_mic32)
+    int* err;
+};
+
 // out = v0 - v1 * left - v2 * below on the cells of sweep order: the forward
 // sweep on q~ = q*pc (v0 = r*pc^2, v1 = fa, v2 = fb), the backward sweep on z
-// (v0 = q~, v1 = fc, v2 = fd).  Grid: P / 128 strips (rounded up to whole
-// clusters) of 64 threads: warp 0 computes, warp 1 moves the strip boundary
-// and the tile stores.  NR: rows of the padded arrays (a multiple of 32).
-//
-// base_dev: when non-null, the launch's progress base is the device-memory
-// value plus `base_host` (launches replayed from a CUDA graph: one bump of
-// that counter per replay, and a fixed offset per sweep of the replay);
-// otherwise `base_host` alone.
-template <bool FWD>
-__global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32Maps maps, float* out, int P, int NR,
-                                                   unsigned long long* progress, unsigned long long base_host,
-                                                   const unsigned long long* base_dev, int* err, const int* skip) {
-    if (skip != nullptr && *skip) return;
-    const unsigned long long base = base_dev != nullptr ? *base_dev + base_host : base_host;
+// (v0 = q~, v1 = fc, v2 = fd).  Blocks of 64 threads: warp 0 computes, warp 1
+// moves the strip boundary and the tile stores.  One scene: P32 / 128
+// strips, rounded up to whole clusters, neighbours in a cluster hand their
+// columns over in shared memory; several scenes: a cooperative grid of
+// persistent CTAs, hand-offs through global memory.
+template <bool FWD, bool SEVERAL>
+__global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32Maps maps, const Mic32Args a) {
+    if (!SEVERAL && a.skip != nullptr && *a.skip) return;
+    const unsigned long long base = a.base_dev != nullptr ? *a.base_dev + a.base_host : a.base_host;
+    int* const err = a.err;
+    float* const out = a.out;
+    const int pitch = a.pitch;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     float* ring = reinterpret_cast<float*>(smem_raw);   // [kM32NA][kM32RingRows][kM32Cols]
     // the previous strip's last column (the cells left of this strip), tagged by row
@@ -121,301 +140,348 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
     volatile int* quit = ctr + 2;           // compute warp gave up (timeout)
     volatile int* tiles_done = ctr + 3;     // tiles whose results are complete in shared memory
     volatile int* tiles_freed = ctr + 4;    // tiles whose TMA store has finished reading shared memory
+    volatile int* cur_item = ctr + 5;       // several scenes: the CTA's current work item
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(const_cast<int*>(ctr) + 8);
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int strip = blockIdx.x;
-    const int nstrips = P / kM32Cols;
-    const int nt = NR / kM32Rows;                               // tiles per strip
-    const bool active = strip < nstrips;                        // the grid is rounded up to whole clusters
-    const bool has_next = strip + 1 < nstrips;
-    // this strip hands its last column to the next one (unless the test hook holds it back)
-    const bool publishes = has_next && !wave_held(err, kWaveKindMic32, strip);
     const long long spin = wave_spin(err);
-    const bool left_in_grid = strip > 0;
-    const int xbox = FWD ? strip * kM32Cols : P - (strip + 1) * kM32Cols;   // memory column of box column 0
-    const int xlast = FWD ? xbox + kM32Cols - 1 : xbox;        // memory column of the strip's last sweep column
-    const int xprev = FWD ? xbox - 1 : xbox + kM32Cols;        // ... and of the previous strip's
-    const unsigned crank = cluster_ctarank(), csize = cluster_nctarank();
-    const bool prev_local = left_in_grid && crank > 0;         // the previous strip fills this ring
-    const bool next_local = publishes && crank + 1 < csize;    // this strip fills the next strip's ring
-    auto mrow = [&](int r) { return FWD ? r : NR - 1 - r; };  // memory row of sweep row r
-    auto tile_y = [&](int t) { return FWD ? t * kM32Rows : NR - (t + 1) * kM32Rows; };
+    const unsigned crank = SEVERAL ? 0u : cluster_ctarank(), csize = SEVERAL ? 1u : cluster_nctarank();
+    // completed phases of each slot's mbarrier (compute warp), kept across work items
+    unsigned phases[kM32Slots] = {0u, 0u, 0u, 0u};
 
     if (threadIdx.x == 0) {
         for (int k = 0; k < kM32Slots; k++) mbar_init(bars + k, 1);
         fence_mbar_init();
-        *bnd_used = 0;
-        *top_done = 0;
-        *quit = 0;
-        *tiles_done = 0;
-        *tiles_freed = 0;
     }
-    for (int k = threadIdx.x; k < kM32BndRing; k += blockDim.x) bnd[k] = ~0ull;   // no row matches
-    for (int k = threadIdx.x; k < kM32TopRing; k += blockDim.x) top[k] = ~0ull;
-    cluster_sync_all();   // every ring and counter of the cluster is initialised
 
-    if (warp == 1 && active) {
-        // ---------------- I/O warp ----------------
-        const unsigned long long* gprev = left_in_grid ? progress + (strip - 1) : nullptr;
-        int hb = (left_in_grid && !prev_local) ? 0 : NR;   // next row of the left column to fetch
-        int tc = 0;                                        // rows of the last column forwarded
-        const int tend = publishes ? NR : 0;
-        int rused = 0;                                     // last seen chunk position of the consumer
-        const unsigned r_bnd = next_local ? mapa_shared((const void*)bnd, crank + 1) : 0u;
-        const unsigned r_used = next_local ? mapa_shared((const void*)bnd_used, crank + 1) : 0u;
-        int ts = 0;                                        // next tile to store
-        unsigned long long gavail = 0;
-        long long idle = 0;
-        while (hb < NR || tc < tend || ts < nt) {
-            bool moved = false;
-            // left column from global memory (the previous strip is in another cluster)
-            const int hb_lim = (*bnd_used + kM32BndChunks - 2) * kM32CH;   // slots consumed two chunks ago
-            if (hb < NR && hb < hb_lim) {
-                const int n = min(min(32, NR - hb), hb_lim - hb);
-                const unsigned long long need = base + (unsigned long long)(hb + n);
-                if (gavail < need) {
-                    unsigned long long v = 0;
-                    if (lane == 0) v = ld_acquire(gprev);
-                    gavail = __shfl_sync(0xffffffffu, v, 0);
+    // One strip of one scene: `strip` of `nstrips`, the scene's padded region
+    // at pack column x0, row y0, P32 x NR; progress counter `pidx` (the previous
+    // strip's is pidx - 1).
+    auto run_strip = [&](int strip, int nstrips, int x0, int P32, int y0, int NR, int pidx) {
+        const int nt = NR / kM32Rows;                           // tiles per strip
+        const bool has_next = strip + 1 < nstrips;
+        // this strip hands its last column to the next one (unless the test hook holds it back)
+        const bool publishes = has_next && !wave_held(err, kWaveKindMic32, strip);
+        const bool left_in_grid = strip > 0;
+        const int xbox = x0 + (FWD ? strip * kM32Cols : P32 - (strip + 1) * kM32Cols);   // pack column of box column 0
+        const int xlast = FWD ? xbox + kM32Cols - 1 : xbox;    // pack column of the strip's last sweep column
+        const int xprev = FWD ? xbox - 1 : xbox + kM32Cols;    // ... and of the previous strip's
+        const bool prev_local = !SEVERAL && left_in_grid && crank > 0;       // the previous strip fills this ring
+        const bool next_local = !SEVERAL && publishes && crank + 1 < csize;  // this strip fills the next strip's ring
+        auto mrow = [&](int r) { return y0 + (FWD ? r : NR - 1 - r); };   // pack row of sweep row r
+        auto tile_y = [&](int t) { return y0 + (FWD ? t * kM32Rows : NR - (t + 1) * kM32Rows); };
+
+        if (warp == 1) {
+            // ---------------- I/O warp ----------------
+            const unsigned long long* gprev = left_in_grid ? a.progress + (pidx - 1) : nullptr;
+            int hb = (left_in_grid && !prev_local) ? 0 : NR;   // next row of the left column to fetch
+            int tc = 0;                                        // rows of the last column forwarded
+            const int tend = publishes ? NR : 0;
+            int rused = 0;                                     // last seen chunk position of the consumer
+            const unsigned r_bnd = next_local ? mapa_shared((const void*)bnd, crank + 1) : 0u;
+            const unsigned r_used = next_local ? mapa_shared((const void*)bnd_used, crank + 1) : 0u;
+            int ts = 0;                                        // next tile to store
+            unsigned long long gavail = 0;
+            long long idle = 0;
+            while (hb < NR || tc < tend || ts < nt) {
+                bool moved = false;
+                // left column from global memory (the previous strip is in another cluster)
+                const int hb_lim = (*bnd_used + kM32BndChunks - 2) * kM32CH;   // slots consumed two chunks ago
+                if (hb < NR && hb < hb_lim) {
+                    const int n = min(min(32, NR - hb), hb_lim - hb);
+                    const unsigned long long need = base + (unsigned long long)(hb + n);
+                    if (gavail < need) {
+                        unsigned long long v = 0;
+                        if (lane == 0) v = ld_acquire(gprev);
+                        gavail = __shfl_sync(0xffffffffu, v, 0);
+                    }
+                    const int avail = (int)min((unsigned long long)n, gavail > base + hb ? gavail - base - hb : 0ull);
+                    if (avail > 0) {
+                        __syncwarp();   // lane 0's acquire orders the reads below
+                        const int r = hb + lane;
+                        if (lane < avail)
+                            bnd[r % kM32BndRing] = m32_entry(r, __ldcg(out + (size_t)mrow(r) * pitch + xprev));
+                        __syncwarp();
+                        hb += avail;
+                        moved = true;
+                    }
                 }
-                const int avail = (int)min((unsigned long long)n, gavail > base + hb ? gavail - base - hb : 0ull);
-                if (avail > 0) {
-                    __syncwarp();   // lane 0's acquire orders the reads below
-                    const int r = hb + lane;
-                    if (lane < avail) bnd[r % kM32BndRing] = m32_entry(r, __ldcg(out + (size_t)mrow(r) * P + xprev));
+                // last column out: to the next strip's ring (same cluster) or to global
+                // memory, every complete run of up to 128 rows at once
+                for (int rep = 0; rep < 4 && tc < tend; rep++) {
+                    const int r = tc + lane;
+                    const unsigned long long e = r < NR ? top[r % kM32TopRing] : 0ull;
+                    const bool ok = r >= NR || m32_entry_is(e, r);
+                    const unsigned bad = __ballot_sync(0xffffffffu, !ok);
+                    int n = bad ? __ffs(bad) - 1 : 32;
+                    n = min(n, NR - tc);
+                    if (n > 0 && next_local) {
+                        // the consumer's ring slot of row r was last used by row r - kM32BndRing
+                        if (tc + n > (rused + kM32BndChunks - 2) * kM32CH) {
+                            int v = 0;
+                            if (lane == 0) v = ld_volatile_cluster_remote(r_used);
+                            rused = __shfl_sync(0xffffffffu, v, 0);
+                        }
+                        n = min(n, (rused + kM32BndChunks - 2) * kM32CH - tc);
+                    }
+                    if (n > 0) {
+                        if (next_local) {
+                            if (lane < n) st_cluster_u64(r_bnd + 8u * (unsigned)(r % kM32BndRing), e);
+                            __syncwarp();
+                        } else {
+                            if (lane < n) out[(size_t)mrow(r) * pitch + xlast] = m32_entry_value(e);
+                            __threadfence();
+                            __syncwarp();
+                            if (lane == 0) st_release(a.progress + pidx, base + (unsigned long long)(tc + n));
+                        }
+                        tc += n;
+                        if (lane == 0) *top_done = tc;
+                        moved = true;
+                    }
+                    if (n < 32) break;
+                }
+                if (ts < nt && *tiles_done > ts) {
+                    // results of tile ts are complete (the compute warp fenced them
+                    // for the async proxy before publishing tiles_done).  The warp
+                    // does not wait for this store to read its tile: once every
+                    // store but the newest has read its tile, tiles < ts are free
+                    // (the compute warp reuses a slot two tiles after its store)
+                    if (lane == 0) {
+                        tma_store_2d(&maps.out, xbox, tile_y(ts), ring + (size_t)(ts & (kM32Slots - 1)) * kM32TileFloats);
+                        bulk_commit();
+                        bulk_wait_read<1>();
+                        *tiles_freed = ts;
+                    }
                     __syncwarp();
-                    hb += avail;
+                    ts++;
                     moved = true;
                 }
-            }
-            // last column out: to the next strip's ring (same cluster) or to global memory
-            if (tc < tend) {
-                const int r = tc + lane;
-                const unsigned long long e = r < NR ? top[r % kM32TopRing] : 0ull;
-                const bool ok = r >= NR || m32_entry_is(e, r);
-                const unsigned bad = __ballot_sync(0xffffffffu, !ok);
-                int n = bad ? __ffs(bad) - 1 : 32;
-                n = min(n, NR - tc);
-                if (n > 0 && next_local) {
-                    // the consumer's ring slot of row r was last used by row r - kM32BndRing
-                    if (tc + n > (rused + kM32BndChunks - 2) * kM32CH) {
-                        int v = 0;
-                        if (lane == 0) v = ld_volatile_cluster_remote(r_used);
-                        rused = __shfl_sync(0xffffffffu, v, 0);
-                    }
-                    n = min(n, (rused + kM32BndChunks - 2) * kM32CH - tc);
-                }
-                if (n > 0) {
-                    if (next_local) {
-                        if (lane < n) st_cluster_u64(r_bnd + 8u * (unsigned)(r % kM32BndRing), e);
-                        __syncwarp();
-                    } else {
-                        if (lane < n) out[(size_t)mrow(r) * P + xlast] = m32_entry_value(e);
-                        __threadfence();
-                        __syncwarp();
-                        if (lane == 0) st_release(progress + strip, base + (unsigned long long)(tc + n));
-                    }
-                    tc += n;
-                    if (lane == 0) *top_done = tc;
-                    moved = true;
+                if (moved) {
+                    idle = 0;
+                } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(err))) {
+                    if (lane == 0) atomicOr(err, 1);
+                    break;
                 }
             }
-            if (ts < nt && *tiles_done > ts) {
-                // results of tile ts are complete (the compute warp fenced them
-                // for the async proxy before publishing tiles_done)
-                if (lane == 0) {
-                    tma_store_2d(&maps.out, xbox, tile_y(ts), ring + (size_t)(ts & (kM32Slots - 1)) * kM32TileFloats);
-                    bulk_commit();
-                    bulk_wait_read<0>();
-                    *tiles_freed = ts + 1;
-                }
-                __syncwarp();
-                ts++;
-                moved = true;
-            }
-            if (moved) {
-                idle = 0;
-            } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(err))) {
-                if (lane == 0) atomicOr(err, 1);
-                break;
-            }
-        }
-        if (lane == 0) bulk_wait_all();
-        __syncwarp();
-    } else if (warp == 0 && active) {
-        // ---------------- compute warp ----------------
-        bool failed = false;
-        int issued = 0;         // tiles whose loads were issued (none after a failure)
-        int unconfirmed = nt;   // first tile whose wait gave up
-        auto issue = [&](int t) {
-            if (t < nt && !failed) {
-                if (lane == 0) {
-                    unsigned long long* bar = bars + (t & (kM32Slots - 1));
-                    mbar_expect_tx(bar, kM32NA * kM32TileBytes);
-                    float* dst = ring + (size_t)(t & (kM32Slots - 1)) * kM32TileFloats;
+            if (lane == 0) bulk_wait_all();
+            __syncwarp();
+        } else {
+            // ---------------- compute warp ----------------
+            bool failed = false;
+            int issued = 0;         // tiles whose loads were issued (none after a failure)
+            int unconfirmed = nt;   // first tile whose wait gave up
+            auto issue = [&](int t) {
+                if (t < nt && !failed) {
+                    if (lane == 0) {
+                        unsigned long long* bar = bars + (t & (kM32Slots - 1));
+                        mbar_expect_tx(bar, kM32NA * kM32TileBytes);
+                        float* dst = ring + (size_t)(t & (kM32Slots - 1)) * kM32TileFloats;
 #pragma unroll
-                    for (int a = 0; a < kM32NA; a++)
-                        tma_load_2d(dst + (size_t)a * kM32ArrayFloats, &maps.in[a], xbox, tile_y(t), bar);
+                        for (int k = 0; k < kM32NA; k++)
+                            tma_load_2d(dst + (size_t)k * kM32ArrayFloats, &maps.in[k], xbox, tile_y(t), bar);
+                    }
+                    issued = t + 1;
                 }
-                issued = t + 1;
-            }
-        };
-        auto poll_tile = [&](int t) -> bool {
-            unsigned long long* bar = bars + (t & (kM32Slots - 1));
-            const unsigned parity = (unsigned)((t / kM32Slots) & 1);
-            long long polls = 0;
-            while (!mbar_try_wait(bar, parity))
-                if (++polls > kWaveSpinLimit) return false;
-            return true;
-        };
-        auto wait_tile = [&](int t) {
-            if (t >= issued) return;
-            if (!poll_tile(t)) {
-                failed = true;
-                atomicOr(err, 1);
-                unconfirmed = min(unconfirmed, t);
-            }
-        };
-        auto spin_ge = [&](volatile int* flag, int need) {  // bounded wait on an I/O-warp counter
-            if (failed) return;  // after one timeout the results are invalid: do not wait again
-            long long polls = 0;
-            while (*flag < need) {
-                if (++polls > 16 * spin) {
+            };
+            // slot phases: tile t of this strip is load number phases[slot] of its slot
+            auto poll_tile = [&](int t) -> bool {
+                const int k = t & (kM32Slots - 1);
+                long long polls = 0;
+                while (!mbar_try_wait(bars + k, phases[k] & 1u))
+                    if (++polls > kWaveSpinLimit) return false;
+                phases[k]++;
+                return true;
+            };
+            auto wait_tile = [&](int t) {
+                if (t >= issued) return;
+                if (!poll_tile(t)) {
                     failed = true;
                     atomicOr(err, 1);
-                    *quit = 1;
-                    return;
+                    unconfirmed = min(unconfirmed, t);
                 }
-            }
-        };
-        issue(0);
-        issue(1);
+            };
+            auto spin_ge = [&](volatile int* flag, int need) {  // bounded wait on an I/O-warp counter
+                if (failed) return;  // after one timeout the results are invalid: do not wait again
+                long long polls = 0;
+                while (*flag < need) {
+                    if (++polls > 16 * spin) {
+                        failed = true;
+                        atomicOr(err, 1);
+                        *quit = 1;
+                        return;
+                    }
+                }
+            };
+            issue(0);
+            issue(1);
 
-        // the lane's float4 in every ring row: box columns 4l .. 4l+3 (the
-        // backward sweep's box is mirrored: its sweep column 4l is box column
-        // 127 - 4l); ring row of sweep row r: r (forward) or r ^ 31 (backward,
-        // whose box rows run against the sweep), modulo the ring
-        const int colbase = FWD ? kM32Lane * lane : kM32Cols - kM32Lane * (lane + 1);
-        constexpr int kRowXor = FWD ? 0 : kM32Rows - 1;
-        auto cell_ptr = [&](int r) {
-            return ring + (size_t)((r ^ kRowXor) & (kM32RingRows - 1)) * kM32Cols + colbase;
-        };
-        // plain (non-volatile) views of the rings for the pipelined per-step
-        // accesses; the row tags make stale reads harmless
-        const unsigned long long* bnd_p = const_cast<const unsigned long long*>(bnd);
-        unsigned long long* top_p = const_cast<unsigned long long*>(top);
-        float o[4] = {0.f, 0.f, 0.f, 0.f};   // the lane's row r - 1 (the cells below)
-        unsigned long long bn = 0ull;        // left-column entry of the next step (read one step ahead)
-        float4 x_n, a_n, b_n;                // operands of the next step (loaded one step ahead)
-        auto load_next = [&](const float* p) {
-            x_n = *reinterpret_cast<const float4*>(p);
-            a_n = *reinterpret_cast<const float4*>(p + kM32ArrayFloats);
-            b_n = *reinterpret_cast<const float4*>(p + 2 * kM32ArrayFloats);
-        };
+            // the lane's float4 in every ring row: box columns 4l .. 4l+3 (the
+            // backward sweep's box is mirrored: its sweep column 4l is box column
+            // 127 - 4l); ring row of sweep row r: r (forward) or r ^ 31 (backward,
+            // whose box rows run against the sweep), modulo the ring
+            const int colbase = FWD ? kM32Lane * lane : kM32Cols - kM32Lane * (lane + 1);
+            constexpr int kRowXor = FWD ? 0 : kM32Rows - 1;
+            auto cell_ptr = [&](int r) {
+                return ring + (size_t)((r ^ kRowXor) & (kM32RingRows - 1)) * kM32Cols + colbase;
+            };
+            // plain (non-volatile) views of the rings for the pipelined per-step
+            // accesses; the row tags make stale reads harmless
+            const unsigned long long* bnd_p = const_cast<const unsigned long long*>(bnd);
+            unsigned long long* top_p = const_cast<unsigned long long*>(top);
+            float o[4] = {0.f, 0.f, 0.f, 0.f};   // the lane's row r - 1 (the cells below)
+            unsigned long long bn = 0ull;        // left-column entry of the next step (read one step ahead)
+            float4 x_n, a_n, b_n;                // operands of the next step (loaded one step ahead)
+            auto load_next = [&](const float* p) {
+                x_n = *reinterpret_cast<const float4*>(p);
+                a_n = *reinterpret_cast<const float4*>(p + kM32ArrayFloats);
+                b_n = *reinterpret_cast<const float4*>(p + 2 * kM32ArrayFloats);
+            };
 
-        // One tile group of 32 steps.  CHECK: some lane's row may lie outside
-        // [0, NR) (first and last groups); a compile-time flag, so that the
-        // steady-state groups carry no per-step range tests.
-        auto tile_steps = [&](int t, auto check_tag) {
-            constexpr bool check = decltype(check_tag)::value;
-            {
-                const int r0 = t * kM32Rows - lane;
-                load_next(cell_ptr(r0 < 0 ? 0 : r0));
-            }
-            // one chunk of the left column per group: a rolled loop over the
-            // tile's two chunks with each chunk's steps unrolled
+            // One tile group of 32 steps.  CHECK: some lane's row may lie outside
+            // [0, NR) (first and last groups); a compile-time flag, so that the
+            // steady-state groups carry no per-step range tests.
+            auto tile_steps = [&](int t, auto check_tag) {
+                constexpr bool check = decltype(check_tag)::value;
+                {
+                    const int r0 = t * kM32Rows - lane;
+                    load_next(cell_ptr(r0 < 0 ? 0 : r0));
+                }
+                // one chunk of the left column per group: a rolled loop over the
+                // tile's two chunks with each chunk's steps unrolled
 #pragma unroll 1
-            for (int g = 0; g < kM32Rows; g += kM32CH) {
+                for (int g = 0; g < kM32Rows; g += kM32CH) {
 #pragma unroll
-                for (int u8 = 0; u8 < kM32CH; u8++) {
-                    const int s = t * kM32Rows + g + u8;
-                    const int r = s - lane;
-                    if (left_in_grid && u8 == 0 && (!check || s < NR)) {
-                        // lane 0 enters a chunk of the left column: every row
-                        // of it must have arrived (one entry per lane, one vote)
-                        const int rr = s + (lane & (kM32CH - 1));
-                        bool ok = rr >= NR || m32_entry_is(bnd_p[rr % kM32BndRing], rr);
-                        if (!__all_sync(0xffffffffu, ok)) {
-                            long long polls = 0;
-                            while (!ok && !failed) {
-                                ok = m32_entry_is(bnd[rr % kM32BndRing], rr);
-                                if (!ok && (++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(err)))) {
-                                    failed = true;
-                                    atomicOr(err, 1);
-                                    *quit = 1;
+                    for (int u8 = 0; u8 < kM32CH; u8++) {
+                        const int s = t * kM32Rows + g + u8;
+                        const int r = s - lane;
+                        if (left_in_grid && u8 == 0 && (!check || s < NR)) {
+                            // lane 0 enters a chunk of the left column: every row
+                            // of it must have arrived (one entry per lane, one vote)
+                            const int rr = s + (lane & (kM32CH - 1));
+                            bool ok = rr >= NR || m32_entry_is(bnd_p[rr % kM32BndRing], rr);
+                            if (!__all_sync(0xffffffffu, ok)) {
+                                long long polls = 0;
+                                while (!ok && !failed) {
+                                    ok = m32_entry_is(bnd[rr % kM32BndRing], rr);
+                                    if (!ok && (++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(err)))) {
+                                        failed = true;
+                                        atomicOr(err, 1);
+                                        *quit = 1;
+                                    }
                                 }
                             }
+                            __syncwarp();   // lane 0 reads the entries its neighbours validated
+                            bn = bnd_p[s % kM32BndRing];
+                            // earlier chunks are read: their slots may be refilled (a
+                            // plain store suffices, every value read from them was
+                            // consumed by arithmetic before this store issues, and a
+                            // refill lands at least two chunks behind it)
+                            if (lane == 0) *bnd_used = s / kM32CH;
                         }
-                        __syncwarp();   // lane 0 reads the entries its neighbours validated
-                        bn = bnd_p[s % kM32BndRing];
-                        // earlier chunks are read: their slots may be refilled (a
-                        // plain store suffices, every value read from them was
-                        // consumed by arithmetic before this store issues, and a
-                        // refill lands at least two chunks behind it)
-                        if (lane == 0) *bnd_used = s / kM32CH;
-                    }
-                    const float4 xv = x_n, av = a_n, bv = b_n;
-                    float* const p = cell_ptr(r < 0 ? 0 : r);
-                    // next step's operands (row r + 1), loaded before this step's store
-                    if (!check || (r + 1 >= 0 && r + 1 < NR)) load_next(cell_ptr(r + 1 < 0 ? 0 : r + 1));
-                    float left = __shfl_up_sync(0xffffffffu, o[3], 1);
-                    const float l0 = left_in_grid ? m32_entry_value(bn) : 0.0f;
-                    // next step's entry (same chunk; a new chunk is read after its check)
-                    if (u8 + 1 != kM32CH) bn = bnd_p[(s + 1) % kM32BndRing];
-                    if (lane == 0) left = l0;
-                    if (!check || (r >= 0 && r < NR)) {
-                        float w[4];
+                        const float4 xv = x_n, av = a_n, bv = b_n;
+                        float* const p = cell_ptr(r < 0 ? 0 : r);
+                        // next step's operands (row r + 1), loaded before this step's store
+                        if (!check || (r + 1 >= 0 && r + 1 < NR)) load_next(cell_ptr(r + 1 < 0 ? 0 : r + 1));
+                        float left = __shfl_up_sync(0xffffffffu, o[3], 1);
+                        const float l0 = left_in_grid ? m32_entry_value(bn) : 0.0f;
+                        // next step's entry (same chunk; a new chunk is read after its check)
+                        if (u8 + 1 != kM32CH) bn = bnd_p[(s + 1) % kM32BndRing];
+                        if (lane == 0) left = l0;
+                        if (!check || (r >= 0 && r < NR)) {
+                            float w[4];
 #pragma unroll
-                        for (int m = 0; m < 4; m++) w[m] = fmaf(-m32_get<FWD>(bv, m), o[m], m32_get<FWD>(xv, m));
+                            for (int m = 0; m < 4; m++) w[m] = fmaf(-m32_get<FWD>(bv, m), o[m], m32_get<FWD>(xv, m));
 #pragma unroll
-                        for (int m = 0; m < 4; m++) {
-                            o[m] = fmaf(-m32_get<FWD>(av, m), left, w[m]);
-                            left = o[m];
+                            for (int m = 0; m < 4; m++) {
+                                o[m] = fmaf(-m32_get<FWD>(av, m), left, w[m]);
+                                left = o[m];
+                            }
+                            *reinterpret_cast<float4*>(p) = m32_pack<FWD>(o);
+                            if (publishes && lane == 31) top_p[r % kM32TopRing] = m32_entry(r, o[3]);
                         }
-                        *reinterpret_cast<float4*>(p) = m32_pack<FWD>(o);
-                        if (publishes && lane == 31) top_p[r % kM32TopRing] = m32_entry(r, o[3]);
                     }
                 }
-            }
-        };
+            };
 
-        const int nsteps = NR + 31;
-        for (int t = 0; t * kM32Rows < nsteps; t++) {
-            if (t < nt) wait_tile(t);
-            // last-column ring: do not run more than half a ring ahead of the I/O warp
-            if (publishes && t * kM32Rows - 31 - *top_done > kM32TopRing / 2)
-                spin_ge(top_done, t * kM32Rows - 31 - kM32TopRing / 2);
+            const int nsteps = NR + 31;
+            for (int t = 0; t * kM32Rows < nsteps; t++) {
+                if (t < nt) wait_tile(t);
+                // last-column ring: do not run more than half a ring ahead of the I/O warp
+                if (publishes && t * kM32Rows - 31 - *top_done > kM32TopRing / 2)
+                    spin_ge(top_done, t * kM32Rows - 31 - kM32TopRing / 2);
+                __syncwarp();
+                if (t == 0 || t >= nt)
+                    tile_steps(t, BoolTag<true>{});
+                else
+                    tile_steps(t, BoolTag<false>{});
+                // tile t-1 is finished for every lane: hand it to the I/O warp for its
+                // TMA store; the slot of tile t-2 is reused for tile t+2 once that
+                // tile's store has read it
+                if (t >= 1 && t - 1 < nt) {
+                    fence_async_smem();
+                    __syncwarp();
+                    if (lane == 0) *tiles_done = t;
+                }
+                if (t + 2 < nt) {
+                    if (t >= 2 && *tiles_freed < t - 1) spin_ge(tiles_freed, t - 1);
+                    __syncwarp();
+                    issue(t + 2);
+                }
+            }
             __syncwarp();
-            if (t == 0 || t >= nt)
-                tile_steps(t, BoolTag<true>{});
-            else
-                tile_steps(t, BoolTag<false>{});
-            // tile t-1 is finished for every lane: hand it to the I/O warp for its
-            // TMA store; the slot of tile t-2 is reused for tile t+2 once that
-            // tile's store has read it
-            if (t >= 1 && t - 1 < nt) {
-                fence_async_smem();
-                __syncwarp();
-                if (lane == 0) *tiles_done = t;
+            if (lane == 0) {
+                *tiles_done = nt;
+                if (left_in_grid) *bnd_used = NR / kM32CH + kM32BndChunks;
             }
-            if (t + 2 < nt) {
-                if (t >= 2 && *tiles_freed < t - 1) spin_ge(tiles_freed, t - 1);
-                __syncwarp();
-                issue(t + 2);
+            // a tile whose wait gave up may still be arriving: wait for it (and the
+            // tiles issued after it) once more, so no copy into this CTA's shared
+            // memory is in flight when it moves on or exits
+            for (int t = unconfirmed; t < issued; t++) (void)poll_tile(t);
+        }
+    };
+    // rings and counters of a strip: no row matches, nothing done
+    auto reset_rings = [&]() {
+        if (threadIdx.x == 0) {
+            *bnd_used = 0;
+            *top_done = 0;
+            *quit = 0;
+            *tiles_done = 0;
+            *tiles_freed = 0;
+        }
+        for (int k = threadIdx.x; k < kM32BndRing; k += blockDim.x) bnd[k] = ~0ull;
+        for (int k = threadIdx.x; k < kM32TopRing; k += blockDim.x) top[k] = ~0ull;
+    };
+
+    if (!SEVERAL) {
+        const int strip = blockIdx.x;
+        const int nstrips = a.P32 / kM32Cols;
+        reset_rings();
+        cluster_sync_all();   // every ring and counter of the cluster is initialised
+        if (strip < nstrips) run_strip(strip, nstrips, 0, a.P32, 0, a.NY32, strip);   // the grid is rounded up to whole clusters
+        cluster_sync_all();   // no CTA leaves while a neighbour may still touch its shared memory
+    } else {
+        // persistent: items are taken in order, so an item's previous strip was
+        // taken earlier by a co-resident CTA and every wait makes progress
+        for (;;) {
+            __syncthreads();   // the previous item is finished by both warps
+            if (threadIdx.x == 0) *cur_item = atomicAdd(&a.work[0], 1);
+            reset_rings();
+            __syncthreads();
+            const int it = *cur_item;
+            if (it >= a.nitems) break;
+            const Mic32Item item = a.items[it];
+            if (a.scenes[item.scene].inner->done) continue;   // that scene's inner solve stopped
+            run_strip(item.strip, item.nstrips, item.x0, item.P32, item.y0, item.NY32, it);
+        }
+        if (threadIdx.x == 0) {
+            __threadfence();
+            if (atomicAdd(&a.work[1], 1) == (int)gridDim.x - 1) {   // the last CTA resets the counters
+                a.work[0] = 0;
+                a.work[1] = 0;
+                __threadfence();
             }
         }
-        __syncwarp();
-        if (lane == 0) {
-            *tiles_done = nt;
-            if (left_in_grid) *bnd_used = NR / kM32CH + kM32BndChunks;
-        }
-        // a tile whose wait gave up may still be arriving: wait for it (and the
-        // tiles issued after it) once more, so no copy into this CTA's shared
-        // memory is in flight when it exits
-        for (int t = unconfirmed; t < issued; t++) (void)poll_tile(t);
     }
-    cluster_sync_all();   // no CTA leaves while a neighbour may still touch its shared memory
 }
 
 // Host side: tensor map for one FP32 array of P x NR (row pitch P floats),
@@ -426,51 +492,84 @@ int mic32_make_map(CUtensorMap* map, float* base, int P, int NR);
 // sweeps' worth.
 __global__ void k_wave_bump(unsigned long long* base, unsigned long long n) { *base += n << 24; }
 
-// Launches one sweep: cooperative (every strip co-resident, so the waits
-// between strips always make progress) and, where the device can hold them,
-// in clusters of up to 8 strips that hand columns over in shared memory.
+// Where a pack's kernels go: stream, error word (with the wait controls),
+// launch counter, progress bases, and the handle whose per-kernel timing
+// applies (null: none).
+struct PackLaunch {
+    cudaStream_t stream;
+    int* err;
+    int device;
+    unsigned long long* launches;
+    unsigned long long wave_launch;   // progress base counter of direct sweeps
+    Sim* timer;
+};
+
+// Launches one sweep of every scene of the pack.  One scene: cooperative
+// (every strip co-resident, so the waits between strips always make
+// progress) and, where the device can hold them, in clusters of up to 8
+// strips that hand columns over in shared memory.  Several scenes: a
+// cooperative grid of persistent CTAs (pk->sweep_ctas) over the work items.
 // graph_slot >= 0: for stream capture; the sweep is number graph_slot of the
-// graph_sweeps sweeps of one replay, uses its own progress counters and the
-// device-memory base plus graph_slot sweeps; slot 0 first advances that base
-// by graph_sweeps, so that every replay gets fresh bases.
+// graph_sweeps sweeps of one replay, uses the graph's progress counters and
+// the device-memory base plus graph_slot sweeps; slot 0 first advances that
+// base by graph_sweeps, so that every replay gets fresh bases.
 template <bool FWD>
-int launch_mic32(Sim* s, const Mic32Maps& maps, float* out, const int* skip, int graph_slot = -1,
-                 int graph_sweeps = 0) {
+int launch_mic32(Pack* pk, PackLaunch& L, float* out, int graph_slot = -1, int graph_sweeps = 0) {
     const bool graph = graph_slot >= 0;
-    const int nstrips = s->P32 / kM32Cols;
-    if (nstrips > s->progress_cap) {
-        set_error("mic32: %d strips exceed the %d progress counters", nstrips, s->progress_cap);
+    const bool several = pk->n > 1;
+    const int nstrips = several ? pk->nitems : pk->scenes[0].P32 / kM32Cols;
+    if (nstrips > pk->progress_cap) {
+        set_error("mic32: %d strips exceed the %d progress counters", nstrips, pk->progress_cap);
         return FS2D_ERR_INVALID;
     }
-    static std::atomic<unsigned long long> configured{0};
-    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)mic32_kernel<FWD>, (int)kM32Smem)) return rc0;
-    unsigned long long base = 0;
-    const unsigned long long* base_dev = nullptr;
-    unsigned long long* progress = s->progress;
+    const void* fn = several ? (const void*)mic32_kernel<FWD, true> : (const void*)mic32_kernel<FWD, false>;
+    static std::atomic<unsigned long long> configured[2] = {{0}, {0}};
+    if (int rc0 = ensure_smem_attr(configured[several ? 1 : 0], L.device, fn, (int)kM32Smem)) return rc0;
+    Mic32Args a{};
+    a.out = out;
+    a.pitch = pk->pitch;
+    a.P32 = pk->scenes[0].P32;
+    a.NY32 = pk->scenes[0].NY32;
+    a.skip = several ? nullptr : &pk->scenes[0].inner->done;
+    a.items = pk->d_items;
+    a.nitems = pk->nitems;
+    a.scenes = pk->d_scenes;
+    a.work = pk->d_ctl + 2;
+    a.err = L.err;
     if (graph) {
-        if (graph_slot == 0) FS2D_LAUNCH(s, k_wave_bump, 1, 1, 0, s->m32_gbase, (unsigned long long)graph_sweeps);
-        base = (unsigned long long)graph_slot << 24;
-        base_dev = s->m32_gbase;
-        progress = s->m32_gprogress;
+        if (graph_slot == 0) {
+            (*L.launches)++;
+            k_wave_bump<<<1, 1, 0, L.stream>>>(pk->gbase, (unsigned long long)graph_sweeps);
+            if (int rc1 = check_cuda(cudaGetLastError(), "k_wave_bump")) return rc1;
+        }
+        a.base_host = (unsigned long long)graph_slot << 24;
+        a.base_dev = pk->gbase;
+        a.progress = pk->gprogress;
     } else {
-        base = wave_begin(s);
+        a.base_host = (++L.wave_launch) << 24;
+        a.base_dev = nullptr;
+        a.progress = pk->progress;
     }
-    int P = s->P32, NR = s->NY32;
-    void* args[] = {(void*)&maps, (void*)&out, (void*)&P, (void*)&NR, (void*)&progress, (void*)&base,
-                    (void*)&base_dev, (void*)&s->err, (void*)&skip};
-    s->launches++;
+    const Mic32Maps& maps = *reinterpret_cast<const Mic32Maps*>(FWD ? pk->maps->fwd : pk->maps->bwd);
+    void* args[] = {(void*)&maps, (void*)&a};
+    (*L.launches)++;
     const char* name = FWD ? "mic32_forward" : "mic32_backward";
-    long long kt = ktimer_begin(s, name);
-    int& cs = s->m32_cluster;   // 0: not chosen yet
-    if (cs == 0) cs = choose_cluster((const void*)mic32_kernel<FWD>, nstrips, 64, kM32Smem);
-    cudaError_t e = launch_clustered((const void*)mic32_kernel<FWD>, nstrips, cs, 64, kM32Smem, s->stream, args);
-    if (e != cudaSuccess && cs > 1 && !graph) {   // clusters refused: plain cooperative launch
-        (void)cudaGetLastError();
-        cs = 1;
-        e = launch_clustered((const void*)mic32_kernel<FWD>, nstrips, 1, 64, kM32Smem, s->stream, args);
+    long long kt = L.timer ? ktimer_begin(L.timer, name) : -1;
+    cudaError_t e;
+    if (several) {
+        e = launch_clustered(fn, pk->sweep_ctas, 1, 64, kM32Smem, L.stream, args);
+    } else {
+        int& cs = pk->cluster;   // 0: not chosen yet
+        if (cs == 0) cs = choose_cluster(fn, nstrips, 64, kM32Smem);
+        e = launch_clustered(fn, nstrips, cs, 64, kM32Smem, L.stream, args);
+        if (e != cudaSuccess && cs > 1 && !graph) {   // clusters refused: plain cooperative launch
+            (void)cudaGetLastError();
+            cs = 1;
+            e = launch_clustered(fn, nstrips, 1, 64, kM32Smem, L.stream, args);
+        }
     }
     int rc = check_cuda(e, name);
-    ktimer_end(s, kt);
+    if (L.timer) ktimer_end(L.timer, kt);
     return rc;
 }
 

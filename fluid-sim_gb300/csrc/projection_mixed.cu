@@ -20,6 +20,8 @@
 #include <math.h>
 #include <string.h>
 #include <algorithm>
+#include <numeric>
+#include <vector>
 #include <cudaTypedefs.h>
 #include "fs2d_device.cuh"
 #include "wave2.cuh"
@@ -114,69 +116,96 @@ __global__ void k_mixed_coef(const float* __restrict__ ax, const float* __restri
     fd[k] = ay[k] * p2;
 }
 
-// FP64 residual r = b - A p on fluid cells (the SpMV of :433-444 in FP64),
-// ||r||inf into the outer scalars.
-__global__ void k_resid64(const uint8_t* __restrict__ cell, const double* __restrict__ A0,
-                          const double* __restrict__ Ax, const double* __restrict__ Ay, const double* __restrict__ rhs,
-                          const double* __restrict__ p, double* r, int NX, size_t N, double* partial,
-                          PcgScalars* outer) {
-    __shared__ double sh[32];
-    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    double m = 0;
-    if (c < N) {
-        double v = 0.0;
-        if (cell[c] == kFluid) {
-            double ap = A0[c] * p[c] + Ax[c - 1] * p[c - 1] + Ax[c] * p[c + 1] + Ay[c - NX] * p[c - NX] +
-                        Ay[c] * p[c + NX];
-            v = rhs[c] - ap;
-        }
-        r[c] = v;
-        m = fabs(v);
-    }
-    m = block_max(m, sh);
-    if (threadIdx.x == 0) partial[blockIdx.x] = m;
-    if (last_block(&outer->ticket[0])) {
-        double mm = 0;
-        for (size_t k = threadIdx.x; k < gridDim.x; k += blockDim.x) mm = fmax(mm, partial[k]);
-        mm = block_max(mm, sh);
-        if (threadIdx.x == 0) outer->r_norm = mm;
-    }
+// ---- the refinement loop over the scenes of a pack ----
+// Every kernel below covers every scene of a pack in one launch: block b
+// belongs to scene blk[b] and is block b - blk0 (FP32 reductions) or
+// b - blk64 (FP64 refinement) of that scene.  A scene's blocks and their
+// order are those of the scene alone, so a scene's results do not depend on
+// the other scenes of the pack.
+
+// Start of a solve: per scene, the refinement stops at once when there is
+// nothing to solve (||b||inf <= 1e-12) or the zero start already meets the
+// tolerance; ctl[1] counts the scenes still refining.  One thread per scene.
+__global__ void k_outer_start(const PackScene* __restrict__ sc, int n, int* ctl) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    PcgScalars* o = sc[k].outer;
+    o->outer_iters = 0;
+    o->inner_total = 0;
+    o->outer_done = (o->rhs_norm > 1e-12 && o->r_norm > o->tol_abs) ? 0 : 1;
+    sc[k].inner->done = 1;
+    sc[k].inner->active = 0;
+    if (!o->outer_done) atomicAdd(&ctl[1], 1);
 }
 
-// Start of an inner solve: r32 = r64 / ||r64||inf, r*pc^2, e = 0, scalars reset.
-__global__ void k_inner_init(const double* __restrict__ r64, const PcgScalars* __restrict__ outer,
-                             const float* __restrict__ pc, float* r32, float* rp32, float* e32, int NX, int P,
-                             size_t N, PcgScalars* inner, double inner_tol) {
-    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+// Start of an inner solve: r32 = r64 / ||r64||inf, r*pc^2, e = 0, scalars
+// reset; the inner tolerance is the reduction the FP64 target still needs
+// (with a factor 2 of margin for the FP32 recurrence), never tighter than
+// inner_tol_min.  Scenes whose refinement stopped are marked inactive.
+__global__ void k_inner_init(const PackScene* __restrict__ sc, const int* __restrict__ blk, int pitch,
+                             const float* __restrict__ pc, float* r32, float* rp32, float* e32, double inner_tol_min,
+                             int* ctl) {
+    const PackScene& S = sc[blk[blockIdx.x]];
+    const PcgScalars* outer = S.outer;
+    if (outer->outer_done) return;
+    const int lb = blockIdx.x - S.blk64;
+    const size_t N = (size_t)S.NX * S.NY;
+    const size_t c = (size_t)lb * blockDim.x + threadIdx.x;
     const double rn = outer->r_norm;
     const double scale = rn > 0 ? 1.0 / rn : 0.0;
     if (c < N) {
-        size_t k = (c / NX) * (size_t)P + (c % NX);
-        float rv = (float)(r64[c] * scale);
-        float p = pc[k];
+        const size_t k = (size_t)S.off + (c / S.NX) * (size_t)pitch + (c % S.NX);
+        const float rv = (float)(S.r[c] * scale);
+        const float p = pc[k];
         r32[k] = rv;
         rp32[k] = rv * (p * p);
         e32[k] = 0.0f;
     }
-    if (c == 0) {
+    if (lb == 0 && threadIdx.x == 0) {
+        PcgScalars* inner = S.inner;
         inner->iter = 0;
         inner->done = (rn > 0) ? 0 : 1;
         inner->first = 1;
         inner->sigma = inner->alpha = inner->beta = 0;
         inner->rhs_norm = 1.0;
         inner->r_norm = 1.0;
-        inner->tol_abs = inner_tol;   // read by k_axpy32 (device memory, so a captured loop can replay it)
+        inner->tol_abs = fmax(inner_tol_min, 0.5 * outer->tol_abs / rn);   // read by k_axpy32
+        inner->active = 1;
+        if (!inner->done) atomicAdd(&ctl[0], 1);
     }
 }
 
+// Inner solve stops (first time only): one scene fewer running.
+__device__ __forceinline__ void inner_stop(PcgScalars* pcg, int how, int* ctl) {
+    if (pcg->done == 0) {
+        pcg->done = how;
+        atomicSub(&ctl[0], 1);
+    }
+}
+
+// Last-block-done over the `nblocks` blocks of one scene.
+__device__ __forceinline__ bool last_block_of(unsigned int* ticket, unsigned nblocks) {
+    __shared__ bool is_last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        is_last = (t == nblocks - 1);
+        if (is_last) *ticket = 0;
+    }
+    __syncthreads();
+    if (is_last) __threadfence();
+    return is_last;
+}
+
 // ---- inner FP32 PCG kernels ----
-// Row-segment layout: block (bx, by) covers columns bx*kRT .. bx*kRT+kRT-1
-// of rows by, by + gridDim.y, ...; sums are accumulated and reduced in
-// double-float (FP32 pairs), in a fixed order (deterministic), and the
-// last block finishes the scalar.
+// Row-segment layout: block (bx, by) of a scene covers columns
+// bx*kRT .. bx*kRT+kRT-1 of rows by, by + gy, ...; sums are accumulated and
+// reduced in double-float (FP32 pairs), in a fixed order (deterministic), and
+// the scene's last block finishes its scalar.
 constexpr int kRT = 256;
 
-__device__ __forceinline__ void df_block_partial(DF v, float2* partial, float2* sh) {
+__device__ __forceinline__ void df_block_partial(DF v, float2* partial, int slot, float2* sh) {
     v = df_warp_sum(v);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     __syncthreads();
@@ -185,11 +214,11 @@ __device__ __forceinline__ void df_block_partial(DF v, float2* partial, float2* 
     if (wid == 0) {
         DF t = lane < nw ? DF{sh[lane].x, sh[lane].y} : DF{0.f, 0.f};
         t = df_warp_sum(t);
-        if (lane == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = make_float2(t.hi, t.lo);
+        if (lane == 0) partial[slot] = make_float2(t.hi, t.lo);
     }
 }
 
-// Sum of the partials of every block (called by the last block).
+// Sum of the partials of every block of a scene (called by its last block).
 __device__ __forceinline__ double df_final(const float2* partial, int n, float2* sh) {
     DF acc{0.f, 0.f};
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
@@ -219,23 +248,27 @@ __device__ __forceinline__ float block_max_f(float v, float* sh) {
     return v;
 }
 
-__global__ void __launch_bounds__(kRT) k_dot32(const float* __restrict__ z, const float* __restrict__ r, int NX,
-                                               int NY, int P, float2* partial, PcgScalars* pcg, int init,
-                                               int max_iters) {
+__global__ void __launch_bounds__(kRT) k_dot32(const PackScene* __restrict__ sc, const int* __restrict__ blk,
+                                               int pitch, const float* __restrict__ z, const float* __restrict__ r,
+                                               int init, int max_iters, int* ctl) {
     __shared__ float2 sh[32];
+    const PackScene& S = sc[blk[blockIdx.x]];
+    PcgScalars* pcg = S.inner;
     if (pcg->done) return;
-    const int i = blockIdx.x * kRT + threadIdx.x;
+    const int lb = blockIdx.x - S.blk0;
+    const int bx = lb % S.gx, by = lb / S.gx;
+    const int i = bx * kRT + threadIdx.x;
     DF a{0.f, 0.f};
-    if (i < NX) {
+    if (i < S.NX) {
 #pragma unroll 4
-        for (int j = blockIdx.y; j < NY; j += gridDim.y) {
-            const size_t k = (size_t)j * P + i;
+        for (int j = by; j < S.NY; j += S.gy) {
+            const size_t k = (size_t)S.off + (size_t)j * pitch + i;
             df_add(a, df_prod(z[k], r[k]));
         }
     }
-    df_block_partial(a, partial, sh);
-    if (last_block(&pcg->ticket[1])) {
-        const double s = df_final(partial, gridDim.x * gridDim.y, sh);
+    df_block_partial(a, S.part, by * S.gx + bx, sh);
+    if (last_block_of(&pcg->ticket[1], S.gx * S.gy)) {
+        const double s = df_final(S.part, S.gx * S.gy, sh);
         if (threadIdx.x == 0) {
             if (init) {
                 pcg->sigma = s;
@@ -244,7 +277,7 @@ __global__ void __launch_bounds__(kRT) k_dot32(const float* __restrict__ z, cons
                 pcg->sigma = s;
                 pcg->iter += 1;
                 pcg->first = 0;
-                if (pcg->iter >= max_iters) pcg->done = 2;
+                if (pcg->iter >= max_iters) inner_stop(pcg, 2, ctl);
             }
         }
     }
@@ -252,39 +285,43 @@ __global__ void __launch_bounds__(kRT) k_dot32(const float* __restrict__ z, cons
 
 // s_new = z + beta s_old (z on the first iteration), w = A s_new on fluid
 // cells, alpha = sigma / (w . s_new).
-__global__ void __launch_bounds__(kRT) k_spmv32(const uint8_t* __restrict__ cell, const float* __restrict__ a0,
-                                                const float* __restrict__ ax, const float* __restrict__ ay,
-                                                const float* __restrict__ z, const float* __restrict__ s_old,
-                                                float* s_new, float* w, int NX, int NY, int P, float2* partial,
-                                                PcgScalars* pcg) {
+__global__ void __launch_bounds__(kRT) k_spmv32(const PackScene* __restrict__ sc, const int* __restrict__ blk,
+                                                int pitch, const float* __restrict__ a0, const float* __restrict__ ax,
+                                                const float* __restrict__ ay, const float* __restrict__ z,
+                                                const float* __restrict__ s_old, float* s_new, float* w, int* ctl) {
     __shared__ float2 sh[32];
+    const PackScene& S = sc[blk[blockIdx.x]];
+    PcgScalars* pcg = S.inner;
     if (pcg->done) return;
     const bool first = pcg->first != 0;
     const float beta = (float)pcg->beta;
-    const int i = blockIdx.x * kRT + threadIdx.x;
+    const int lb = blockIdx.x - S.blk0;
+    const int bx = lb % S.gx, by = lb / S.gx;
+    const int i = bx * kRT + threadIdx.x;
+    const int P = pitch;
     DF a{0.f, 0.f};
-    if (i < NX) {
-        for (int j = blockIdx.y; j < NY; j += gridDim.y) {
-            const size_t k = (size_t)j * P + i;
-            const float sc = first ? z[k] : fmaf(beta, s_old[k], z[k]);
-            s_new[k] = sc;
+    if (i < S.NX) {
+        for (int j = by; j < S.NY; j += S.gy) {
+            const size_t k = (size_t)S.off + (size_t)j * P + i;
+            const float sc0 = first ? z[k] : fmaf(beta, s_old[k], z[k]);
+            s_new[k] = sc0;
             float out = 0.0f;
-            if (cell[(size_t)j * NX + i] == kFluid) {
+            if (S.cell[(size_t)j * S.NX + i] == kFluid) {
                 const float sl = first ? z[k - 1] : fmaf(beta, s_old[k - 1], z[k - 1]);
                 const float sr = first ? z[k + 1] : fmaf(beta, s_old[k + 1], z[k + 1]);
                 const float sd = first ? z[k - P] : fmaf(beta, s_old[k - P], z[k - P]);
                 const float su = first ? z[k + P] : fmaf(beta, s_old[k + P], z[k + P]);
-                out = a0[k] * sc + ax[k - 1] * sl + ax[k] * sr + ay[k - P] * sd + ay[k] * su;
+                out = a0[k] * sc0 + ax[k - 1] * sl + ax[k] * sr + ay[k - P] * sd + ay[k] * su;
             }
             w[k] = out;
-            df_add(a, df_prod(out, sc));
+            df_add(a, df_prod(out, sc0));
         }
     }
-    df_block_partial(a, partial, sh);
-    if (last_block(&pcg->ticket[2])) {
-        const double sum = df_final(partial, gridDim.x * gridDim.y, sh);
+    df_block_partial(a, S.part, by * S.gx + bx, sh);
+    if (last_block_of(&pcg->ticket[2], S.gx * S.gy)) {
+        const double sum = df_final(S.part, S.gx * S.gy, sh);
         if (threadIdx.x == 0) {
-            if (sum == 0.0) pcg->done = 1;
+            if (sum == 0.0) inner_stop(pcg, 1, ctl);
             else pcg->alpha = pcg->sigma / sum;
         }
     }
@@ -292,18 +329,22 @@ __global__ void __launch_bounds__(kRT) k_spmv32(const uint8_t* __restrict__ cell
 
 // e += alpha s, r -= alpha w, rp = r pc^2, ||r||inf (stop when below the
 // inner tolerance, pcg->tol_abs).
-__global__ void __launch_bounds__(kRT) k_axpy32(float* e, float* r, float* rp, const float* __restrict__ pc,
-                                                const float* __restrict__ s, const float* __restrict__ w, int NX,
-                                                int NY, int P, float* partial, PcgScalars* pcg) {
+__global__ void __launch_bounds__(kRT) k_axpy32(const PackScene* __restrict__ sc, const int* __restrict__ blk,
+                                                int pitch, float* e, float* r, float* rp, const float* __restrict__ pc,
+                                                const float* __restrict__ s, const float* __restrict__ w, int* ctl) {
     __shared__ float sh[32];
+    const PackScene& S = sc[blk[blockIdx.x]];
+    PcgScalars* pcg = S.inner;
     if (pcg->done) return;
     const float alpha = (float)pcg->alpha;
-    const int i = blockIdx.x * kRT + threadIdx.x;
+    const int lb = blockIdx.x - S.blk0;
+    const int bx = lb % S.gx, by = lb / S.gx;
+    const int i = bx * kRT + threadIdx.x;
     float m = 0.f;
-    if (i < NX) {
+    if (i < S.NX) {
 #pragma unroll 2
-        for (int j = blockIdx.y; j < NY; j += gridDim.y) {
-            const size_t k = (size_t)j * P + i;
+        for (int j = by; j < S.NY; j += S.gy) {
+            const size_t k = (size_t)S.off + (size_t)j * pitch + i;
             e[k] = fmaf(alpha, s[k], e[k]);
             const float rv = fmaf(-alpha, w[k], r[k]);
             r[k] = rv;
@@ -313,24 +354,94 @@ __global__ void __launch_bounds__(kRT) k_axpy32(float* e, float* r, float* rp, c
         }
     }
     m = block_max_f(m, sh);
-    if (threadIdx.x == 0) partial[blockIdx.y * gridDim.x + blockIdx.x] = m;
-    if (last_block(&pcg->ticket[3])) {
+    float* partf = reinterpret_cast<float*>(S.part);
+    if (threadIdx.x == 0) partf[by * S.gx + bx] = m;
+    if (last_block_of(&pcg->ticket[3], S.gx * S.gy)) {
         float mm = 0.f;
-        for (int k = threadIdx.x; k < (int)(gridDim.x * gridDim.y); k += blockDim.x) mm = fmaxf(mm, partial[k]);
+        for (int k = threadIdx.x; k < S.gx * S.gy; k += blockDim.x) mm = fmaxf(mm, partf[k]);
         mm = block_max_f(mm, sh);
         if (threadIdx.x == 0) {
             pcg->r_norm = mm;
-            if (mm <= pcg->tol_abs) pcg->done = 1;
+            if (mm <= pcg->tol_abs) inner_stop(pcg, 1, ctl);
         }
     }
 }
 
-// p += e * ||r||inf (undo the inner scaling) in FP64.
-__global__ void k_update64(double* p, const float* __restrict__ e, const PcgScalars* __restrict__ outer, int NX, int P,
-                           size_t N) {
-    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (c < N) p[c] = p[c] + (double)e[(c / NX) * (size_t)P + (c % NX)] * outer->r_norm;
+// End of an inner solve: p += e * ||r||inf (undo the inner scaling) in FP64.
+__global__ void k_update64(const PackScene* __restrict__ sc, const int* __restrict__ blk, int pitch,
+                           const float* __restrict__ e) {
+    const PackScene& S = sc[blk[blockIdx.x]];
+    if (!S.inner->active) return;
+    const size_t N = (size_t)S.NX * S.NY;
+    const size_t c = (size_t)(blockIdx.x - S.blk64) * blockDim.x + threadIdx.x;
+    if (c < N) S.p[c] = S.p[c] + (double)e[(size_t)S.off + (c / S.NX) * (size_t)pitch + (c % S.NX)] * S.outer->r_norm;
 }
+
+// FP64 residual r = b - A p on fluid cells (the SpMV of :433-444 in FP64) and
+// its norm; the scene's last block counts the sweep and ends the refinement
+// when the reference's test ||r||inf <= tol * ||b||inf holds or the sweep cap
+// is reached.
+__global__ void k_resid64(const PackScene* __restrict__ sc, const int* __restrict__ blk, int max_outer, int* ctl) {
+    __shared__ double sh[32];
+    const PackScene& S = sc[blk[blockIdx.x]];
+    PcgScalars* inner = S.inner;
+    if (!inner->active) return;
+    const int NX = S.NX;
+    const size_t N = (size_t)NX * S.NY;
+    const int lb = blockIdx.x - S.blk64;
+    const size_t c = (size_t)lb * blockDim.x + threadIdx.x;
+    double m = 0;
+    if (c < N) {
+        double v = 0.0;
+        if (S.cell[c] == kFluid) {
+            const double* A0 = S.A0;
+            const double* Ax = S.Ax;
+            const double* Ay = S.Ay;
+            const double* p = S.p;
+            double ap = A0[c] * p[c] + Ax[c - 1] * p[c - 1] + Ax[c] * p[c + 1] + Ay[c - NX] * p[c - NX] +
+                        Ay[c] * p[c + NX];
+            v = S.rhs[c] - ap;
+        }
+        S.r[c] = v;
+        m = fabs(v);
+    }
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) S.part64[lb] = m;
+    PcgScalars* outer = S.outer;
+    if (last_block_of(&outer->ticket[0], S.nb64)) {
+        double mm = 0;
+        for (int k = threadIdx.x; k < S.nb64; k += blockDim.x) mm = fmax(mm, S.part64[k]);
+        mm = block_max(mm, sh);
+        if (threadIdx.x == 0) {
+            outer->r_norm = mm;
+            outer->outer_iters += 1;
+            outer->inner_total += inner->iter;
+            inner->active = 0;
+            if (mm <= outer->tol_abs || outer->outer_iters >= max_outer) {
+                outer->outer_done = 1;
+                atomicSub(&ctl[1], 1);
+            }
+        }
+    }
+}
+
+#define PK_LAUNCH_PLAIN(stream, kernel, grid, block, ...)                      \
+    do {                                                                        \
+        kernel<<<(grid), (block), 0, (stream)>>>(__VA_ARGS__);                  \
+        int _rc = ::fs2d::check_cuda(cudaGetLastError(), #kernel);              \
+        if (_rc) return _rc;                                                    \
+    } while (0)
+
+// A launch of a pack's kernel: counted, timed when asked, errors reported.
+#define PK_LAUNCH(L, kernel, grid, block, ...)                                  \
+    do {                                                                        \
+        (*(L).launches)++;                                                      \
+        long long _kt = (L).timer ? ::fs2d::ktimer_begin((L).timer, #kernel) : -1; \
+        kernel<<<(grid), (block), 0, (L).stream>>>(__VA_ARGS__);               \
+        if ((L).timer) ::fs2d::ktimer_end((L).timer, _kt);                      \
+        int _rc = ::fs2d::check_cuda(cudaGetLastError(), #kernel);              \
+        if (_rc) return _rc;                                                    \
+    } while (0)
 
 }  // namespace
 
@@ -340,181 +451,513 @@ int mic32_make_map(CUtensorMap* map, float* base, int P, int NR) {
 
 static_assert(sizeof(Mic32Maps) <= sizeof(Mic32MapsHost::fwd), "tensor map storage");
 
-// Tensor maps of the FP32 MIC(0) sweeps, built once per handle.
-int mixed_setup_maps(Sim* s) {
-    Mixed32& m = s->m32;
+namespace {
+
+// Tensor maps of the FP32 MIC(0) sweeps over the pack's arrays.
+int pack_setup_maps(Pack* pk) {
+    Mixed32& m = pk->m;
     Mic32Maps f{}, b{};
     int rc = 0;
     float* fin[3] = {m.rp, m.fa, m.fb};
     float* bin[3] = {m.q, m.fc, m.fd};
-    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&f.in[a], fin[a], s->P32, s->NY32);
-    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&b.in[a], bin[a], s->P32, s->NY32);
-    if (!rc) rc = mic32_make_map(&f.out, m.q, s->P32, s->NY32);
-    if (!rc) rc = mic32_make_map(&b.out, m.z, s->P32, s->NY32);
+    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&f.in[a], fin[a], pk->pitch, pk->rows);
+    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&b.in[a], bin[a], pk->pitch, pk->rows);
+    if (!rc) rc = mic32_make_map(&f.out, m.q, pk->pitch, pk->rows);
+    if (!rc) rc = mic32_make_map(&b.out, m.z, pk->pitch, pk->rows);
     if (rc) return rc;
-    memcpy(s->m32maps->fwd, &f, sizeof(f));
-    memcpy(s->m32maps->bwd, &b, sizeof(b));
+    memcpy(pk->maps->fwd, &f, sizeof(f));
+    memcpy(pk->maps->bwd, &b, sizeof(b));
+    return 0;
+}
+
+template <typename T>
+int dev_alloc(T** p, size_t n) {
+    *p = nullptr;
+    cudaError_t e = cudaMalloc((void**)p, (n ? n : 1) * sizeof(T));
+    if (e != cudaSuccess) {
+        set_error("cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
+        return FS2D_ERR_ALLOC;
+    }
+    return check_cuda(cudaMemset(*p, 0, (n ? n : 1) * sizeof(T)), "cudaMemset");
+}
+
+// The sixteen FP32 arrays of a Mixed32.
+void mixed_array_slots(Mixed32& m, float** f[16]) {
+    float** g[16] = {&m.a0, &m.ax, &m.ay, &m.pc, &m.fa, &m.fb, &m.fc, &m.fd,
+                     &m.r,  &m.rp, &m.q,  &m.z,  &m.w,  &m.s0, &m.s1, &m.e};
+    for (int k = 0; k < 16; k++) f[k] = g[k];
+}
+
+// Scene table entry of a handle placed at pack column x0, row y0.
+PackScene scene_entry(Sim* s, int pitch, int x0, int y0) {
+    PackScene e{};
+    e.NX = s->NX;
+    e.NY = s->NY;
+    e.P32 = (s->NX + kM32Cols - 1) / kM32Cols * kM32Cols;
+    e.NY32 = (s->NY + kM32Rows - 1) / kM32Rows * kM32Rows;
+    e.x0 = x0;
+    e.y0 = y0;
+    e.off = (long long)y0 * pitch + x0;
+    e.gx = (s->NX + kRT - 1) / kRT;
+    e.gy = std::max(1, std::min(s->NY, 1216 / e.gx));
+    e.nb64 = (int)blocks_for(s->N, kT);
+    e.cell = s->cell;
+    e.A0 = s->Adiag;
+    e.Ax = s->Ax;
+    e.Ay = s->Ay;
+    e.rhs = s->rhs;
+    e.p = s->p;
+    e.r = s->r;
+    e.outer = s->pcg;
+    e.inner = s->pcg32;
+    e.part = nullptr;     // the pack's own partials, placed by pack_finish
+    e.part64 = nullptr;
+    return e;
+}
+
+// Every scene's region lies inside the pack's arrays and every pointer the
+// kernels follow is set (checked on the host before anything is launched).
+int pack_check(const Pack* pk) {
+    if (pk->pitch % kM32Cols || pk->rows % kM32Rows || pk->n != (int)pk->scenes.size()) {
+        set_error("pack: pitch %d / rows %d not whole strips and tiles", pk->pitch, pk->rows);
+        return FS2D_ERR_INVALID;
+    }
+    for (int k = 0; k < pk->n; k++) {
+        const PackScene& e = pk->scenes[k];
+        const bool inside = e.x0 >= 0 && e.y0 >= 0 && e.x0 % kM32Cols == 0 && e.P32 >= e.NX && e.NY32 >= e.NY &&
+                            e.P32 % kM32Cols == 0 && e.NY32 % kM32Rows == 0 && e.x0 + e.P32 <= pk->pitch &&
+                            e.y0 + e.NY32 <= pk->rows && e.off == (long long)e.y0 * pk->pitch + e.x0;
+        const bool set = e.cell && e.A0 && e.Ax && e.Ay && e.rhs && e.p && e.r && e.outer && e.inner && e.part &&
+                         e.part64 && e.gx >= 1 && e.gy >= 1 && e.nb64 >= 1;
+        if (!inside || !set) {
+            set_error("pack: scene %d (%d x %d at %d, %d) does not fit the %d x %d arrays or lacks an array", k,
+                      e.NX, e.NY, e.x0, e.y0, pk->pitch, pk->rows);
+            return FS2D_ERR_INVALID;
+        }
+    }
+    const Mixed32& m = pk->m;
+    const float* arr[16] = {m.a0, m.ax, m.ay, m.pc, m.fa, m.fb, m.fc, m.fd, m.r, m.rp, m.q, m.z, m.w, m.s0, m.s1, m.e};
+    for (const float* a : arr)
+        if (!a) {
+            set_error("pack: FP32 array missing");
+            return FS2D_ERR_INVALID;
+        }
+    return 0;
+}
+
+// Block maps, work items and device copies of a pack's scene table.
+int pack_finish(Pack* pk) {
+    std::vector<int> blk, blk64;
+    std::vector<Mic32Item> items;
+    for (int k = 0; k < pk->n; k++) {
+        PackScene& e = pk->scenes[k];
+        e.blk0 = (int)blk.size();
+        blk.insert(blk.end(), (size_t)e.gx * e.gy, k);
+        e.blk64 = (int)blk64.size();
+        blk64.insert(blk64.end(), (size_t)e.nb64, k);
+        const int ns = e.P32 / kM32Cols;
+        for (int st = 0; st < ns; st++) items.push_back(Mic32Item{k, st, ns, e.x0, e.P32, e.y0, e.NY32});
+    }
+    pk->nblk = (int)blk.size();
+    pk->nblk64 = (int)blk64.size();
+    pk->nitems = (int)items.size();
+    pk->progress_cap = std::max(pk->nitems, 1);
+    int rc = 0;
+    // reduction partials of every scene: its FP32 blocks' slots from blk0, its
+    // FP64 blocks' from blk64, in buffers the pack owns
+    if (!rc) rc = dev_alloc(&pk->part, (size_t)pk->nblk);
+    if (!rc) rc = dev_alloc(&pk->part64, (size_t)pk->nblk64);
+    if (rc) return rc;
+    for (PackScene& e : pk->scenes) {
+        e.part = pk->part + e.blk0;
+        e.part64 = pk->part64 + e.blk64;
+    }
+    if ((rc = pack_check(pk))) return rc;
+    if (!rc) rc = dev_alloc(&pk->d_scenes, pk->scenes.size());
+    if (!rc) rc = dev_alloc(&pk->d_blk, blk.size());
+    if (!rc) rc = dev_alloc(&pk->d_blk64, blk64.size());
+    if (!rc) rc = dev_alloc(&pk->d_items, items.size());
+    if (!rc) rc = dev_alloc(&pk->d_ctl, 8);
+    if (!rc) rc = dev_alloc(&pk->progress, (size_t)pk->progress_cap);
+    if (!rc) rc = dev_alloc(&pk->gprogress, (size_t)pk->progress_cap);
+    if (!rc) rc = dev_alloc(&pk->gbase, 1);
+    if (rc) return rc;
+    FS2D_CUDA(cudaMemcpy(pk->d_scenes, pk->scenes.data(), pk->scenes.size() * sizeof(PackScene),
+                         cudaMemcpyHostToDevice));
+    FS2D_CUDA(cudaMemcpy(pk->d_blk, blk.data(), blk.size() * sizeof(int), cudaMemcpyHostToDevice));
+    FS2D_CUDA(cudaMemcpy(pk->d_blk64, blk64.data(), blk64.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (!items.empty())
+        FS2D_CUDA(cudaMemcpy(pk->d_items, items.data(), items.size() * sizeof(Mic32Item), cudaMemcpyHostToDevice));
+    FS2D_CUDA(cudaMallocHost((void**)&pk->h_ctl, 8 * sizeof(int)));
+    memset(pk->h_ctl, 0, 8 * sizeof(int));
+    pk->maps = new (std::nothrow) Mic32MapsHost();
+    if (!pk->maps) {
+        set_error("out of host memory");
+        return FS2D_ERR_ALLOC;
+    }
+    return pack_setup_maps(pk);
+}
+
+}  // namespace
+
+void pack_free(Pack* pk) {
+    if (!pk) return;
+    if (pk->graph) cudaGraphExecDestroy(pk->graph);
+    if (pk->owns_arrays) {
+        float** f[16];
+        mixed_array_slots(pk->m, f);
+        for (int k = 0; k < 16; k++)
+            if (*f[k]) cudaFree(*f[k]);
+    }
+    void* ptrs[] = {pk->d_scenes, pk->d_blk, pk->d_blk64, pk->d_items, pk->d_ctl, pk->progress, pk->gprogress,
+                    pk->gbase, pk->part, pk->part64};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    if (pk->h_ctl) cudaFreeHost(pk->h_ctl);
+    delete pk->maps;
+    delete pk;
+}
+
+int pack_create_single(Sim* s) {
+    Pack* pk = new (std::nothrow) Pack();
+    if (!pk) {
+        set_error("out of host memory");
+        return FS2D_ERR_ALLOC;
+    }
+    pk->n = 1;
+    pk->pitch = s->P32;
+    pk->rows = s->NY32;
+    pk->m = s->m32;
+    pk->owns_arrays = false;
+    pk->scenes.push_back(scene_entry(s, s->P32, 0, 0));
+    int rc = pack_finish(pk);
+    if (rc) {
+        pack_free(pk);
+        return rc;
+    }
+    s->pack = pk;
+    return 0;
+}
+
+// Shelf packing: scenes by decreasing padded height, left to right on
+// shelves of a common width (a multiple of 128 columns, at least the widest
+// scene and about the square root of the total area), a new shelf when the
+// next scene does not fit.
+int pack_create_batch(Sim* const* sims, int n, Pack** out) {
+    *out = nullptr;
+    std::vector<int> order(n);
+    long long area = 0;
+    int wmax = 0;
+    for (int k = 0; k < n; k++) {
+        order[k] = k;
+        const int w = (sims[k]->NX + kM32Cols - 1) / kM32Cols * kM32Cols;
+        const int h = (sims[k]->NY + kM32Rows - 1) / kM32Rows * kM32Rows;
+        area += (long long)w * h;
+        wmax = std::max(wmax, w);
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return sims[a]->NY > sims[b]->NY; });
+    int width = (int)std::sqrt((double)area);
+    width = std::max(wmax, (width + kM32Cols - 1) / kM32Cols * kM32Cols);
+    std::vector<int> x0(n), y0(n);
+    int x = 0, y = 0, shelf_h = 0;
+    for (int k : order) {
+        const int w = (sims[k]->NX + kM32Cols - 1) / kM32Cols * kM32Cols;
+        const int h = (sims[k]->NY + kM32Rows - 1) / kM32Rows * kM32Rows;
+        if (x + w > width) {
+            y += shelf_h;
+            x = 0;
+            shelf_h = 0;
+        }
+        x0[k] = x;
+        y0[k] = y;
+        x += w;
+        shelf_h = std::max(shelf_h, h);
+    }
+    const int rows = y + shelf_h;
+    Pack* pk = new (std::nothrow) Pack();
+    if (!pk) {
+        set_error("out of host memory");
+        return FS2D_ERR_ALLOC;
+    }
+    pk->n = n;
+    pk->pitch = width;
+    pk->rows = rows;
+    pk->owns_arrays = true;
+    float** f[16];
+    mixed_array_slots(pk->m, f);
+    int rc = 0;
+    for (int k = 0; k < 16 && !rc; k++) rc = dev_alloc(f[k], (size_t)width * rows);
+    for (int k = 0; k < n && !rc; k++) {
+        // the scene's FP32 arrays become views into the pack at its place (its
+        // own arrays are released), and its own pack is rebuilt on them
+        Sim* s = sims[k];
+        const long long off = (long long)y0[k] * width + x0[k];
+        float** g[16];
+        mixed_array_slots(s->m32, g);
+        for (int a = 0; a < 16; a++) {
+            if (s->m32_owned && *g[a]) cudaFree(*g[a]);
+            *g[a] = *f[a] + off;
+        }
+        s->m32_owned = false;
+        s->P32 = width;
+        pack_free(s->pack);
+        s->pack = nullptr;
+        rc = pack_create_single(s);
+        if (!rc) pk->scenes.push_back(scene_entry(s, width, x0[k], y0[k]));
+    }
+    if (!rc) rc = pack_finish(pk);
+    if (rc) {
+        pack_free(pk);
+        return rc;
+    }
+    // persistent sweep CTAs: one per SM (a sweep CTA takes most of an SM's
+    // shared memory), at most one per work item
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    pk->sweep_ctas = std::max(1, std::min(sms, pk->nitems));
+    *out = pk;
+    return 0;
+}
+
+// FP32 copies of the matrix, the MIC(0) factor and the folded coefficients of
+// the handle's built system (its region of its pack's arrays).
+int mixed_setup(Sim* s) {
+    const int NX = s->NX, NY = s->NY, P = s->P32;
+    const size_t N = s->N;
+    const unsigned nb = blocks_for(N, kT);
+    Mixed32& m = s->m32;
+    FS2D_LAUNCH(s, k_mixed_matrix, nb, kT, 0, s->Adiag, s->Ax, s->Ay, m.a0, m.ax, m.ay, NX, P, N);
+    {
+        MicFactor32 op{{m.a0, m.ax - 1, m.ay - 1, m.ay - P, m.ax - P}, m.pc, P, (float)s->opt.mic_tau,
+                       (float)s->opt.mic_sigma};
+        int rc = launch_wave2<MicFactor32, 2, 16>(s, op, WaveGeom{1, 1, 1, NX - 1, 1, NY - 1}, nullptr);
+        if (rc) return rc;
+    }
+    FS2D_LAUNCH(s, k_mixed_coef, nb, kT, 0, m.ax, m.ay, m.pc, m.fa, m.fb, m.fc, m.fd, NX, NY, P);
     return 0;
 }
 
 constexpr int kM32GraphIters = 8;   // inner iterations per graph replay (even: the search-direction ping-pong)
+
+// One inner iteration of every scene of the pack; graph = inside a stream capture.
+static int pack_iteration(Pack* pk, PackLaunch& L, int it, bool graph, int max_iters) {
+    Mixed32& m = pk->m;
+    float* sbuf[2] = {m.s0, m.s1};
+    float* s_old = sbuf[it & 1];
+    float* s_new = sbuf[(it + 1) & 1];
+    PK_LAUNCH(L, k_spmv32, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w,
+              pk->d_ctl);
+    PK_LAUNCH(L, k_axpy32, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.e, m.r, m.rp, m.pc, s_new, m.w,
+              pk->d_ctl);
+    const int slot = graph ? 2 * (it % kM32GraphIters) : -1;   // sweeps of one replay
+    int rc = launch_mic32<true>(pk, L, m.q, slot, 2 * kM32GraphIters);
+    if (rc) return rc;
+    rc = launch_mic32<false>(pk, L, m.z, graph ? slot + 1 : -1, 2 * kM32GraphIters);
+    if (rc) return rc;
+    PK_LAUNCH(L, k_dot32, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.z, m.r, 0, max_iters, pk->d_ctl);
+    return 0;
+}
+
+// Captures kM32GraphIters inner iterations as a CUDA graph (once per pack);
+// false: launch directly (per-kernel timing is on, or capture is not
+// available here).
+static bool pack_graph(Pack* pk, PackLaunch& L, int max_iters) {
+    if ((L.timer && !L.timer->kt_patterns.empty()) || pk->graph_state < 0) return false;
+    if (pk->graph_state == 1) return true;
+    pk->graph_state = -1;   // until the capture below succeeds
+    const unsigned long long l0 = *L.launches;
+    if (cudaStreamBeginCapture(L.stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    int rc1 = 0;
+    for (int k = 0; k < kM32GraphIters && !rc1; k++) rc1 = pack_iteration(pk, L, k, true, max_iters);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(L.stream, &g);
+    pk->graph_launches = *L.launches - l0;
+    *L.launches = l0;   // captured, not run
+    if (rc1 || e != cudaSuccess || g == nullptr) {
+        if (g) cudaGraphDestroy(g);
+        (void)cudaGetLastError();
+        return false;
+    }
+    e = cudaGraphInstantiate(&pk->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        pk->graph = nullptr;
+        return false;
+    }
+    pk->graph_state = 1;
+    return true;
+}
+
+// The refinement loop of every scene of the pack: FP32 inner solves of
+// A e = r / ||r||inf (batches of iterations replayed from a CUDA graph until
+// every scene's inner solve stopped), p += e ||r||inf and the FP64 residual,
+// until every scene met the reference's stopping test or the sweep cap.  The
+// host polls one counter per graph replay and one per sweep for the whole pack.
+static int pack_solve_impl(Pack* pk, const fs2d_options& opt, PackLaunch& L) {
+    Mixed32& m = pk->m;
+    const int max_iters = opt.pcg_max_iters;
+    const int batch = 4;
+    FS2D_CUDA(cudaMemsetAsync(pk->d_ctl, 0, 2 * sizeof(int), L.stream));
+    PK_LAUNCH(L, k_outer_start, blocks_for(pk->n, 128), 128, pk->d_scenes, pk->n, pk->d_ctl);
+    auto poll = [&](int which, int* value) -> int {
+        FS2D_CUDA(cudaMemcpyAsync(pk->h_ctl + which, pk->d_ctl + which, sizeof(int), cudaMemcpyDeviceToHost, L.stream));
+        FS2D_CUDA(cudaStreamSynchronize(L.stream));
+        *value = pk->h_ctl[which];
+        return 0;
+    };
+    int refining = 0;
+    if (int rc = poll(1, &refining)) return rc;
+    for (int outer = 0; outer < opt.ir_max_outer && refining > 0; outer++) {
+        PK_LAUNCH(L, k_inner_init, pk->nblk64, kT, pk->d_scenes, pk->d_blk64, pk->pitch, m.pc, m.r, m.rp, m.e,
+                  opt.ir_inner_tol, pk->d_ctl);
+        int rc = launch_mic32<true>(pk, L, m.q);
+        if (rc) return rc;
+        rc = launch_mic32<false>(pk, L, m.z);
+        if (rc) return rc;
+        PK_LAUNCH(L, k_dot32, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.z, m.r, 1, max_iters, pk->d_ctl);
+        int it = 0, running = 1;
+        if (pack_graph(pk, L, max_iters)) {
+            // whole batches of iterations from the captured graph (kernels of a
+            // scene whose inner solve stopped return at once)
+            for (; it + kM32GraphIters <= max_iters + kM32GraphIters && running > 0; it += kM32GraphIters) {
+                FS2D_CUDA(cudaGraphLaunch(pk->graph, L.stream));
+                *L.launches += pk->graph_launches;
+                if ((rc = poll(0, &running))) return rc;
+            }
+        }
+        for (; it < max_iters && running > 0; it++) {
+            if ((rc = pack_iteration(pk, L, it, false, max_iters))) return rc;
+            if ((it + 1) % batch == 0 || it + 1 == max_iters) {
+                if ((rc = poll(0, &running))) return rc;
+            }
+        }
+        PK_LAUNCH(L, k_update64, pk->nblk64, kT, pk->d_scenes, pk->d_blk64, pk->pitch, m.e);
+        PK_LAUNCH(L, k_resid64, pk->nblk64, kT, pk->d_scenes, pk->d_blk64, opt.ir_max_outer, pk->d_ctl);
+        if ((rc = poll(1, &refining))) return rc;
+    }
+    return 0;
+}
+
+int pack_solve(Pack* pk, const fs2d_options& opt, cudaStream_t stream, unsigned long long* launches, int* err,
+               int device, Sim* timer) {
+    PackLaunch L{stream, err, device, launches, pk->wave_launch, timer};
+    int rc = pack_solve_impl(pk, opt, L);
+    pk->wave_launch = L.wave_launch;
+    return rc;
+}
+
+namespace {
+// Sets the inner-solve stop flag of every scene of the pack (one thread per scene).
+__global__ void k_set_done(const PackScene* __restrict__ sc, int n, int done) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < n) sc[k].inner->done = done;
+}
+}  // namespace
+
+// Autotuner of the persistent sweep of several scenes: the schedule (the
+// order in which whole scenes enter the work list: as given, or by
+// decreasing rows, or by decreasing cells) and the number of persistent CTAs
+// (all SMs, three quarters, half) are each timed on forward sweeps of the
+// pack (CUDA events, after a warm-up sweep), and the fastest pair is kept.
+// A scene's results do not depend on either choice: its strips are computed
+// in the same order by the same step code whichever CTA takes them.
+int pack_tune(Pack* pk, cudaStream_t stream, int* err, int device, unsigned long long* launches, double* best_us) {
+    if (pk->n < 2) return 0;
+    int sms = 1;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    std::vector<int> order(pk->n);
+    std::vector<std::vector<Mic32Item>> schedules;
+    for (int variant = 0; variant < 3; variant++) {
+        std::iota(order.begin(), order.end(), 0);
+        if (variant == 1)
+            std::stable_sort(order.begin(), order.end(),
+                             [&](int a, int b) { return pk->scenes[a].NY32 > pk->scenes[b].NY32; });
+        if (variant == 2)
+            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                return (long long)pk->scenes[a].NY32 * pk->scenes[a].P32 > (long long)pk->scenes[b].NY32 * pk->scenes[b].P32;
+            });
+        std::vector<Mic32Item> items;
+        for (int k : order) {
+            const PackScene& e = pk->scenes[k];
+            const int ns = e.P32 / kM32Cols;
+            for (int st = 0; st < ns; st++) items.push_back(Mic32Item{k, st, ns, e.x0, e.P32, e.y0, e.NY32});
+        }
+        schedules.push_back(items);
+    }
+    const int ctas[3] = {sms, sms * 3 / 4, sms / 2};
+    cudaEvent_t e0, e1;
+    FS2D_CUDA(cudaEventCreate(&e0));
+    FS2D_CUDA(cudaEventCreate(&e1));
+    PK_LAUNCH_PLAIN(stream, k_set_done, blocks_for(pk->n, 128), 128, pk->d_scenes, pk->n, 0);
+    PackLaunch L{stream, err, device, launches, pk->wave_launch, nullptr};
+    double best = 1e300;
+    int best_s = 0, best_c = sms;
+    int rc = 0;
+    for (int si = 0; si < 3 && !rc; si++) {
+        rc = check_cuda(cudaMemcpyAsync(pk->d_items, schedules[si].data(), schedules[si].size() * sizeof(Mic32Item),
+                                        cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
+        for (int ci = 0; ci < 3 && !rc; ci++) {
+            pk->sweep_ctas = std::max(1, std::min(ctas[ci], pk->nitems));
+            rc = launch_mic32<true>(pk, L, pk->m.q);   // warm-up
+            if (!rc) rc = check_cuda(cudaEventRecord(e0, stream), "cudaEventRecord");
+            for (int r = 0; r < 3 && !rc; r++) rc = launch_mic32<true>(pk, L, pk->m.q);
+            if (!rc) rc = check_cuda(cudaEventRecord(e1, stream), "cudaEventRecord");
+            if (!rc) rc = check_cuda(cudaEventSynchronize(e1), "cudaEventSynchronize");
+            float ms = 0;
+            if (!rc) cudaEventElapsedTime(&ms, e0, e1);
+            if (!rc && ms < best) {
+                best = ms;
+                best_s = si;
+                best_c = pk->sweep_ctas;
+            }
+        }
+    }
+    if (!rc) rc = check_cuda(cudaMemcpyAsync(pk->d_items, schedules[best_s].data(),
+                                             schedules[best_s].size() * sizeof(Mic32Item), cudaMemcpyHostToDevice,
+                                             stream), "cudaMemcpyAsync");
+    pk->sweep_ctas = best_c;
+    pk->schedule = best_s;
+    pk->wave_launch = L.wave_launch;
+    if (!rc) {
+        k_set_done<<<blocks_for(pk->n, 128), 128, 0, stream>>>(pk->d_scenes, pk->n, 1);
+        rc = check_cuda(cudaGetLastError(), "k_set_done");
+    }
+    if (!rc) rc = check_cuda(cudaStreamSynchronize(stream), "cudaStreamSynchronize");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (best_us) *best_us = best * 1000.0 / 3;
+    return rc;
+}
+
+int mixed_finish(Sim* s, int* status) {
+    FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, s->pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
+    if (int rcw = wait_stream(s, s->stream)) return rcw;
+    const PcgScalars& o = *s->pcg_host;
+    s->last_iters = o.inner_total;
+    s->last_outer = o.outer_iters;
+    const bool solved = o.rhs_norm > 1e-12;
+    s->last_rel_res = o.rhs_norm > 0 ? (solved ? o.r_norm : o.rhs_norm) / o.rhs_norm : 0.0;
+    if (status) *status = (solved && o.r_norm > o.tol_abs) ? FS2D_ERR_NOT_CONVERGED : 0;
+    return 0;
+}
 
 int projection_mixed(Sim* s, int* status) { return projection_mixed_rhs(s, nullptr, status); }
 
 // b == nullptr: the physical right-hand side; otherwise A p = b for a device
 // array b on the fluid cells.
 int projection_mixed_rhs(Sim* s, const double* b, int* status) {
-    const int NX = s->NX, NY = s->NY, P = s->P32;   // FP32 arrays: pitch P32
-    const size_t N = s->N;
-    const unsigned nb = blocks_for(N, kT);
-    Mixed32& m = s->m32;
     // the FP64 matrix, rhs, ||b||inf, p = 0, r = b (exactly the reference's)
     int rc = projection_build(s);
     if (rc) return rc;
     if (b && (rc = projection_set_rhs(s, b))) return rc;
-    FS2D_LAUNCH(s, k_mixed_matrix, nb, kT, 0, s->Adiag, s->Ax, s->Ay, m.a0, m.ax, m.ay, NX, P, N);
-    {
-        MicFactor32 op{{m.a0, m.ax - 1, m.ay - 1, m.ay - P, m.ax - P}, m.pc, P, (float)s->opt.mic_tau,
-                       (float)s->opt.mic_sigma};
-        rc = launch_wave2<MicFactor32, 2, 16>(s, op, WaveGeom{1, 1, 1, NX - 1, 1, NY - 1}, nullptr);
-        if (rc) return rc;
-    }
-    FS2D_LAUNCH(s, k_mixed_coef, nb, kT, 0, m.ax, m.ay, m.pc, m.fa, m.fb, m.fc, m.fd, NX, NY, P);
-
-    PcgScalars* outer = s->pcg;     // rhs_norm, tol_abs from projection_build; r_norm = ||r64||
-    PcgScalars* inner = s->pcg32;
-    const int* done = &inner->done;
-    const Mic32Maps& fmaps = *reinterpret_cast<const Mic32Maps*>(s->m32maps->fwd);
-    const Mic32Maps& bmaps = *reinterpret_cast<const Mic32Maps*>(s->m32maps->bwd);
-    const int max_iters = s->opt.pcg_max_iters;
-    const int batch = 4;
-    // inner kernels: ~8 blocks per SM of row segments
-    const int gx = (NX + kRT - 1) / kRT;
-    const dim3 rg(gx, std::max(1, std::min(NY, 1216 / gx)));
-    float2* part2 = reinterpret_cast<float2*>(s->partial);
-    float* partf = reinterpret_cast<float*>(s->partial);
-    int total_iters = 0, outer_iters = 0, status_out = 0;
-
-    FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, outer, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
-    if (int rcw = wait_stream(s, s->stream)) return rcw;
-    const double rhs_norm = s->pcg_host->rhs_norm;
-    const double tol_abs = s->pcg_host->tol_abs;
-    double r_norm = rhs_norm;
-    if (rhs_norm > 1e-12) {
-        for (outer_iters = 0; outer_iters < s->opt.ir_max_outer; outer_iters++) {
-            if (r_norm <= tol_abs) break;
-            // each inner solve works on r / ||r||inf: it has to reduce that
-            // by tol_abs / ||r||inf (with a factor 2 of margin for the FP32
-            // recurrence), but never asks for more than ir_inner_tol
-            const double inner_tol = std::max(s->opt.ir_inner_tol, 0.5 * tol_abs / r_norm);
-            FS2D_LAUNCH(s, k_inner_init, nb, kT, 0, s->r, outer, m.pc, m.r, m.rp, m.e, NX, P, N, inner, inner_tol);
-            rc = launch_mic32<true>(s, fmaps, m.q, done);
-            if (rc) return rc;
-            rc = launch_mic32<false>(s, bmaps, m.z, done);
-            if (rc) return rc;
-            FS2D_LAUNCH(s, k_dot32, rg, kRT, 0, m.z, m.r, NX, NY, P, part2, inner, 1, max_iters);
-            // one inner iteration; graph = true inside a stream capture
-            auto iteration = [&](int it, bool graph) -> int {
-                float* sbuf[2] = {m.s0, m.s1};
-                float* s_old = sbuf[it & 1];
-                float* s_new = sbuf[(it + 1) & 1];
-                FS2D_LAUNCH(s, k_spmv32, rg, kRT, 0, s->cell, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w, NX, NY, P,
-                            part2, inner);
-                FS2D_LAUNCH(s, k_axpy32, rg, kRT, 0, m.e, m.r, m.rp, m.pc, s_new, m.w, NX, NY, P, partf, inner);
-                const int slot = graph ? 2 * (it % kM32GraphIters) : -1;   // sweeps of one replay
-                int rc1 = launch_mic32<true>(s, fmaps, m.q, done, slot, 2 * kM32GraphIters);
-                if (rc1) return rc1;
-                rc1 = launch_mic32<false>(s, bmaps, m.z, done, graph ? slot + 1 : -1, 2 * kM32GraphIters);
-                if (rc1) return rc1;
-                FS2D_LAUNCH(s, k_dot32, rg, kRT, 0, m.z, m.r, NX, NY, P, part2, inner, 0, max_iters);
-                return 0;
-            };
-            // true once the inner solve stopped; a failed copy or wait also
-            // stops it and leaves its status in rc_poll
-            int rc_poll = 0;
-            auto poll_done = [&]() -> bool {
-                rc_poll = check_cuda(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars),
-                                                     cudaMemcpyDeviceToHost, s->stream),
-                                     "cudaMemcpyAsync");
-                if (!rc_poll) rc_poll = wait_stream(s, s->stream);
-                return rc_poll != 0 || s->pcg32_host->done != 0;
-            };
-            // Captures kM32GraphIters iterations as a CUDA graph (once per handle,
-            // again whenever the reduction scratch moved); false: launch directly
-            // (per-kernel timing is on, or capture is not available here).
-            auto ensure_graph = [&]() -> bool {
-                if (!s->kt_patterns.empty() || s->m32_graph_state < 0) return false;
-                if (s->m32_graph_state == 1 && s->m32_graph_key == (const void*)s->partial) return true;
-                if (s->m32_graph) {
-                    cudaGraphExecDestroy(s->m32_graph);
-                    s->m32_graph = nullptr;
-                }
-                s->m32_graph_state = -1;   // until the capture below succeeds
-                const unsigned long long l0 = s->launches;
-                if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
-                    (void)cudaGetLastError();
-                    return false;
-                }
-                int rc1 = 0;
-                for (int k = 0; k < kM32GraphIters && !rc1; k++) rc1 = iteration(k, true);
-                cudaGraph_t g = nullptr;
-                cudaError_t e = cudaStreamEndCapture(s->stream, &g);
-                s->m32_graph_launches = s->launches - l0;
-                s->launches = l0;   // captured, not run
-                if (rc1 || e != cudaSuccess || g == nullptr) {
-                    if (g) cudaGraphDestroy(g);
-                    (void)cudaGetLastError();
-                    return false;
-                }
-                e = cudaGraphInstantiate(&s->m32_graph, g, 0);
-                cudaGraphDestroy(g);
-                if (e != cudaSuccess) {
-                    (void)cudaGetLastError();
-                    s->m32_graph = nullptr;
-                    return false;
-                }
-                s->m32_graph_key = s->partial;
-                s->m32_graph_state = 1;
-                return true;
-            };
-            int it = 0;
-            if (ensure_graph()) {
-                // whole batches of iterations from the captured graph (kernels
-                // after convergence return at once on the done flag)
-                for (; it + kM32GraphIters <= max_iters; it += kM32GraphIters) {
-                    FS2D_CUDA(cudaGraphLaunch(s->m32_graph, s->stream));
-                    s->launches += s->m32_graph_launches;
-                    if (poll_done()) {
-                        it = max_iters;
-                        break;
-                    }
-                }
-            }
-            for (; it < max_iters; it++) {
-                if ((rc = iteration(it, false))) return rc;
-                if ((it + 1) % batch == 0 || it + 1 == max_iters) {
-                    if (poll_done()) break;
-                }
-            }
-            if (rc_poll) return rc_poll;
-            FS2D_LAUNCH(s, k_update64, nb, kT, 0, s->p, m.e, outer, NX, P, N);
-            FS2D_LAUNCH(s, k_resid64, nb, kT, 0, s->cell, s->Adiag, s->Ax, s->Ay, s->rhs, s->p, s->r, NX, N,
-                        s->partial, outer);
-            FS2D_CUDA(cudaMemcpyAsync(s->pcg32_host, inner, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
-            FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, outer, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
-            if (int rcw = wait_stream(s, s->stream)) return rcw;
-            total_iters += s->pcg32_host->iter;
-            r_norm = s->pcg_host->r_norm;
-        }
-        if (r_norm > tol_abs) status_out = FS2D_ERR_NOT_CONVERGED;
-    } else {
-        r_norm = rhs_norm;
-    }
-    s->last_iters = total_iters;
-    s->last_outer = outer_iters;
-    s->last_rel_res = rhs_norm > 0 ? r_norm / rhs_norm : 0.0;
-    if (status) *status = status_out;
-    return 0;
+    if ((rc = mixed_setup(s))) return rc;
+    if ((rc = pack_solve(s->pack, s->opt, s->stream, &s->launches, s->err, s->device, s))) return rc;
+    return mixed_finish(s, status);
 }
 
 }  // namespace fs2d

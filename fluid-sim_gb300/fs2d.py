@@ -104,6 +104,9 @@ SIGNATURES = {
                                      C.c_void_p]),
     "fs2d_batch_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fs2d_batch_destroy": (C.c_int, [C.c_void_p]),
+    "fs2d_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
+    "fs2d_batch_sweep_schedule": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_double)]),
     "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
     "fs2d_save_stats": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p]),
     "fs2d_write_stats": (C.c_int, [C.c_void_p, C.c_int, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t,
@@ -466,6 +469,19 @@ class Batch:
         h = C.c_void_p()
         _check(load().fs2d_batch_scene(self.h, int(k), C.byref(h)))
         return FluidSim2D._view(h, self.scenes[k])
+
+    def sweep_schedule(self):
+        """The tuned persistent sweep of a mixed-precision batch: schedule,
+        CTAs, work items and the sweep's time in microseconds."""
+        sc, ct, it, us = C.c_int(), C.c_int(), C.c_int(), C.c_double()
+        _check(load().fs2d_batch_sweep_schedule(self.h, C.byref(sc), C.byref(ct), C.byref(it), C.byref(us)))
+        return {"schedule": sc.value, "ctas": ct.value, "items": it.value, "sweep_us": us.value}
+
+    def launch_count(self):
+        """Kernels launched so far by the batch and its scenes."""
+        n = C.c_ulonglong()
+        _check(load().fs2d_batch_launch_count(self.h, C.byref(n)))
+        return n.value
 
     @property
     def workers(self):

@@ -246,6 +246,17 @@ int fs2d_batch_scene(fs2d_batch* batch, int k, fs2d_sim** sim);
 int fs2d_batch_workers(fs2d_batch* batch, int* workers);   /* 0 until chosen */
 int fs2d_batch_set_workers(fs2d_batch* batch, int workers); /* 0: choose again on the next frames */
 int fs2d_batch_destroy(fs2d_batch* batch);
+/* Kernels launched so far by the batch and its scenes. */
+int fs2d_batch_launch_count(fs2d_batch* batch, unsigned long long* out);
+/* Mixed precision: the batch solves every scene's pressure system together
+ * (one launch per kernel of the inner solve for all scenes; the FP32 MIC(0)
+ * sweeps as persistent CTAs over work items of one strip of 128 columns of
+ * one scene).  fs2d_batch_create times candidate schedules (0: scenes in the
+ * given order, 1: by decreasing rows, 2: by decreasing cells) and CTA counts
+ * on forward sweeps and keeps the fastest; this reports the choice, the
+ * number of work items and the chosen sweep's time (schedule -1 for an FP64
+ * batch).  Any pointer may be NULL. */
+int fs2d_batch_sweep_schedule(fs2d_batch* batch, int* schedule, int* ctas, int* items, double* sweepUs);
 /* fs2d_forward / fs2d_backward for every scene of a batch (each a closed box:
  * no EMPTY cell, semi-Lagrangian mode), scenes issued concurrently by the
  * batch's workers (all hardware threads up to 16 while the count is not

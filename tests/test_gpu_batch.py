@@ -1,9 +1,12 @@
 """Batches of independent scenes (fs2d_batch_*): PIC/FLIP dam breaks of
-uneven sizes advanced concurrently by host worker threads, each scene on
-its own stream.  Every scene's state after the batch's frames must equal,
-bit for bit, the state of the same scene run alone through fs2d_run_frame
-(same seed), whatever the worker count, including the count the batch
-chooses itself on its first frames."""
+uneven sizes.  Host worker threads queue each scene's stages on its own
+stream; with mixed precision every scene's pressure solve runs in one pack
+(one launch per kernel of the inner solve for all scenes, the sweeps as
+persistent work items).  Every scene's state after the batch's frames must
+equal, bit for bit, the state of the same scene run alone through
+fs2d_run_frame (same seed), whatever the worker count, including the count
+the batch chooses itself on its first frames, and a scene of a batch must
+still run alone on its region of the batch's arrays."""
 import numpy as np
 import pytest
 
@@ -37,6 +40,23 @@ def test_batch_matches_scenes_run_alone(workers):
     for k, sc in enumerate(scs):
         assert_same(b.scene(k).get_state(FIELDS), alone(sc, 100 + k, 3))
         assert b.scene(k).stats()["frames"] == 3
+    b.close()
+
+
+def test_batch_of_wide_scenes_matches_scenes_run_alone():
+    """Scenes of one to three strips of the FP32 sweeps (strips of 128
+    columns): the persistent sweep's work items hand columns over between
+    the strips of each scene only."""
+    scs = scenes.batch_dam_breaks(6, seed=11, lo=100, hi=300)
+    b = fs2d.Batch(scs, workers=2, seed=30, **OPTS)
+    b.step(2)
+    for k, sc in enumerate(scs):
+        assert_same(b.scene(k).get_state(FIELDS), alone(sc, 30 + k, 2))
+    assert b.launch_count() > 0
+    # a scene of the batch run alone, on its region of the batch's arrays
+    v = b.scene(4)
+    assert v.runFrame() in (0, 4)
+    assert_same(v.get_state(FIELDS), alone(scs[4], 34, 3))
     b.close()
 
 
