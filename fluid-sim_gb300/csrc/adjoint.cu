@@ -338,7 +338,7 @@ int forward_step(Sim* s) {
     int rc = sl_advect(s);
     if (!rc) rc = apply_gravity(s);
     int status = 0;
-    if (!rc) rc = s->opt.precision == FS2D_PRECISION_MIXED ? projection_mixed(s, &status) : projection(s, &status);
+    if (!rc) rc = s->opt.precision != FS2D_PRECISION_FP64 ? projection_mixed(s, &status) : projection(s, &status);
     if (!rc) rc = update_velocity(s);
     if (!rc && status) {
         set_error("rollout: the pressure solve hit its iteration cap");

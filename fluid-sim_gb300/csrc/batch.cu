@@ -278,7 +278,7 @@ int fs2d_batch_create(const fs2d_config* cfgs, int n, const fs2d_options* opt, i
     b->status_msg.assign(n, std::string());
     b->workers = workers == 0 ? 0 : std::min({workers, n, 64});
     b->opt = o;
-    if (o.precision == FS2D_PRECISION_MIXED) {
+    if (o.precision != FS2D_PRECISION_FP64) {
         std::vector<Sim*> ss(n);
         for (int k = 0; k < n; k++) ss[k] = sim_of(b->sims[k]);
         int rc = pack_create_batch(ss.data(), n, &b->pack);

@@ -302,7 +302,7 @@ int alloc_all(Sim* s) {
     A(stats, 1);
     A(err, kErrWords);
     if ((rc = set_wave_controls(s, kWaveSpinLimit, 0, -1))) return rc;
-    if (s->opt.precision == FS2D_PRECISION_MIXED) {
+    if (s->opt.precision != FS2D_PRECISION_FP64) {
         Mixed32& m = s->m32;
         s->P32 = (s->NX + 127) / 128 * 128;
         s->NY32 = (s->NY + 31) / 32 * 32;
@@ -380,7 +380,7 @@ int run_stage_impl(Sim* s, int stage, int* status) {
         case FS2D_STAGE_APPLY_GRAVITY: return apply_gravity(s);
         case FS2D_STAGE_CREATE_SOLID_LEVEL_SET: return 0;  // empty in the reference (:734-736)
         case FS2D_STAGE_APPLY_PROJECTION:
-            return s->opt.precision == FS2D_PRECISION_MIXED ? projection_mixed(s, status) : projection(s, status);
+            return s->opt.precision != FS2D_PRECISION_FP64 ? projection_mixed(s, status) : projection(s, status);
         case FS2D_STAGE_UPDATE_VELOCITY: return update_velocity(s);
         case FS2D_STAGE_UPDATE_PARTICLE_VELOCITIES: return g2p(s);
         case FS2D_STAGE_APPLY_ADVECTION: return advect_particles(s);
@@ -565,7 +565,8 @@ int fs2d_create(const fs2d_config* cfg, const fs2d_options* opt, fs2d_sim** out)
         }
     fs2d_options o;
     if (opt) o = *opt; else fs2d_default_options(&o);
-    if (o.precision != FS2D_PRECISION_FP64 && o.precision != FS2D_PRECISION_MIXED) {
+    if (o.precision != FS2D_PRECISION_FP64 && o.precision != FS2D_PRECISION_MIXED &&
+        o.precision != FS2D_PRECISION_FP32) {
         set_error("fs2d_create: unknown precision mode %d", o.precision);
         return FS2D_ERR_INVALID;
     }

@@ -147,6 +147,7 @@ struct Pack {
     int pitch = 0, rows = 0;              // array extent: rows x pitch floats
     Mixed32 m;                            // the arrays
     bool owns_arrays = false;             // freed with the pack (a batch); else the handle's
+    bool plain = false;                   // plain FP32 PCG (FP32 dot products, no FP64 refinement)
     std::vector<PackScene> scenes;        // scene table (host copy)
     PackScene* d_scenes = nullptr;
     float2* part = nullptr;               // FP32 reduction partials, one per block of nblk

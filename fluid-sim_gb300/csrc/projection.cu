@@ -446,7 +446,7 @@ int projection_set_rhs(Sim* s, const double* b) {
 // labels and level set), with the handle's precision; the solution is left
 // in s->p.
 int projection_solve_custom(Sim* s, const double* b, int* status) {
-    if (s->opt.precision == FS2D_PRECISION_MIXED) return projection_mixed_rhs(s, b, status);
+    if (s->opt.precision != FS2D_PRECISION_FP64) return projection_mixed_rhs(s, b, status);
     int rc0 = projection_build(s);
     if (rc0) return rc0;
     if ((rc0 = projection_set_rhs(s, b))) return rc0;

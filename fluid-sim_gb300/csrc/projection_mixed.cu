@@ -1,4 +1,5 @@
-// projection_mixed.cu — mixed-precision pressure solve (FS2D_PRECISION_MIXED).
+// projection_mixed.cu — mixed-precision pressure solve (FS2D_PRECISION_MIXED)
+// and the plain FP32 solve (FS2D_PRECISION_FP32).
 //
 // The reference's MIC(0)-PCG (src/FluidSim2D.cpp:252-467) with the inner
 // iteration in FP32 and the accuracy owned by FP64:
@@ -205,7 +206,26 @@ __device__ __forceinline__ bool last_block_of(unsigned int* ticket, unsigned nbl
 // the scene's last block finishes its scalar.
 constexpr int kRT = 256;
 
+__device__ __forceinline__ float f_warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <bool PLAIN>
 __device__ __forceinline__ void df_block_partial(DF v, float2* partial, int slot, float2* sh) {
+    if (PLAIN) {   // FP32 tree sum
+        float f = f_warp_sum(v.hi);
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        __syncthreads();
+        if (lane == 0) sh[wid] = make_float2(f, 0.f);
+        __syncthreads();
+        if (wid == 0) {
+            float t = f_warp_sum(lane < nw ? sh[lane].x : 0.f);
+            if (lane == 0) partial[slot] = make_float2(t, 0.f);
+        }
+        return;
+    }
     v = df_warp_sum(v);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     __syncthreads();
@@ -219,7 +239,20 @@ __device__ __forceinline__ void df_block_partial(DF v, float2* partial, int slot
 }
 
 // Sum of the partials of every block of a scene (called by its last block).
+template <bool PLAIN>
 __device__ __forceinline__ double df_final(const float2* partial, int n, float2* sh) {
+    if (PLAIN) {   // FP32 tree sum of the block partials
+        float f = 0.f;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) f += partial[k].x;
+        f = f_warp_sum(f);
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+        __syncthreads();
+        if (lane == 0) sh[wid] = make_float2(f, 0.f);
+        __syncthreads();
+        float t = 0.f;
+        if (wid == 0) t = f_warp_sum(lane < nw ? sh[lane].x : 0.f);
+        return (double)t;
+    }
     DF acc{0.f, 0.f};
     for (int k = threadIdx.x; k < n; k += blockDim.x) {
         const float2 v = partial[k];
@@ -248,6 +281,15 @@ __device__ __forceinline__ float block_max_f(float v, float* sh) {
     return v;
 }
 
+// Products accumulated exactly in double-float (FP64-accurate dots), or, for
+// the plain FP32 solve (PLAIN), in FP32 arithmetic (the low part stays 0).
+template <bool PLAIN>
+__device__ __forceinline__ void acc_prod(DF& a, float x, float y) {
+    if (PLAIN) a.hi = fmaf(x, y, a.hi);
+    else df_add(a, df_prod(x, y));
+}
+
+template <bool PLAIN>
 __global__ void __launch_bounds__(kRT) k_dot32(const PackScene* __restrict__ sc, const int* __restrict__ blk,
                                                int pitch, const float* __restrict__ z, const float* __restrict__ r,
                                                int init, int max_iters, int* ctl) {
@@ -263,12 +305,12 @@ __global__ void __launch_bounds__(kRT) k_dot32(const PackScene* __restrict__ sc,
 #pragma unroll 4
         for (int j = by; j < S.NY; j += S.gy) {
             const size_t k = (size_t)S.off + (size_t)j * pitch + i;
-            df_add(a, df_prod(z[k], r[k]));
+            acc_prod<PLAIN>(a, z[k], r[k]);
         }
     }
-    df_block_partial(a, S.part, by * S.gx + bx, sh);
+    df_block_partial<PLAIN>(a, S.part, by * S.gx + bx, sh);
     if (last_block_of(&pcg->ticket[1], S.gx * S.gy)) {
-        const double s = df_final(S.part, S.gx * S.gy, sh);
+        const double s = df_final<PLAIN>(S.part, S.gx * S.gy, sh);
         if (threadIdx.x == 0) {
             if (init) {
                 pcg->sigma = s;
@@ -285,6 +327,7 @@ __global__ void __launch_bounds__(kRT) k_dot32(const PackScene* __restrict__ sc,
 
 // s_new = z + beta s_old (z on the first iteration), w = A s_new on fluid
 // cells, alpha = sigma / (w . s_new).
+template <bool PLAIN>
 __global__ void __launch_bounds__(kRT) k_spmv32(const PackScene* __restrict__ sc, const int* __restrict__ blk,
                                                 int pitch, const float* __restrict__ a0, const float* __restrict__ ax,
                                                 const float* __restrict__ ay, const float* __restrict__ z,
@@ -314,12 +357,12 @@ __global__ void __launch_bounds__(kRT) k_spmv32(const PackScene* __restrict__ sc
                 out = a0[k] * sc0 + ax[k - 1] * sl + ax[k] * sr + ay[k - P] * sd + ay[k] * su;
             }
             w[k] = out;
-            df_add(a, df_prod(out, sc0));
+            acc_prod<PLAIN>(a, out, sc0);
         }
     }
-    df_block_partial(a, S.part, by * S.gx + bx, sh);
+    df_block_partial<PLAIN>(a, S.part, by * S.gx + bx, sh);
     if (last_block_of(&pcg->ticket[2], S.gx * S.gy)) {
-        const double sum = df_final(S.part, S.gx * S.gy, sh);
+        const double sum = df_final<PLAIN>(S.part, S.gx * S.gy, sh);
         if (threadIdx.x == 0) {
             if (sum == 0.0) inner_stop(pcg, 1, ctl);
             else pcg->alpha = pcg->sigma / sum;
@@ -629,6 +672,7 @@ int pack_create_single(Sim* s) {
     pk->rows = s->NY32;
     pk->m = s->m32;
     pk->owns_arrays = false;
+    pk->plain = s->opt.precision == FS2D_PRECISION_FP32;
     pk->scenes.push_back(scene_entry(s, s->P32, 0, 0));
     int rc = pack_finish(pk);
     if (rc) {
@@ -683,6 +727,7 @@ int pack_create_batch(Sim* const* sims, int n, Pack** out) {
     pk->pitch = width;
     pk->rows = rows;
     pk->owns_arrays = true;
+    pk->plain = sims[0]->opt.precision == FS2D_PRECISION_FP32;
     float** f[16];
     mixed_array_slots(pk->m, f);
     int rc = 0;
@@ -746,8 +791,12 @@ static int pack_iteration(Pack* pk, PackLaunch& L, int it, bool graph, int max_i
     float* sbuf[2] = {m.s0, m.s1};
     float* s_old = sbuf[it & 1];
     float* s_new = sbuf[(it + 1) & 1];
-    PK_LAUNCH(L, k_spmv32, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.a0, m.ax, m.ay, m.z, s_old, s_new, m.w,
-              pk->d_ctl);
+    if (pk->plain)
+        PK_LAUNCH(L, k_spmv32<true>, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.a0, m.ax, m.ay, m.z, s_old,
+                  s_new, m.w, pk->d_ctl);
+    else
+        PK_LAUNCH(L, k_spmv32<false>, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.a0, m.ax, m.ay, m.z, s_old,
+                  s_new, m.w, pk->d_ctl);
     PK_LAUNCH(L, k_axpy32, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.e, m.r, m.rp, m.pc, s_new, m.w,
               pk->d_ctl);
     const int slot = graph ? 2 * (it % kM32GraphIters) : -1;   // sweeps of one replay
@@ -755,7 +804,11 @@ static int pack_iteration(Pack* pk, PackLaunch& L, int it, bool graph, int max_i
     if (rc) return rc;
     rc = launch_mic32<false>(pk, L, m.z, graph ? slot + 1 : -1, 2 * kM32GraphIters);
     if (rc) return rc;
-    PK_LAUNCH(L, k_dot32, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.z, m.r, 0, max_iters, pk->d_ctl);
+    if (pk->plain)
+        PK_LAUNCH(L, k_dot32<true>, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.z, m.r, 0, max_iters, pk->d_ctl);
+    else
+        PK_LAUNCH(L, k_dot32<false>, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.z, m.r, 0, max_iters,
+                  pk->d_ctl);
     return 0;
 }
 
@@ -798,8 +851,15 @@ static bool pack_graph(Pack* pk, PackLaunch& L, int max_iters) {
 // every scene's inner solve stopped), p += e ||r||inf and the FP64 residual,
 // until every scene met the reference's stopping test or the sweep cap.  The
 // host polls one counter per graph replay and one per sweep for the whole pack.
-static int pack_solve_impl(Pack* pk, const fs2d_options& opt, PackLaunch& L) {
+static int pack_solve_impl(Pack* pk, const fs2d_options& opt_in, PackLaunch& L) {
     Mixed32& m = pk->m;
+    fs2d_options opt = opt_in;
+    if (pk->plain) {
+        // plain FP32 PCG: one FP32 solve to the solve's own tolerance (the FP64
+        // residual is still computed once, for the statistics and the status)
+        opt.ir_max_outer = 1;
+        opt.ir_inner_tol = opt.pcg_tol;
+    }
     const int max_iters = opt.pcg_max_iters;
     const int batch = 4;
     FS2D_CUDA(cudaMemsetAsync(pk->d_ctl, 0, 2 * sizeof(int), L.stream));
@@ -819,7 +879,12 @@ static int pack_solve_impl(Pack* pk, const fs2d_options& opt, PackLaunch& L) {
         if (rc) return rc;
         rc = launch_mic32<false>(pk, L, m.z);
         if (rc) return rc;
-        PK_LAUNCH(L, k_dot32, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.z, m.r, 1, max_iters, pk->d_ctl);
+        if (pk->plain)
+            PK_LAUNCH(L, k_dot32<true>, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.z, m.r, 1, max_iters,
+                      pk->d_ctl);
+        else
+            PK_LAUNCH(L, k_dot32<false>, pk->nblk, kRT, pk->d_scenes, pk->d_blk, pk->pitch, m.z, m.r, 1, max_iters,
+                      pk->d_ctl);
         int it = 0, running = 1;
         if (pack_graph(pk, L, max_iters)) {
             // whole batches of iterations from the captured graph (kernels of a

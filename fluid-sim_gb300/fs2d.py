@@ -21,7 +21,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libfs2d.so")
 
-PRECISION = {"fp64": 0, "mixed": 1}
+PRECISION = {"fp64": 0, "mixed": 1, "fp32": 2}
 P2G = {"ordered": 0, "atomic": 1}
 STAGES = {
     "createWaterLevelSet": 1,

@@ -66,8 +66,12 @@ extern "C" {
 
 /* ---- precision of the device path ---- */
 #define FS2D_PRECISION_FP64  0  /* every stage in FP64 with the reference's operation order */
-#define FS2D_PRECISION_MIXED 1  /* FP32 fields/transfers/SpMV/preconditioner, FP64 dots, norms
-                                   and outer iterative-refinement residual */
+#define FS2D_PRECISION_MIXED 1  /* FP32 SpMV/preconditioner/vector updates, FP64-accurate dot
+                                   products, FP64 outer iterative-refinement residual and
+                                   stopping test */
+#define FS2D_PRECISION_FP32  2  /* plain FP32 PCG: FP32 SpMV, preconditioner, vector updates and
+                                   dot products, one solve to pcg_tol on the FP32 residual, no
+                                   refinement; the FP64 residual is reported */
 
 /* ---- P2G accumulation ---- */
 #define FS2D_P2G_ORDERED 0  /* per-face sums in particle-index order: reproducible, matches the reference */

@@ -93,3 +93,27 @@ def test_graph_replay_matches_direct_launches():
     assert a.stats()["pcgIterations"] == b.stats()["pcgIterations"]
     a.close()
     b.close()
+
+
+def test_plain_fp32_pcg():
+    """Config 1's first GPU form: plain FP32 MIC(0)-PCG (FP32 dot products, one
+    solve to the tolerance on the FP32 residual, no FP64 refinement).  Its
+    FP64 residual is reported (NOT_CONVERGED when FP32 rounding keeps it above
+    the tolerance) and its pressure stays within FP32_RTOL of the FP64
+    solution solved to 1e-12, the mixed path within MIXED_RTOL."""
+    import scenes
+    FP32_RTOL, MIXED_RTOL = 1e-4, 1e-5
+    sc, cell, phi, u, v = scenes.pressure_disks(256, 256, seed=9)
+    ref = fs2d.FluidSim2D(sc, seed=1, precision="fp64", pcg_tol=1e-12, pcg_max_iters=2000)
+    p64, _ = ref.solve_pressure(cell, phi, u, v)
+    ref.close()
+    for prec, rtol in (("fp32", FP32_RTOL), ("mixed", MIXED_RTOL)):
+        sim = fs2d.FluidSim2D(sc, seed=1, precision=prec, pcg_tol=1e-6, pcg_max_iters=400)
+        p, st = sim.solve_pressure(cell, phi, u, v)
+        sim.close()
+        assert np.abs(p - p64).max() <= rtol * np.abs(p64).max(), (prec, st)
+        if prec == "fp32":
+            assert st["irOuterIterations"] == 1 and st["pcgRelResidual"] < 1e-4
+            assert st["lastStatus"] in (0, 4) and (st["lastStatus"] == 4) == (st["pcgRelResidual"] > 1e-6)
+        else:
+            assert st["lastStatus"] == 0 and st["pcgRelResidual"] <= 1e-6
