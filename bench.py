@@ -90,7 +90,7 @@ def parse():
     ap.add_argument("--adjoint-size", type=int, default=128, help="closed-box rollout grid (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=64)
     ap.add_argument("--batch-scenes", type=int, default=256, help="batched dam breaks (0: skip)")
-    ap.add_argument("--batch-steps", type=int, default=5)
+    ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--batch-adjoint-scenes", type=int, default=32, help="batched closed-box rollouts (0: skip)")
     ap.add_argument("--sl-steps", type=int, default=10, help="steps of the semi-Lagrangian 1024^2 variant (0: skip)")
     ap.add_argument("--batch-adjoint-steps", type=int, default=16)
@@ -623,6 +623,7 @@ def main():
         bt.step(args.batch_steps)
         torch.cuda.synchronize()
         conc_s = time.perf_counter() - t0
+        phases = bt.phase_ms()
         if world > 1:
             t = torch.tensor([conc_s], device="cuda", dtype=torch.float64)
             torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -635,6 +636,24 @@ def main():
         torch.cuda.synchronize()
         seq_s = time.perf_counter() - t0
         sides = sorted(sc["sizeX"] for sc in all_b)
+        # the persistent sweep of the pack (FP32 MIC(0) forward, every scene's
+        # strips as work items) as the autotuner timed it at batch creation
+        # (CUDA events, warm), against 16 B per cell (3 operands in, 1 out)
+        sched = bt.sweep_schedule()
+        my_cells = sum(sc["sizeX"] * sc["sizeY"] for sc in bscs)
+        peak = 6800.0
+        try:
+            peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        except Exception:
+            pass
+        sweep_gbs = 16.0 * my_cells / (sched["sweep_us"] * 1e-6) / 1e9 if sched["sweep_us"] > 0 else None
+        batch_roofline = {"kernel": "mic32 (several scenes, persistent)", "bound": "hbm",
+                          "algorithmic_bytes_per_launch": 16 * my_cells, "avg_launch_us": round(sched["sweep_us"], 2),
+                          "achieved": round(sweep_gbs, 1) if sweep_gbs else None, "peak": peak, "unit": "GB/s",
+                          "frac": round(sweep_gbs / peak, 4) if sweep_gbs else None,
+                          "schedule": sched["schedule"], "ctas": sched["ctas"], "work_items": sched["items"],
+                          "timing": "CUDA events over 3 forward sweeps of every scene, after a warm-up sweep, "
+                                    "by the batch's autotuner at creation"}
         batch = {"scenes": len(all_b), "scenes_per_rank": [len(p) for p in bparts], "cells": bcells, "side_min": sides[0], "side_median": sides[len(sides) // 2],
                  "side_max": sides[-1], "steps": args.batch_steps, "workers": workers,
                  "value": bcells * args.batch_steps / conc_s, "unit": UNIT,
@@ -642,6 +661,10 @@ def main():
                  "sequential_value_rank0": sum(sc["sizeX"] * sc["sizeY"] for sc in bscs) / seq_s,
                  "concurrency_speedup_rank0": seq_s / (conc_s / args.batch_steps),
                  "gpu_launches_per_batch_step": (l1 - l0) // max(args.batch_steps, 1),
+                 "roofline": batch_roofline,
+                 "phase_ms_per_batch_step": {"stages_before_solve": round(phases[0] / args.batch_steps, 2),
+                                             "joint_pressure_solve": round(phases[1] / args.batch_steps, 2),
+                                             "stages_after_solve": round(phases[2] / args.batch_steps, 2)},
                  "warmup_s": warm_s,
                  "timing": "host wall clock around fs2d_batch_step (each frame returns after its device work), "
                            "max over ranks; sequential = rank 0's scenes with one worker, one step"}

@@ -46,6 +46,7 @@ struct fs2d_batch {
     int* err = nullptr;                   // error word and wait controls of the pack's sweeps
     unsigned long long launches = 0;      // kernels of the pack solves
     double sweep_us = 0;                  // the tuned persistent sweep's time (pack_tune)
+    double phase_ms[3] = {0, 0, 0};       // last fs2d_batch_step: before the solve, the solve, after it
 };
 
 namespace fs2d {
@@ -152,7 +153,10 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
     auto parts = assign(b, w);
     const int n = (int)b->sims.size();
     std::vector<int> st(n, 0);
+    using clk = std::chrono::steady_clock;
+    auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
     for (int f = 0; f < nframes; f++) {
+        auto t0 = clk::now();
         int rc = on_workers(parts, b->device, [&](int k) {
             st[k] = 0;
             fs2d_sim* p = b->sims[k];
@@ -162,6 +166,9 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
         });
         if (rc) return rc;
         for (int k = 0; k < n; k++) FS2D_CUDA(cudaStreamWaitEvent(b->stream, b->ready[k], 0));
+        FS2D_CUDA(cudaStreamSynchronize(b->stream));   // the scenes' stages before the solve are done
+        b->phase_ms[0] += ms_since(t0);
+        t0 = clk::now();
         rc = pack_solve(b->pack, b->opt, b->stream, &b->launches, b->err, b->device, nullptr);
         if (rc) return rc;
         int perr = 0;
@@ -173,6 +180,8 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
             return FS2D_ERR_TIMEOUT;
         }
         FS2D_CUDA(cudaEventRecord(b->solved, b->stream));
+        b->phase_ms[1] += ms_since(t0);
+        t0 = clk::now();
         rc = on_workers(parts, b->device, [&](int k) {
             fs2d_sim* p = b->sims[k];
             int r = check_cuda(cudaStreamWaitEvent(sim_of(p)->stream, b->solved, 0), "cudaStreamWaitEvent");
@@ -185,6 +194,7 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
             }
             return r;
         });
+        b->phase_ms[2] += ms_since(t0);
         if (rc) return rc;
     }
     return 0;
@@ -333,6 +343,7 @@ int fs2d_batch_step(fs2d_batch* b, int nframes) {
         b->workers = best;
     }
     if (nframes == 0) return FS2D_OK;
+    b->phase_ms[0] = b->phase_ms[1] = b->phase_ms[2] = 0;
     int rc = b->pack ? run_packed(b, b->workers, nframes) : run(b, b->workers, nframes);
     if (rc) return rc;
     for (size_t k = 0; k < b->status.size(); k++)
@@ -391,6 +402,20 @@ int fs2d_batch_sweep_schedule(fs2d_batch* b, int* schedule, int* ctas, int* item
     if (ctas) *ctas = pk ? pk->sweep_ctas : 0;
     if (items) *items = pk ? pk->nitems : 0;
     if (sweep_us) *sweep_us = pk ? b->sweep_us : 0.0;
+    return FS2D_OK;
+}
+
+int fs2d_batch_set_schedule(fs2d_batch* b, int schedule, int ctas) {
+    if (!b || !b->pack) {
+        fs2d::set_error("fs2d_batch_set_schedule: not a mixed-precision batch");
+        return FS2D_ERR_INVALID;
+    }
+    return fs2d::pack_set_schedule(b->pack, schedule, ctas, b->stream);
+}
+
+int fs2d_batch_phase_ms(fs2d_batch* b, double* ms) {
+    if (!b || !ms) return FS2D_ERR_INVALID;
+    for (int k = 0; k < 3; k++) ms[k] = b->phase_ms[k];
     return FS2D_OK;
 }
 

@@ -106,13 +106,15 @@ struct PackScene {
 };
 
 // Work item of a sweep over several scenes: one strip of 128 columns of one
-// scene; a scene's strips are consecutive items in sweep order.
+// scene.  Any order of the work list is valid in which each strip comes after
+// the strip before it in its scene.
 struct Mic32Item {
     int scene;               // index in the pack's scene table
     int strip;               // strip of the scene (0: first in sweep order)
     int nstrips;             // strips of the scene
     int x0, P32;             // the scene's pack column and padded width
     int y0, NY32;            // the scene's pack row and padded rows
+    int pidx;                // progress counter of this strip (the scene's strips have consecutive counters)
 };
 
 // TMA descriptors of the two FP32 MIC(0) sweeps (see mic32_tma.cuh).
@@ -372,6 +374,9 @@ int pack_solve(Pack* pk, const fs2d_options& opt, cudaStream_t stream, unsigned 
 // scenes by timing forward sweeps of each candidate; *best_us (may be null)
 // receives the chosen sweep's time.
 int pack_tune(Pack* pk, cudaStream_t stream, int* err, int device, unsigned long long* launches, double* best_us);
+// Sets the persistent sweep's schedule (0..3, see pack_tune) and, ctas > 0,
+// its CTA count.
+int pack_set_schedule(Pack* pk, int schedule, int ctas, cudaStream_t stream);
 // Statistics of the handle's last mixed solve (from its scalars); *status =
 // FS2D_ERR_NOT_CONVERGED when it stopped short of its tolerance.
 int mixed_finish(Sim* s, int* status);

@@ -460,8 +460,9 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
         if (strip < nstrips) run_strip(strip, nstrips, 0, a.P32, 0, a.NY32, strip);   // the grid is rounded up to whole clusters
         cluster_sync_all();   // no CTA leaves while a neighbour may still touch its shared memory
     } else {
-        // persistent: items are taken in order, so an item's previous strip was
-        // taken earlier by a co-resident CTA and every wait makes progress
+        // persistent: items are taken in list order and a strip's previous strip
+        // comes earlier in the list, so it was taken earlier by a co-resident CTA
+        // and every wait makes progress
         for (;;) {
             __syncthreads();   // the previous item is finished by both warps
             if (threadIdx.x == 0) *cur_item = atomicAdd(&a.work[0], 1);
@@ -471,7 +472,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             if (it >= a.nitems) break;
             const Mic32Item item = a.items[it];
             if (a.scenes[item.scene].inner->done) continue;   // that scene's inner solve stopped
-            run_strip(item.strip, item.nstrips, item.x0, item.P32, item.y0, item.NY32, it);
+            run_strip(item.strip, item.nstrips, item.x0, item.P32, item.y0, item.NY32, item.pidx);
         }
         if (threadIdx.x == 0) {
             __threadfence();

@@ -204,7 +204,9 @@ __device__ __forceinline__ bool last_block_of(unsigned int* ticket, unsigned nbl
 // bx*kRT .. bx*kRT+kRT-1 of rows by, by + gy, ...; sums are accumulated and
 // reduced in double-float (FP32 pairs), in a fixed order (deterministic), and
 // the scene's last block finishes its scalar.
-constexpr int kRT = 256;
+constexpr int kRT = 256;   // threads per block of the inner kernels
+constexpr int kRV = 4;     // columns per thread
+constexpr int kRC = kRT * kRV;
 
 __device__ __forceinline__ float f_warp_sum(float v) {
 #pragma unroll
@@ -289,6 +291,17 @@ __device__ __forceinline__ void acc_prod(DF& a, float x, float y) {
     else df_add(a, df_prod(x, y));
 }
 
+// The inner kernels see a scene as row segments of kRC columns: thread t of
+// block (bx, by) takes the four adjacent columns bx*kRC + 4t .. +3 (128-bit
+// accesses; the pack's pitch and every scene's column origin are multiples
+// of 128 floats) of rows by, by + gy, ..., over the scene's padded width
+// P32, whose padding holds zeros.
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float4 fma4(float a, float4 x, float4 y) {
+    return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+
 template <bool PLAIN>
 __global__ void __launch_bounds__(kRT) k_dot32(const PackScene* __restrict__ sc, const int* __restrict__ blk,
                                                int pitch, const float* __restrict__ z, const float* __restrict__ r,
@@ -299,13 +312,17 @@ __global__ void __launch_bounds__(kRT) k_dot32(const PackScene* __restrict__ sc,
     if (pcg->done) return;
     const int lb = blockIdx.x - S.blk0;
     const int bx = lb % S.gx, by = lb / S.gx;
-    const int i = bx * kRT + threadIdx.x;
+    const int i = bx * kRC + kRV * threadIdx.x;
     DF a{0.f, 0.f};
-    if (i < S.NX) {
-#pragma unroll 4
+    if (i < S.P32) {
+#pragma unroll 2
         for (int j = by; j < S.NY; j += S.gy) {
             const size_t k = (size_t)S.off + (size_t)j * pitch + i;
-            acc_prod<PLAIN>(a, z[k], r[k]);
+            const float4 zz = ld4(z + k), rr = ld4(r + k);
+            acc_prod<PLAIN>(a, zz.x, rr.x);
+            acc_prod<PLAIN>(a, zz.y, rr.y);
+            acc_prod<PLAIN>(a, zz.z, rr.z);
+            acc_prod<PLAIN>(a, zz.w, rr.w);
         }
     }
     df_block_partial<PLAIN>(a, S.part, by * S.gx + bx, sh);
@@ -326,7 +343,10 @@ __global__ void __launch_bounds__(kRT) k_dot32(const PackScene* __restrict__ sc,
 }
 
 // s_new = z + beta s_old (z on the first iteration), w = A s_new on fluid
-// cells, alpha = sigma / (w . s_new).
+// cells, alpha = sigma / (w . s_new).  A cell is fluid unless its FP32
+// diagonal carries the -0.0 marker of non-fluid cells; the first and last
+// rows and the first column are solid borders, so the neighbour reads stay
+// inside the scene's region.
 template <bool PLAIN>
 __global__ void __launch_bounds__(kRT) k_spmv32(const PackScene* __restrict__ sc, const int* __restrict__ blk,
                                                 int pitch, const float* __restrict__ a0, const float* __restrict__ ax,
@@ -337,27 +357,40 @@ __global__ void __launch_bounds__(kRT) k_spmv32(const PackScene* __restrict__ sc
     PcgScalars* pcg = S.inner;
     if (pcg->done) return;
     const bool first = pcg->first != 0;
-    const float beta = (float)pcg->beta;
+    const float beta = first ? 0.0f : (float)pcg->beta;
     const int lb = blockIdx.x - S.blk0;
     const int bx = lb % S.gx, by = lb / S.gx;
-    const int i = bx * kRT + threadIdx.x;
+    const int i = bx * kRC + kRV * threadIdx.x;
     const int P = pitch;
+    // s of one cell or four, from z and s_old (the first iteration: z alone)
+    auto s1 = [&](size_t k) { return first ? z[k] : fmaf(beta, s_old[k], z[k]); };
+    auto s4 = [&](size_t k) { return first ? ld4(z + k) : fma4(beta, ld4(s_old + k), ld4(z + k)); };
     DF a{0.f, 0.f};
-    if (i < S.NX) {
+    if (i < S.P32) {
         for (int j = by; j < S.NY; j += S.gy) {
             const size_t k = (size_t)S.off + (size_t)j * P + i;
-            const float sc0 = first ? z[k] : fmaf(beta, s_old[k], z[k]);
-            s_new[k] = sc0;
-            float out = 0.0f;
-            if (S.cell[(size_t)j * S.NX + i] == kFluid) {
-                const float sl = first ? z[k - 1] : fmaf(beta, s_old[k - 1], z[k - 1]);
-                const float sr = first ? z[k + 1] : fmaf(beta, s_old[k + 1], z[k + 1]);
-                const float sd = first ? z[k - P] : fmaf(beta, s_old[k - P], z[k - P]);
-                const float su = first ? z[k + P] : fmaf(beta, s_old[k + P], z[k + P]);
-                out = a0[k] * sc0 + ax[k - 1] * sl + ax[k] * sr + ay[k - P] * sd + ay[k] * su;
+            const float4 sc0 = s4(k);
+            st4(s_new + k, sc0);
+            float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (j > 0 && j < S.NY - 1) {
+                const float4 d = ld4(a0 + k);
+                if (!(signbit(d.x) && signbit(d.y) && signbit(d.z) && signbit(d.w))) {
+                    const float sl = i > 0 ? s1(k - 1) : 0.0f;
+                    const float sr = i + kRV < S.P32 ? s1(k + kRV) : 0.0f;
+                    const float axl = i > 0 ? ax[k - 1] : 0.0f;
+                    const float4 axv = ld4(ax + k), ayd = ld4(ay + k - P), ayv = ld4(ay + k);
+                    const float4 sd = s4(k - P), su = s4(k + P);
+                    if (!signbit(d.x)) out.x = d.x * sc0.x + axl * sl + axv.x * sc0.y + ayd.x * sd.x + ayv.x * su.x;
+                    if (!signbit(d.y)) out.y = d.y * sc0.y + axv.x * sc0.x + axv.y * sc0.z + ayd.y * sd.y + ayv.y * su.y;
+                    if (!signbit(d.z)) out.z = d.z * sc0.z + axv.y * sc0.y + axv.z * sc0.w + ayd.z * sd.z + ayv.z * su.z;
+                    if (!signbit(d.w)) out.w = d.w * sc0.w + axv.z * sc0.z + axv.w * sr + ayd.w * sd.w + ayv.w * su.w;
+                }
             }
-            w[k] = out;
-            acc_prod<PLAIN>(a, out, sc0);
+            st4(w + k, out);
+            acc_prod<PLAIN>(a, out.x, sc0.x);
+            acc_prod<PLAIN>(a, out.y, sc0.y);
+            acc_prod<PLAIN>(a, out.z, sc0.z);
+            acc_prod<PLAIN>(a, out.w, sc0.w);
         }
     }
     df_block_partial<PLAIN>(a, S.part, by * S.gx + bx, sh);
@@ -382,18 +415,18 @@ __global__ void __launch_bounds__(kRT) k_axpy32(const PackScene* __restrict__ sc
     const float alpha = (float)pcg->alpha;
     const int lb = blockIdx.x - S.blk0;
     const int bx = lb % S.gx, by = lb / S.gx;
-    const int i = bx * kRT + threadIdx.x;
+    const int i = bx * kRC + kRV * threadIdx.x;
     float m = 0.f;
-    if (i < S.NX) {
+    if (i < S.P32) {
 #pragma unroll 2
         for (int j = by; j < S.NY; j += S.gy) {
             const size_t k = (size_t)S.off + (size_t)j * pitch + i;
-            e[k] = fmaf(alpha, s[k], e[k]);
-            const float rv = fmaf(-alpha, w[k], r[k]);
-            r[k] = rv;
-            const float p = pc[k];
-            rp[k] = rv * (p * p);
-            m = fmaxf(m, fabsf(rv));
+            st4(e + k, fma4(alpha, ld4(s + k), ld4(e + k)));
+            const float4 rv = fma4(-alpha, ld4(w + k), ld4(r + k));
+            st4(r + k, rv);
+            const float4 p = ld4(pc + k);
+            st4(rp + k, make_float4(rv.x * (p.x * p.x), rv.y * (p.y * p.y), rv.z * (p.z * p.z), rv.w * (p.w * p.w)));
+            m = fmaxf(m, fmaxf(fmaxf(fabsf(rv.x), fabsf(rv.y)), fmaxf(fabsf(rv.z), fabsf(rv.w))));
         }
     }
     m = block_max_f(m, sh);
@@ -541,7 +574,7 @@ PackScene scene_entry(Sim* s, int pitch, int x0, int y0) {
     e.x0 = x0;
     e.y0 = y0;
     e.off = (long long)y0 * pitch + x0;
-    e.gx = (s->NX + kRT - 1) / kRT;
+    e.gx = (e.P32 + kRC - 1) / kRC;
     e.gy = std::max(1, std::min(s->NY, 1216 / e.gx));
     e.nb64 = (int)blocks_for(s->N, kT);
     e.cell = s->cell;
@@ -599,7 +632,8 @@ int pack_finish(Pack* pk) {
         e.blk64 = (int)blk64.size();
         blk64.insert(blk64.end(), (size_t)e.nb64, k);
         const int ns = e.P32 / kM32Cols;
-        for (int st = 0; st < ns; st++) items.push_back(Mic32Item{k, st, ns, e.x0, e.P32, e.y0, e.NY32});
+        const int p0 = (int)items.size();
+        for (int st = 0; st < ns; st++) items.push_back(Mic32Item{k, st, ns, e.x0, e.P32, e.y0, e.NY32, p0 + st});
     }
     pk->nblk = (int)blk.size();
     pk->nblk64 = (int)blk64.size();
@@ -925,35 +959,83 @@ __global__ void k_set_done(const PackScene* __restrict__ sc, int n, int done) {
 }  // namespace
 
 // Autotuner of the persistent sweep of several scenes: the schedule (the
-// order in which whole scenes enter the work list: as given, or by
-// decreasing rows, or by decreasing cells) and the number of persistent CTAs
+// order of the work list: whole scenes as given, by decreasing rows or by
+// decreasing cells, or strip-major) and the number of persistent CTAs
 // (all SMs, three quarters, half) are each timed on forward sweeps of the
 // pack (CUDA events, after a warm-up sweep), and the fastest pair is kept.
 // A scene's results do not depend on either choice: its strips are computed
 // in the same order by the same step code whichever CTA takes them.
+// The work list of schedule `variant` (see pack_tune).
+static std::vector<Mic32Item> pack_schedule(const Pack* pk, int variant) {
+    std::vector<int> order(pk->n);
+    std::vector<int> strip0(pk->n);   // progress counter of each scene's first strip (as pack_finish numbers them)
+    for (int k = 0, c = 0; k < pk->n; k++) {
+        strip0[k] = c;
+        c += pk->scenes[k].P32 / kM32Cols;
+    }
+    std::iota(order.begin(), order.end(), 0);
+    if (variant == 1)
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return pk->scenes[a].NY32 > pk->scenes[b].NY32; });
+    if (variant == 2)
+        std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+            return (long long)pk->scenes[a].NY32 * pk->scenes[a].P32 > (long long)pk->scenes[b].NY32 * pk->scenes[b].P32;
+        });
+    std::vector<Mic32Item> items;
+    if (variant < 3) {
+        for (int k : order) {
+            const PackScene& e = pk->scenes[k];
+            const int ns = e.P32 / kM32Cols;
+            for (int st = 0; st < ns; st++)
+                items.push_back(Mic32Item{k, st, ns, e.x0, e.P32, e.y0, e.NY32, strip0[k] + st});
+        }
+    } else {
+        // strip-major: every scene's first strip (scenes by decreasing rows),
+        // then every second strip, ...: a strip is taken long after the strip
+        // it waits for, so its left column is usually there already
+        std::stable_sort(order.begin(), order.end(),
+                         [&](int a, int b) { return pk->scenes[a].NY32 > pk->scenes[b].NY32; });
+        for (int st = 0;; st++) {
+            bool any = false;
+            for (int k : order) {
+                const PackScene& e = pk->scenes[k];
+                const int ns = e.P32 / kM32Cols;
+                if (st < ns) {
+                    items.push_back(Mic32Item{k, st, ns, e.x0, e.P32, e.y0, e.NY32, strip0[k] + st});
+                    any = true;
+                }
+            }
+            if (!any) break;
+        }
+    }
+    return items;
+}
+
+int pack_set_schedule(Pack* pk, int schedule, int ctas, cudaStream_t stream) {
+    if (pk->n < 2 || schedule < 0 || schedule > 3 || ctas < 0) {
+        set_error("schedule %d / %d CTAs: a batch's schedule is 0..3 and its CTA count >= 0", schedule, ctas);
+        return FS2D_ERR_INVALID;
+    }
+    const std::vector<Mic32Item> items = pack_schedule(pk, schedule);
+    FS2D_CUDA(cudaMemcpyAsync(pk->d_items, items.data(), items.size() * sizeof(Mic32Item), cudaMemcpyHostToDevice,
+                              stream));
+    FS2D_CUDA(cudaStreamSynchronize(stream));
+    pk->schedule = schedule;
+    if (ctas > 0) {
+        int dev = 0, sms = 1;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        pk->sweep_ctas = std::max(1, std::min({ctas, sms, pk->nitems}));
+    }
+    return 0;
+}
+
 int pack_tune(Pack* pk, cudaStream_t stream, int* err, int device, unsigned long long* launches, double* best_us) {
     if (pk->n < 2) return 0;
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    std::vector<int> order(pk->n);
     std::vector<std::vector<Mic32Item>> schedules;
-    for (int variant = 0; variant < 3; variant++) {
-        std::iota(order.begin(), order.end(), 0);
-        if (variant == 1)
-            std::stable_sort(order.begin(), order.end(),
-                             [&](int a, int b) { return pk->scenes[a].NY32 > pk->scenes[b].NY32; });
-        if (variant == 2)
-            std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-                return (long long)pk->scenes[a].NY32 * pk->scenes[a].P32 > (long long)pk->scenes[b].NY32 * pk->scenes[b].P32;
-            });
-        std::vector<Mic32Item> items;
-        for (int k : order) {
-            const PackScene& e = pk->scenes[k];
-            const int ns = e.P32 / kM32Cols;
-            for (int st = 0; st < ns; st++) items.push_back(Mic32Item{k, st, ns, e.x0, e.P32, e.y0, e.NY32});
-        }
-        schedules.push_back(items);
-    }
+    for (int variant = 0; variant < 4; variant++) schedules.push_back(pack_schedule(pk, variant));
     const int ctas[3] = {sms, sms * 3 / 4, sms / 2};
     cudaEvent_t e0, e1;
     FS2D_CUDA(cudaEventCreate(&e0));
@@ -963,7 +1045,7 @@ int pack_tune(Pack* pk, cudaStream_t stream, int* err, int device, unsigned long
     double best = 1e300;
     int best_s = 0, best_c = sms;
     int rc = 0;
-    for (int si = 0; si < 3 && !rc; si++) {
+    for (int si = 0; si < (int)schedules.size() && !rc; si++) {
         rc = check_cuda(cudaMemcpyAsync(pk->d_items, schedules[si].data(), schedules[si].size() * sizeof(Mic32Item),
                                         cudaMemcpyHostToDevice, stream), "cudaMemcpyAsync");
         for (int ci = 0; ci < 3 && !rc; ci++) {

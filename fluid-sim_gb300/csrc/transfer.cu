@@ -11,8 +11,9 @@
 // contribution becomes a key (4*e + corner) in its face's bucket (counting
 // sort: count, exclusive scan, scatter); each face then sorts its few keys
 // and adds them in key order — the reference's order — so the sums are
-// bit-identical and independent of thread scheduling.  Atomic mode adds
-// with FP64 atomics instead (fast, order not reproducible).
+// bit-identical and independent of thread scheduling.  Atomic mode sums
+// each warp's contributions per face and adds them with FP64 atomics (fast,
+// order not reproducible).
 //
 // Extrapolation: the reference's breadth-first search assigns every unknown
 // face a layer L = its 4-connected (L1) grid distance to the nearest known
@@ -141,11 +142,44 @@ __global__ void k_p2g_sum(const double2* __restrict__ pos, const double2* __rest
     mask[f] = (sum == 0.0) ? kUnknown : 0u;
 }
 
+// Warp-aggregated add: the lanes of a warp that add to the same face (f >= 0)
+// first sum their (value, weight) pairs — each lane adds its successor's
+// partial sum along the list of lanes with that face, jumping pointers, so
+// after five rounds the first lane of the list holds the list's sum — and
+// only that lane issues the two atomics.  Particles stored near each other
+// (the particle array keeps the cell order of FluidSim2D::create) share faces,
+// so a warp issues a few atomics per face instead of one per particle.
+__device__ __forceinline__ void agg_add(int f, double val, double wt, double* a, double* w) {
+    const int lane = threadIdx.x & 31;
+    const unsigned peers = __match_any_sync(0xffffffffu, f);
+    const unsigned above = lane == 31 ? 0u : peers & (0xffffffffu << (lane + 1));
+    int nxt = above ? __ffs(above) - 1 : -1;
+#pragma unroll
+    for (int d = 0; d < 5; d++) {
+        const int src = nxt < 0 ? lane : nxt;
+        const double v2 = __shfl_sync(0xffffffffu, val, src);
+        const double w2 = __shfl_sync(0xffffffffu, wt, src);
+        const int n2 = __shfl_sync(0xffffffffu, nxt, src);
+        if (nxt >= 0) {
+            val += v2;
+            wt += w2;
+            nxt = n2;
+        }
+    }
+    if (f >= 0 && lane == __ffs(peers) - 1) {
+        atomicAdd(a + f, val);
+        atomicAdd(w + f, wt);
+    }
+}
+
+// P2G, fast mode: bilinear splats summed per warp and face, then FP64 atomics
+// (sums are not in particle order: not reproducible bit for bit).  Whole
+// warps run the aggregation; lanes past the last particle add nothing.
 __global__ void k_p2g_atomic(const double2* __restrict__ pos, const double2* __restrict__ vel, size_t np, double dx,
                              int NX, int NY, double* u, double* udiv, double* v, double* vdiv) {
-    size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
-    if (e >= np) return;
-    double2 p = pos[e], w = vel[e];
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    const bool live = e < np;
+    double2 p = live ? pos[e] : make_double2(0.0, 0.0), w = live ? vel[e] : make_double2(0.0, 0.0);
     double x, y;
     upos(p, dx, x, y);
     Bilinear bu(x, y, NX + 1, NY);
@@ -153,11 +187,8 @@ __global__ void k_p2g_atomic(const double2* __restrict__ pos, const double2* __r
     Bilinear bv(x, y, NX, NY + 1);
 #pragma unroll
     for (int k = 0; k < 4; k++) {
-        int fu = bu.face(k, NX + 1), fv = bv.face(k, NX);
-        atomicAdd(u + fu, bu.contrib(k, w.x));
-        atomicAdd(udiv + fu, bu.contrib(k, 1.0));
-        atomicAdd(v + fv, bv.contrib(k, w.y));
-        atomicAdd(vdiv + fv, bv.contrib(k, 1.0));
+        agg_add(live ? bu.face(k, NX + 1) : -1, bu.contrib(k, w.x), bu.contrib(k, 1.0), u, udiv);
+        agg_add(live ? bv.face(k, NX) : -1, bv.contrib(k, w.y), bv.contrib(k, 1.0), v, vdiv);
     }
 }
 

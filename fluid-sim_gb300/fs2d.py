@@ -105,6 +105,8 @@ SIGNATURES = {
     "fs2d_batch_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "fs2d_batch_destroy": (C.c_int, [C.c_void_p]),
     "fs2d_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
+    "fs2d_batch_phase_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "fs2d_batch_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fs2d_batch_sweep_schedule": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]),
     "fs2d_get_stage_times": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]),
@@ -476,6 +478,17 @@ class Batch:
         sc, ct, it, us = C.c_int(), C.c_int(), C.c_int(), C.c_double()
         _check(load().fs2d_batch_sweep_schedule(self.h, C.byref(sc), C.byref(ct), C.byref(it), C.byref(us)))
         return {"schedule": sc.value, "ctas": ct.value, "items": it.value, "sweep_us": us.value}
+
+    def set_schedule(self, schedule, ctas=0):
+        """Override the autotuned sweep schedule (0..3) and CTA count."""
+        _check(load().fs2d_batch_set_schedule(self.h, int(schedule), int(ctas)))
+
+    def phase_ms(self):
+        """Wall-clock ms of the last step() of a mixed-precision batch: the
+        scenes' stages before the solve, the joint solve, the stages after it."""
+        ms = (C.c_double * 3)()
+        _check(load().fs2d_batch_phase_ms(self.h, ms))
+        return list(ms)
 
     def launch_count(self):
         """Kernels launched so far by the batch and its scenes."""

@@ -255,12 +255,22 @@ int fs2d_batch_launch_count(fs2d_batch* batch, unsigned long long* out);
 /* Mixed precision: the batch solves every scene's pressure system together
  * (one launch per kernel of the inner solve for all scenes; the FP32 MIC(0)
  * sweeps as persistent CTAs over work items of one strip of 128 columns of
- * one scene).  fs2d_batch_create times candidate schedules (0: scenes in the
- * given order, 1: by decreasing rows, 2: by decreasing cells) and CTA counts
- * on forward sweeps and keeps the fastest; this reports the choice, the
- * number of work items and the chosen sweep's time (schedule -1 for an FP64
- * batch).  Any pointer may be NULL. */
+ * one scene).  fs2d_batch_create times candidate schedules and CTA counts
+ * on forward sweeps and keeps the fastest (schedules 0-2 list whole scenes:
+ * as given, by decreasing rows, by decreasing cells; schedule 3 lists every
+ * scene's first strip, then every second strip, ...); this reports the
+ * choice, the number of work items and the chosen sweep's time (schedule -1
+ * for an FP64 batch).  Any pointer may be NULL. */
 int fs2d_batch_sweep_schedule(fs2d_batch* batch, int* schedule, int* ctas, int* items, double* sweepUs);
+/* Overrides the autotuner: schedule 0..3 and, ctas > 0, the number of
+ * persistent CTAs (at most the SM count).  A scene's results do not depend on
+ * either. */
+int fs2d_batch_set_schedule(fs2d_batch* batch, int schedule, int ctas);
+/* Host wall-clock milliseconds of the frames of the last fs2d_batch_step of a
+ * mixed-precision batch, summed over its frames: ms[0] the scenes' stages up
+ * to their pressure solves, ms[1] the batch's joint pressure solve, ms[2] the
+ * remaining stages (zeros for an FP64 batch). */
+int fs2d_batch_phase_ms(fs2d_batch* batch, double* ms);
 /* fs2d_forward / fs2d_backward for every scene of a batch (each a closed box:
  * no EMPTY cell, semi-Lagrangian mode), scenes issued concurrently by the
  * batch's workers (all hardware threads up to 16 while the count is not

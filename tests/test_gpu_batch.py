@@ -43,16 +43,27 @@ def test_batch_matches_scenes_run_alone(workers):
     b.close()
 
 
-def test_batch_of_wide_scenes_matches_scenes_run_alone():
+@pytest.mark.parametrize("schedule,ctas", [(None, 0), (0, 0), (1, 3), (2, 0), (3, 2)])
+def test_batch_of_wide_scenes_matches_scenes_run_alone(schedule, ctas):
     """Scenes of one to three strips of the FP32 sweeps (strips of 128
     columns): the persistent sweep's work items hand columns over between
-    the strips of each scene only."""
+    the strips of each scene only, whatever the schedule of the work list
+    (the autotuner's choice, or each schedule forced, with few CTAs)."""
     scs = scenes.batch_dam_breaks(6, seed=11, lo=100, hi=300)
     b = fs2d.Batch(scs, workers=2, seed=30, **OPTS)
+    sch = b.sweep_schedule()
+    assert 0 <= sch["schedule"] <= 3 and sch["items"] >= 6 and sch["sweep_us"] > 0
+    if schedule is not None:
+        b.set_schedule(schedule, ctas)
+        assert b.sweep_schedule()["schedule"] == schedule
     b.step(2)
     for k, sc in enumerate(scs):
         assert_same(b.scene(k).get_state(FIELDS), alone(sc, 30 + k, 2))
     assert b.launch_count() > 0
+    assert all(ms > 0 for ms in b.phase_ms())
+    if schedule is not None:
+        b.close()
+        return
     # a scene of the batch run alone, on its region of the batch's arrays
     v = b.scene(4)
     assert v.runFrame() in (0, 4)
