@@ -664,7 +664,8 @@ def main():
                  "roofline": batch_roofline,
                  "phase_ms_per_batch_step": {"stages_before_solve": round(phases[0] / args.batch_steps, 2),
                                              "joint_pressure_solve": round(phases[1] / args.batch_steps, 2),
-                                             "stages_after_solve": round(phases[2] / args.batch_steps, 2)},
+                                             "stages_after_solve": round(phases[2] / args.batch_steps, 2),
+                                             "level_set_sweeps_device": round(phases[3] / args.batch_steps, 2)},
                  "warmup_s": warm_s,
                  "timing": "host wall clock around fs2d_batch_step (each frame returns after its device work), "
                            "max over ranks; sequential = rank 0's scenes with one worker, one step"}

@@ -46,7 +46,13 @@ struct fs2d_batch {
     int* err = nullptr;                   // error word and wait controls of the pack's sweeps
     unsigned long long launches = 0;      // kernels of the pack solves
     double sweep_us = 0;                  // the tuned persistent sweep's time (pack_tune)
-    double phase_ms[3] = {0, 0, 0};       // last fs2d_batch_step: before the solve, the solve, after it
+    // last fs2d_batch_step: before the solve, the solve, after it (host
+    // clock), and the batched level-set sweeps (device time, within the first)
+    double phase_ms[4] = {0, 0, 0, 0};
+    // createWaterLevelSet's sweeps of every scene, one launch per sweep
+    fs2d::LsBatch* ls = nullptr;
+    cudaEvent_t swept = nullptr;          // the batched sweeps are done
+    cudaEvent_t ls_t0 = nullptr, ls_t1 = nullptr;
 };
 
 namespace fs2d {
@@ -157,10 +163,26 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
     auto ms_since = [](clk::time_point t) { return std::chrono::duration<double, std::milli>(clk::now() - t).count(); };
     for (int f = 0; f < nframes; f++) {
         auto t0 = clk::now();
+        // createWaterLevelSet: seeds per scene, every scene's sweeps in one
+        // launch per sweep on the batch's stream, the rest per scene
         int rc = on_workers(parts, b->device, [&](int k) {
             st[k] = 0;
             fs2d_sim* p = b->sims[k];
-            int r = frame_stages(p, 0, frame_solve_stage(p) + 1, &st[k], 1);
+            int r = frame_levelset(p, 1);
+            if (!r) r = check_cuda(cudaEventRecord(b->ready[k], sim_of(p)->stream), "cudaEventRecord");
+            return r;
+        });
+        if (rc) return rc;
+        for (int k = 0; k < n; k++) FS2D_CUDA(cudaStreamWaitEvent(b->stream, b->ready[k], 0));
+        FS2D_CUDA(cudaEventRecord(b->ls_t0, b->stream));
+        if ((rc = ls_batch_sweeps(b->ls, b->stream, b->err, &b->launches))) return rc;
+        FS2D_CUDA(cudaEventRecord(b->ls_t1, b->stream));
+        FS2D_CUDA(cudaEventRecord(b->swept, b->stream));
+        rc = on_workers(parts, b->device, [&](int k) {
+            fs2d_sim* p = b->sims[k];
+            int r = check_cuda(cudaStreamWaitEvent(sim_of(p)->stream, b->swept, 0), "cudaStreamWaitEvent");
+            if (!r) r = frame_levelset(p, 2);
+            if (!r) r = frame_stages(p, 1, frame_solve_stage(p) + 1, &st[k], 1);
             if (!r) r = check_cuda(cudaEventRecord(b->ready[k], sim_of(p)->stream), "cudaEventRecord");
             return r;
         });
@@ -168,6 +190,9 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
         for (int k = 0; k < n; k++) FS2D_CUDA(cudaStreamWaitEvent(b->stream, b->ready[k], 0));
         FS2D_CUDA(cudaStreamSynchronize(b->stream));   // the scenes' stages before the solve are done
         b->phase_ms[0] += ms_since(t0);
+        float ls_ms = 0;
+        cudaEventElapsedTime(&ls_ms, b->ls_t0, b->ls_t1);
+        b->phase_ms[3] += ls_ms;
         t0 = clk::now();
         rc = pack_solve(b->pack, b->opt, b->stream, &b->launches, b->err, b->device, nullptr);
         if (rc) return rc;
@@ -176,7 +201,7 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
         FS2D_CUDA(cudaStreamSynchronize(b->stream));
         if (perr) {
             FS2D_CUDA(cudaMemset(b->err, 0, sizeof(int)));
-            set_error("a wavefront sweep of the batch's pressure solve timed out");
+            set_error("a wavefront sweep of the batch (level set or pressure solve) timed out");
             return FS2D_ERR_TIMEOUT;
         }
         FS2D_CUDA(cudaEventRecord(b->solved, b->stream));
@@ -306,6 +331,10 @@ int fs2d_batch_create(const fs2d_config* cfgs, int n, const fs2d_options* opt, i
             rc = check_cuda(cudaMemcpy(b->err, wd, sizeof(wd), cudaMemcpyHostToDevice), "cudaMemcpy");
         }
         if (!rc) rc = pack_tune(b->pack, b->stream, b->err, b->device, &b->launches, &b->sweep_us);
+        if (!rc) b->ls = ls_batch_create(ss.data(), n, b->device, &rc);
+        if (!rc) rc = check_cuda(cudaEventCreateWithFlags(&b->swept, cudaEventDisableTiming), "cudaEventCreate");
+        if (!rc) rc = check_cuda(cudaEventCreate(&b->ls_t0), "cudaEventCreate");
+        if (!rc) rc = check_cuda(cudaEventCreate(&b->ls_t1), "cudaEventCreate");
         if (rc) {
             fs2d_batch_destroy(b);
             return rc;
@@ -343,7 +372,7 @@ int fs2d_batch_step(fs2d_batch* b, int nframes) {
         b->workers = best;
     }
     if (nframes == 0) return FS2D_OK;
-    b->phase_ms[0] = b->phase_ms[1] = b->phase_ms[2] = 0;
+    b->phase_ms[0] = b->phase_ms[1] = b->phase_ms[2] = b->phase_ms[3] = 0;
     int rc = b->pack ? run_packed(b, b->workers, nframes) : run(b, b->workers, nframes);
     if (rc) return rc;
     for (size_t k = 0; k < b->status.size(); k++)
@@ -389,6 +418,9 @@ int fs2d_batch_destroy(fs2d_batch* b) {
     for (cudaEvent_t e : b->ready)
         if (e) cudaEventDestroy(e);
     if (b->solved) cudaEventDestroy(b->solved);
+    fs2d::ls_batch_free(b->ls);
+    for (cudaEvent_t e : {b->swept, b->ls_t0, b->ls_t1})
+        if (e) cudaEventDestroy(e);
     if (b->err) cudaFree(b->err);
     if (b->stream) cudaStreamDestroy(b->stream);
     delete b;
@@ -415,7 +447,7 @@ int fs2d_batch_set_schedule(fs2d_batch* b, int schedule, int ctas) {
 
 int fs2d_batch_phase_ms(fs2d_batch* b, double* ms) {
     if (!b || !ms) return FS2D_ERR_INVALID;
-    for (int k = 0; k < 3; k++) ms[k] = b->phase_ms[k];
+    for (int k = 0; k < 4; k++) ms[k] = b->phase_ms[k];
     return FS2D_OK;
 }
 

@@ -483,6 +483,23 @@ int frame_stages(fs2d_sim* p, int k0, int k1, int* status, int solve_part) {
     return 0;
 }
 
+// createWaterLevelSet (stage 0 in both modes) of a batch frame, around the
+// batch's sweeps: part 1 records the stage's start and queues the seeds,
+// part 2 the rest of the stage.
+int frame_levelset(fs2d_sim* p, int part) {
+    Host* h = H(p);
+    Sim* s = &h->sim;
+    if (part == 1) {
+        FS2D_CUDA(cudaEventRecord(s->ev[0], s->stream));
+        return levelset_seed(s);
+    }
+    int rc = levelset_finish(s);
+    if (rc) return rc;
+    FS2D_CUDA(cudaEventRecord(s->ev[1], s->stream));
+    h->stats_pending = true;
+    return 0;
+}
+
 int frame_solve_stage(fs2d_sim* p) {
     Sim* s = &H(p)->sim;
     const int* st = s->mode == FS2D_SEMILAGRANGIAN ? kSlStages : kPicStages;

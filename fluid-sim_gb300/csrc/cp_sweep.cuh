@@ -234,11 +234,20 @@ struct CpArgs {
     double dx, dr;
 };
 
+// One scene of a launch over several scenes: its tensor maps and arguments
+// (progress, base, err and skip come from the launch's WaveWork).
+struct CpScene {   // aligned as CUtensorMap
+    CpMaps maps;
+    CpArgs a;
+};
+
 // Sweep direction (SX, SY): columns visited in +x (SX > 0) or -x order, rows
-// in +y or -y order.
-template <int SX, int SY>
-__global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ CpMaps maps, const CpArgs a) {
-    if (a.skip != nullptr && *a.skip) return;
+// in +y or -y order.  SEVERAL = false: one scene, CTA b = strip b.
+// SEVERAL = true: persistent CTAs over w's work items (see WaveWork).
+template <int SX, int SY, bool SEVERAL>
+__global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ CpMaps maps1, const CpArgs a1,
+                                                      const WaveWork w) {
+    if (!SEVERAL && a1.skip != nullptr && *a1.skip) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     int* tiles = reinterpret_cast<int*>(smem_raw);
     float4* gring = reinterpret_cast<float4*>(smem_raw + (size_t)kCpSlots * kCpTileBytes);  // [33][kCpR]
@@ -254,11 +263,14 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
     volatile int* quit = ctr + 4;
     volatile int* tiles_done = ctr + 5;
     volatile int* tiles_freed = ctr + 6;
+    volatile int* cur_item = ctr + 7;
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(const_cast<int*>(ctr) + 16);
-
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int strip = blockIdx.x;
+
+  // One strip of one scene (the whole grid of a launch per scene, or one
+  // work item of a launch over several scenes).
+  auto run_strip = [&](const CpMaps& maps, const CpArgs& a, const int strip) {
     const int NX = a.NX, NY = a.NY, P = a.P;
     const int nstrips = (NY + 31) / 32;
     const int nt = P / kCpCols;
@@ -370,7 +382,10 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
             if (moved) {
                 idle = 0;
             } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(a.err))) {
-                if (lane == 0) atomicOr(a.err, 1);
+                if (lane == 0) {
+                    atomicOr(a.err, 1);
+                    *quit = 1;
+                }
                 break;
             }
         }
@@ -412,6 +427,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
             if (++polls > kWaveSpinLimit) {
                 failed = true;
                 atomicOr(a.err, 1);
+                *quit = 1;   // a copy may still be in flight: this CTA takes no further strip
                 break;
             }
         }
@@ -553,6 +569,43 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
     // t + 1 < nt), so no TMA load is in flight when the CTA exits
     if (lane == 0) *tiles_done = nt;
     (void)failed;
+  };
+
+    if (!SEVERAL) {
+        run_strip(maps1, a1, blockIdx.x);
+        return;
+    }
+    const CpScene* scenes = static_cast<const CpScene*>(w.scenes);
+    if (threadIdx.x == 0) *quit = 0;
+    bool used = false;   // the ring barriers hold an earlier strip's phases
+    for (;;) {
+        __syncthreads();   // both warps are done with the previous item
+        if (*quit) break;  // a wait of this CTA gave up: its rings and barriers stay as they are
+        if (threadIdx.x == 0) *cur_item = atomicAdd(&w.work[0], 1);
+        __syncthreads();
+        const int it = *cur_item;
+        if (it >= w.nitems) break;
+        const WaveItem item = w.items[it];
+        if (w.skip[item.scene]) continue;   // no cell of that scene would change in this sweep
+        const CpScene* sc = scenes + item.scene;
+        CpArgs a = sc->a;
+        a.progress = w.progress + (item.pidx - item.strip);
+        a.base = w.base;
+        a.err = w.err;
+        a.skip = nullptr;
+        if (used && threadIdx.x == 0)   // run_strip initialises them again (same thread, in order)
+            for (int k = 0; k < kCpSlots; k++) mbar_inval(bars + k);
+        used = true;
+        run_strip(sc->maps, a, item.strip);
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&w.work[1], 1) == (int)gridDim.x - 1) {   // the last CTA resets the counters
+            w.work[0] = 0;
+            w.work[1] = 0;
+            __threadfence();
+        }
+    }
 }
 
 }  // namespace fs2d

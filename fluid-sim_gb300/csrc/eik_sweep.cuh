@@ -122,9 +122,20 @@ __device__ __forceinline__ double ek_value(unsigned long long w0, unsigned long 
 }
 __device__ __forceinline__ bool ek_changed(unsigned long long w1) { return ((w1 >> 32) & 1ull) != 0; }
 
-template <int SX, int SY>
-__global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ EkMaps maps, const EkArgs a) {
-    if (a.skip != nullptr && *a.skip) return;
+// One scene of a launch over several scenes: its tensor maps and arguments
+// (progress, base, err and skip come from the launch's WaveWork; the
+// update region i_lo .. j_hi from the direction).
+struct EkScene {   // aligned as CUtensorMap
+    EkMaps maps;
+    EkArgs a;
+};
+
+// SEVERAL = false: one scene, CTA b = strip b, in clusters.  SEVERAL = true:
+// persistent CTAs over w's work items (see WaveWork), no clusters.
+template <int SX, int SY, bool SEVERAL>
+__global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ EkMaps maps1, const EkArgs a1,
+                                                       const WaveWork w) {
+    if (!SEVERAL && a1.skip != nullptr && *a1.skip) return;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     double* tiles = reinterpret_cast<double*>(smem_raw);
     unsigned char* mtiles = smem_raw + (size_t)kEkSlots * kEkTileBytes;
@@ -138,11 +149,19 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
     volatile int* quit = ctr + 2;
     volatile int* tiles_done = ctr + 3;
     volatile int* tiles_freed = ctr + 4;
+    volatile int* cur_item = ctr + 5;
     unsigned long long* bars = reinterpret_cast<unsigned long long*>(const_cast<int*>(ctr) + 16);
-
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int strip = blockIdx.x;
+    // every CTA of the cluster (one scene) or of the block (several scenes)
+    auto sync_all = [&]() {
+        if (SEVERAL) __syncthreads();
+        else cluster_sync_all();
+    };
+
+  // One strip of one scene (the whole grid of a launch per scene, or one
+  // work item of a launch over several scenes).
+  auto run_strip = [&](const EkMaps& maps, const EkArgs& a, const int strip) {
     const int NX = a.NX, NY = a.NY, P = a.P;
     const int nstrips = (NY + kEkRows - 1) / kEkRows;
     const int nt = P / kEkCols;
@@ -152,7 +171,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
     const long long spin = wave_spin(a.err);
     const bool below_in_grid = strip > 0;
     const bool active = strip < nstrips;                       // the grid is rounded up to whole clusters
-    const unsigned crank = cluster_ctarank(), csize = cluster_nctarank();
+    const unsigned crank = SEVERAL ? 0u : cluster_ctarank(), csize = SEVERAL ? 1u : cluster_nctarank();
     const bool prev_local = below_in_grid && crank > 0;        // the previous strip fills this ring
     const bool next_local = publishes && crank + 1 < csize;    // this strip fills the next strip's ring
     const int y0 = SY > 0 ? kEkRows * strip : NY - kEkRows - kEkRows * strip;   // memory row of box row 0
@@ -168,7 +187,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
     }
     for (int k = threadIdx.x; k < 2 * kEkRing; k += blockDim.x) bnd[k] = ~0ull;      // no column matches
     for (int k = threadIdx.x; k < 2 * kEkTopRing; k += blockDim.x) top[k] = ~0ull;
-    cluster_sync_all();   // every ring and counter of the cluster is initialised
+    sync_all();   // every ring and counter of the cluster is initialised
 
     if (warp == 1 && active) {
         // ---------------- I/O warp ----------------
@@ -274,7 +293,10 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
             if (moved) {
                 idle = 0;
             } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(a.err))) {
-                if (lane == 0) atomicOr(a.err, 1);
+                if (lane == 0) {
+                    atomicOr(a.err, 1);
+                    *quit = 1;
+                }
                 break;
             }
         }
@@ -305,6 +327,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                 if (++polls > kWaveSpinLimit) {
                     failed = true;
                     atomicOr(a.err, 1);
+                    *quit = 1;   // a copy may still be in flight: this CTA takes no further strip
                     break;
                 }
             }
@@ -428,7 +451,48 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         }
         (void)failed;
     }
-    cluster_sync_all();   // no CTA leaves while a neighbour may still touch its shared memory
+    sync_all();   // no CTA leaves while a neighbour may still touch its shared memory
+  };
+
+    if (!SEVERAL) {
+        run_strip(maps1, a1, blockIdx.x);
+        return;
+    }
+    const EkScene* scenes = static_cast<const EkScene*>(w.scenes);
+    if (threadIdx.x == 0) *quit = 0;
+    bool used = false;   // the ring barriers hold an earlier strip's phases
+    for (;;) {
+        __syncthreads();   // both warps are done with the previous item
+        if (*quit) break;  // a wait of this CTA gave up: its rings and barriers stay as they are
+        if (threadIdx.x == 0) *cur_item = atomicAdd(&w.work[0], 1);
+        __syncthreads();
+        const int it = *cur_item;
+        if (it >= w.nitems) break;
+        const WaveItem item = w.items[it];
+        if (w.skip[item.scene]) continue;   // no cell of that scene would change in this sweep
+        const EkScene* sc = scenes + item.scene;
+        EkArgs a = sc->a;
+        a.progress = w.progress + (item.pidx - item.strip);
+        a.base = w.base;
+        a.err = w.err;
+        a.skip = nullptr;
+        if (used && threadIdx.x == 0)   // run_strip initialises them again (same thread, in order)
+            for (int k = 0; k < kEkSlots; k++) mbar_inval(bars + k);
+        used = true;
+        a.i_lo = SX > 0 ? 1 : 0;
+        a.i_hi = SX > 0 ? a.NX - 1 : a.NX - 2;
+        a.j_lo = SY > 0 ? 1 : 0;
+        a.j_hi = SY > 0 ? a.NY - 1 : a.NY - 2;
+        run_strip(sc->maps, a, item.strip);
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(&w.work[1], 1) == (int)gridDim.x - 1) {   // the last CTA resets the counters
+            w.work[0] = 0;
+            w.work[1] = 0;
+            __threadfence();
+        }
+    }
 }
 
 }  // namespace fs2d

@@ -165,4 +165,25 @@ __device__ __forceinline__ bool wave_held(const int* err, int kind, int strip) {
     return (err[1] & kind) != 0 && err[2] == strip;
 }
 
+// Level-set sweeps of several scenes in one launch: persistent CTAs take
+// work items (one strip of one scene each) in list order from work[0];
+// work[1] counts the CTAs that finished, and the last one resets both for
+// the next launch.  A strip's previous strip comes earlier in the list, so
+// the CTA it waits for took its item earlier and is running.  Progress
+// counter pidx belongs to the item's strip, pidx - 1 to the scene's previous
+// strip; an item of a scene whose skip flag is set is passed over.
+struct WaveItem {
+    int scene, strip, pidx;
+};
+struct WaveWork {
+    const void* scenes;                  // CpScene[] or EkScene[]
+    const WaveItem* items;
+    int nitems;
+    int* work;
+    unsigned long long* progress;
+    unsigned long long base;
+    int* err;
+    const int* skip;                     // per scene
+};
+
 }  // namespace fs2d

@@ -344,6 +344,15 @@ inline unsigned int blocks_for(size_t n, int threads) { return (unsigned int)((n
 
 // ---- stage entry points (implemented in the per-stage .cu files) ----
 int levelset_create(Sim* s);              // createWaterLevelSet
+// createWaterLevelSet of a batch of scenes: levelset_seed per scene, then
+// ls_batch_sweeps (every scene's sweeps, one launch per sweep for all of
+// them), then levelset_finish per scene.
+int levelset_seed(Sim* s);
+int levelset_finish(Sim* s);
+struct LsBatch;
+LsBatch* ls_batch_create(Sim* const* sims, int n, int device, int* rc);
+void ls_batch_free(LsBatch* b);
+int ls_batch_sweeps(LsBatch* b, cudaStream_t stream, int* err, unsigned long long* launches);
 int p2g(Sim* s);                          // transferVelocityToGrid
 int sl_advect(Sim* s);                    // applySemiLagrangianAdvection
 int apply_gravity(Sim* s);                // applyGravity
@@ -411,6 +420,7 @@ void rollout_free(Sim* s);
 
 // ---- frames in parts (capi.cu), for batches that solve their scenes together ----
 int frame_stages(fs2d_sim* p, int k0, int k1, int* status, int solve_part = 0);
+int frame_levelset(fs2d_sim* p, int part);
 int frame_solve_stage(fs2d_sim* p);   // index of applyProjection in the frame's stage order
 int frame_close(fs2d_sim* p, int rc, int status);
 Sim* sim_of(fs2d_sim* p);

@@ -115,14 +115,10 @@ __global__ void k_cp_const(CpConst* kc, int NX, int NY, double dx, double dr) {
 
 // Would any cell change under one closest-point update with the current
 // values?  (Every candidate in the reference's order, against the cell's own.)
-__global__ void k_cp_check(const int* __restrict__ t, const float4* __restrict__ pos_df,
-                           const double2* __restrict__ pos, const float2* __restrict__ xtab,
-                           const float2* __restrict__ ytab, const CpConst* __restrict__ kcp, int NX, int NY, int P,
-                           double dx, double dr, int* noop) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y;
-    if (i >= NX) return;
-    const CpConst kc = *kcp;
+__device__ __forceinline__ bool cp_check_cell(const int* __restrict__ t, const float4* __restrict__ pos_df,
+                                              const double2* __restrict__ pos, const float2* __restrict__ xtab,
+                                              const float2* __restrict__ ytab, const CpConst& kc, int NX, int NY,
+                                              int P, double dx, double dr, int i, int j) {
     const size_t c = (size_t)j * P + i;
     const float2 xc = xtab[i], yc = ytab[j];
     CpCur cur;
@@ -148,18 +144,33 @@ __global__ void k_cp_check(const int* __restrict__ t, const float4* __restrict__
         cur.t = cp_cell_slow(own, own_p, nb[0], np4[0], true, nb[1], np4[1], true, nb[2], np4[2], true, nb[3], np4[3],
                              true, xc, yc, kc, pos, i, j, dx, dr, &sp);
     }
-    if (cur.t != own) *noop = 0;
+    return cur.t != own;
+}
+
+__global__ void k_cp_check(const int* __restrict__ t, const float4* __restrict__ pos_df,
+                           const double2* __restrict__ pos, const float2* __restrict__ xtab,
+                           const float2* __restrict__ ytab, const CpConst* __restrict__ kcp, int NX, int NY, int P,
+                           double dx, double dr, int* noop) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= NX) return;
+    const CpConst kc = *kcp;
+    if (cp_check_cell(t, pos_df, pos, xtab, ytab, kc, NX, NY, P, dx, dr, i, j)) *noop = 0;
 }
 
 // phi = d(t) of every cell (HUGE_VAL without a particle), as the reference
 // stores it with t.
+__device__ __forceinline__ void cp_phi_cell(const int* __restrict__ t, const double2* __restrict__ pos, size_t np,
+                                            double* phi, int NX, int P, double dx, double dr, int i, int j) {
+    const int e = t[(size_t)j * P + i];
+    phi[(size_t)j * NX + i] = (e < 0 || (size_t)e >= np) ? HUGE_VAL : corner_dist(pos[e], i, j, dx, dr);
+}
 __global__ void k_cp_phi(const int* __restrict__ t, const double2* __restrict__ pos, size_t np, double* phi, int NX,
                          int NY, int P, double dx, double dr) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
     if (i >= NX) return;
-    const int e = t[(size_t)j * P + i];
-    phi[(size_t)j * NX + i] = (e < 0 || (size_t)e >= np) ? HUGE_VAL : corner_dist(pos[e], i, j, dx, dr);
+    cp_phi_cell(t, pos, np, phi, NX, P, dx, dr, i, j);
 }
 
 // ---- redistance ----
@@ -167,10 +178,8 @@ __global__ void k_cp_phi(const int* __restrict__ t, const double2* __restrict__ 
 // Surface flags from the sign changes the reference tests
 // (src/FluidSim2D.cpp:803-834: pairs with the base cell in [0,NX-2]x[0,NY-2]),
 // then non-surface negative cells -> -inf (:836-842).  Reads phi, writes out.
-__global__ void k_surface(const double* __restrict__ phi, double* out, int NX, int NY, int P) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y;
-    if (i >= NX) return;
+__device__ __forceinline__ void surface_cell(const double* __restrict__ phi, double* out, int NX, int NY, int P, int i,
+                                             int j) {
     size_t c = (size_t)j * NX + i;
     double p = phi[c];
     bool surf = false;
@@ -179,6 +188,12 @@ __global__ void k_surface(const double* __restrict__ phi, double* out, int NX, i
     if (i <= NX - 2 && j <= NY - 2 && p * phi[c + NX] < 0) surf = true;
     if (i <= NX - 2 && j >= 1 && phi[c - NX] * p < 0) surf = true;
     out[(size_t)j * P + i] = (!surf && p < 0) ? -HUGE_VAL : p;
+}
+__global__ void k_surface(const double* __restrict__ phi, double* out, int NX, int NY, int P) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= NX) return;
+    surface_cell(phi, out, NX, NY, P, i, j);
 }
 
 // One Eikonal update (src/FluidSim2D.cpp:848-857); a = upwind x neighbour,
@@ -194,11 +209,8 @@ __device__ __forceinline__ double eikonal(double own, double a, double b, double
 }
 
 
-__global__ void k_eik_check(const double* __restrict__ phi, uint8_t* mask, int NX, int NY, int P, int i_lo,
-                            int i_hi, int j_lo, int j_hi, int sx, int sy, double dx, int* noop) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    int j = blockIdx.y;
-    if (i >= NX) return;
+__device__ __forceinline__ bool eik_check_cell(const double* __restrict__ phi, uint8_t* mask, int P, int i_lo,
+                                               int i_hi, int j_lo, int j_hi, int sx, int sy, double dx, int i, int j) {
     size_t c = (size_t)j * P + i;
     bool ch = false;
     if (i >= i_lo && i <= i_hi && j >= j_lo && j <= j_hi) {
@@ -209,7 +221,14 @@ __global__ void k_eik_check(const double* __restrict__ phi, uint8_t* mask, int N
         }
     }
     mask[c] = ch ? 1 : 0;
-    if (ch) *noop = 0;
+    return ch;
+}
+__global__ void k_eik_check(const double* __restrict__ phi, uint8_t* mask, int NX, int NY, int P, int i_lo,
+                            int i_hi, int j_lo, int j_hi, int sx, int sy, double dx, int* noop) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int j = blockIdx.y;
+    if (i >= NX) return;
+    if (eik_check_cell(phi, mask, P, i_lo, i_hi, j_lo, j_hi, sx, sy, dx, i, j)) *noop = 0;
 }
 
 // Min-smoothing pass (src/FluidSim2D.cpp:904-919): Jacobi, interior cells.
@@ -305,7 +324,7 @@ static int launch_cp_sweep_dir(Sim* s, const int* skip) {
         return FS2D_ERR_INVALID;
     }
     static std::atomic<unsigned long long> configured{0};
-    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)cp_sweep_kernel<SX, SY>, (int)kCpSmem)) return rc0;
+    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)cp_sweep_kernel<SX, SY, false>, (int)kCpSmem)) return rc0;
     CpArgs a;
     a.pos_df = s->pos_df;
     a.pos = s->pos;
@@ -325,10 +344,11 @@ static int launch_cp_sweep_dir(Sim* s, const int* skip) {
     a.dx = s->dx;
     a.dr = s->dr;
     const CpMaps* maps = reinterpret_cast<const CpMaps*>(s->cpmaps->b);
-    void* args[] = {(void*)maps, (void*)&a};
+    WaveWork w{};
+    void* args[] = {(void*)maps, (void*)&a, (void*)&w};
     s->launches++;
     long long kt = ktimer_begin(s, "cp_sweep");
-    int rc = check_cuda(cudaLaunchCooperativeKernel((const void*)cp_sweep_kernel<SX, SY>, dim3(nstrips), dim3(64),
+    int rc = check_cuda(cudaLaunchCooperativeKernel((const void*)cp_sweep_kernel<SX, SY, false>, dim3(nstrips), dim3(64),
                                                     args, kCpSmem, s->stream),
                         "cp_sweep");
     ktimer_end(s, kt);
@@ -343,7 +363,7 @@ static int launch_eik_sweep_dir(Sim* s, const WaveGeom& g, const int* skip) {
         return FS2D_ERR_INVALID;
     }
     static std::atomic<unsigned long long> configured{0};
-    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)eik_sweep_kernel<SX, SY>, (int)kEkSmem)) return rc0;
+    if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)eik_sweep_kernel<SX, SY, false>, (int)kEkSmem)) return rc0;
     EkArgs a;
     a.hb = reinterpret_cast<double2*>(s->cp_hb_p);
     a.progress = s->progress;
@@ -360,16 +380,17 @@ static int launch_eik_sweep_dir(Sim* s, const WaveGeom& g, const int* skip) {
     a.dx = s->dx;
     a.c2 = 2 * s->dx * s->dx;
     const EkMaps* maps = reinterpret_cast<const EkMaps*>(s->ekmaps->b);
-    void* args[] = {(void*)maps, (void*)&a};
+    WaveWork w{};
+    void* args[] = {(void*)maps, (void*)&a, (void*)&w};
     s->launches++;
     long long kt = ktimer_begin(s, "eik_sweep");
     int& cs = s->ek_cluster;   // 0: not chosen yet
-    if (cs == 0) cs = choose_cluster((const void*)eik_sweep_kernel<SX, SY>, nstrips, 64, kEkSmem);
-    cudaError_t e = launch_clustered((const void*)eik_sweep_kernel<SX, SY>, nstrips, cs, 64, kEkSmem, s->stream, args);
+    if (cs == 0) cs = choose_cluster((const void*)eik_sweep_kernel<SX, SY, false>, nstrips, 64, kEkSmem);
+    cudaError_t e = launch_clustered((const void*)eik_sweep_kernel<SX, SY, false>, nstrips, cs, 64, kEkSmem, s->stream, args);
     if (e != cudaSuccess && cs > 1) {   // clusters refused: plain cooperative launch
         (void)cudaGetLastError();
         cs = 1;
-        e = launch_clustered((const void*)eik_sweep_kernel<SX, SY>, nstrips, 1, 64, kEkSmem, s->stream, args);
+        e = launch_clustered((const void*)eik_sweep_kernel<SX, SY, false>, nstrips, 1, 64, kEkSmem, s->stream, args);
     }
     int rc = check_cuda(e, "eik_sweep");
     ktimer_end(s, kt);
@@ -412,13 +433,13 @@ int cp_setup_maps(Sim* s) {
     return 0;
 }
 
-int levelset_create(Sim* s) {
+// createWaterLevelSet in parts around its two groups of sweeps (a batch of
+// scenes runs each sweep of all its scenes in one launch, ls_batch_sweeps).
+// Seeds (constructFromParticles), float-pair positions, corner tables and
+// the constants of the closest-point decisions.
+int levelset_seed(Sim* s) {
     const int NX = s->NX, NY = s->NY;
     const int T = 256;
-    // one extra int per sweep for the no-op flags, at the end of `partial`'s
-    // companion: reuse the err-adjacent scratch in `max_layer`
-    int* noop = (int*)s->max_layer + 4;
-
     const int P = s->P;
     const size_t NP = (size_t)P * NY;
     // constructFromParticles: seed (pitched t)
@@ -436,37 +457,18 @@ int levelset_create(Sim* s) {
     if (s->np > 0) FS2D_LAUNCH(s, k_posdf, blocks_for(s->np, T), T, 0, s->pos, s->np, s->pos_df, s->cpc);
     FS2D_LAUNCH(s, k_cp_tabs, blocks_for(std::max(P, NY), T), T, 0, s->cp_tab, s->cp_tab + P, P, NY, s->dx);
     FS2D_LAUNCH(s, k_cp_const, 1, 1, 0, s->cpc, NX, NY, s->dx, s->dr);
+    return 0;
+}
 
-    // fastSweepIterate: 4 x {(+,+), (-,+), (+,-), (-,-)}
-    const int dirs[4][2] = {{1, 1}, {-1, 1}, {1, -1}, {-1, -1}};
+// The reference's sweep directions, in its order: 4 x {(+,+), (-,+), (+,-), (-,-)}.
+static const int kDirs[4][2] = {{1, 1}, {-1, 1}, {1, -1}, {-1, -1}};
+
+// Smoothing, labels and statistics (after the Eikonal sweeps).
+int levelset_finish(Sim* s) {
+    const int NX = s->NX, NY = s->NY;
+    const int T = 256;
     dim3 g2(blocks_for(NX, 128), NY);
-    for (int rep = 0; rep < 4; rep++) {
-        for (int d = 0; d < 4; d++) {
-            FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));  // -1 -> nonzero = no-op
-            FS2D_LAUNCH(s, k_cp_check, g2, 128, 0, s->t, s->pos_df, s->pos, s->cp_tab, s->cp_tab + P, s->cpc, NX, NY,
-                        P, s->dx, s->dr, noop);
-            int rc = launch_cp_sweep(s, dirs[d][0], dirs[d][1], noop);
-            if (rc) return rc;
-        }
-    }
-    FS2D_LAUNCH(s, k_cp_phi, g2, 128, 0, s->t, s->pos, s->np, s->phi, NX, NY, P, s->dx, s->dr);
-
-    // redistance on the pitched copy phi_p
-    FS2D_LAUNCH(s, k_surface, g2, 128, 0, s->phi, s->phi_p, NX, NY, P);
-    for (int rep = 0; rep < 4; rep++) {
-        for (int d = 0; d < 4; d++) {
-            int sx = dirs[d][0], sy = dirs[d][1];
-            int i_lo = sx > 0 ? 1 : 0, i_hi = sx > 0 ? NX - 1 : NX - 2;
-            int j_lo = sy > 0 ? 1 : 0, j_hi = sy > 0 ? NY - 1 : NY - 2;
-            FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));
-            FS2D_LAUNCH(s, k_eik_check, g2, 128, 0, s->phi_p, s->emask, NX, NY, P, i_lo, i_hi, j_lo, j_hi, sx, sy,
-                        s->dx, noop);
-            WaveGeom g{sx, sy, i_lo, i_hi, j_lo, j_hi};
-            int rc = launch_eik_sweep(s, g, noop);
-            if (rc) return rc;
-        }
-    }
-    FS2D_LAUNCH(s, k_smooth, g2, 128, 0, s->phi_p, P, s->phi, NX, NY);
+    FS2D_LAUNCH(s, k_smooth, g2, 128, 0, s->phi_p, s->P, s->phi, NX, NY);
     FS2D_LAUNCH(s, k_smooth, g2, 128, 0, s->phi, NX, s->phi_tmp, NX, NY);
 
     // labels + statistics (phi_tmp -> phi)
@@ -478,6 +480,363 @@ int levelset_create(Sim* s) {
                     s->partial, s->stats);
     } else {
         FS2D_CUDA(cudaMemsetAsync(&s->stats->particle_energy, 0, sizeof(double), s->stream));
+    }
+    return 0;
+}
+
+int levelset_create(Sim* s) {
+    const int NX = s->NX, NY = s->NY;
+    const int P = s->P;
+    // the no-op flag of the current sweep, in the err-adjacent scratch of `max_layer`
+    int* noop = (int*)s->max_layer + 4;
+    int rc = levelset_seed(s);
+    if (rc) return rc;
+
+    // fastSweepIterate: 4 x 4 directions
+    dim3 g2(blocks_for(NX, 128), NY);
+    for (int rep = 0; rep < 4; rep++) {
+        for (int d = 0; d < 4; d++) {
+            FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));  // -1 -> nonzero = no-op
+            FS2D_LAUNCH(s, k_cp_check, g2, 128, 0, s->t, s->pos_df, s->pos, s->cp_tab, s->cp_tab + P, s->cpc, NX, NY,
+                        P, s->dx, s->dr, noop);
+            if ((rc = launch_cp_sweep(s, kDirs[d][0], kDirs[d][1], noop))) return rc;
+        }
+    }
+    FS2D_LAUNCH(s, k_cp_phi, g2, 128, 0, s->t, s->pos, s->np, s->phi, NX, NY, P, s->dx, s->dr);
+
+    // redistance on the pitched copy phi_p
+    FS2D_LAUNCH(s, k_surface, g2, 128, 0, s->phi, s->phi_p, NX, NY, P);
+    for (int rep = 0; rep < 4; rep++) {
+        for (int d = 0; d < 4; d++) {
+            int sx = kDirs[d][0], sy = kDirs[d][1];
+            int i_lo = sx > 0 ? 1 : 0, i_hi = sx > 0 ? NX - 1 : NX - 2;
+            int j_lo = sy > 0 ? 1 : 0, j_hi = sy > 0 ? NY - 1 : NY - 2;
+            FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));
+            FS2D_LAUNCH(s, k_eik_check, g2, 128, 0, s->phi_p, s->emask, NX, NY, P, i_lo, i_hi, j_lo, j_hi, sx, sy,
+                        s->dx, noop);
+            WaveGeom g{sx, sy, i_lo, i_hi, j_lo, j_hi};
+            if ((rc = launch_eik_sweep(s, g, noop))) return rc;
+        }
+    }
+    return levelset_finish(s);
+}
+
+// ---- the level-set sweeps of a batch of scenes ----
+
+namespace {
+
+// One scene of the batched per-cell kernels (128-thread blocks, one row
+// segment each: block blk0 + j * gx + bx covers columns 128 bx .. of row j).
+struct LsCells {
+    int* t;
+    const float4* pos_df;
+    const double2* pos;
+    const float2* xtab;
+    const float2* ytab;
+    const CpConst* kc;
+    double* phi;
+    double* phi_p;
+    uint8_t* emask;
+    size_t np;
+    int NX, NY, P;
+    int blk0, gx;
+    int unused;   // no padding: the host compares tables byte by byte
+    double dx, dr;
+};
+
+static_assert(sizeof(LsCells) == 9 * 8 + 8 + 6 * 4 + 2 * 8, "LsCells has no padding");
+
+__device__ __forceinline__ const LsCells& ls_cell(const LsCells* __restrict__ sc, const int* __restrict__ blk, int& k,
+                                                  int& i, int& j) {
+    k = blk[blockIdx.x];
+    const LsCells& S = sc[k];
+    const int local = blockIdx.x - S.blk0;
+    j = local / S.gx;
+    i = (local % S.gx) * 128 + threadIdx.x;
+    return S;
+}
+
+__global__ void k_cp_check_all(const LsCells* __restrict__ sc, const int* __restrict__ blk, int* noop) {
+    int k, i, j;
+    const LsCells& S = ls_cell(sc, blk, k, i, j);
+    if (i >= S.NX) return;
+    const CpConst kc = *S.kc;
+    if (cp_check_cell(S.t, S.pos_df, S.pos, S.xtab, S.ytab, kc, S.NX, S.NY, S.P, S.dx, S.dr, i, j)) noop[k] = 0;
+}
+
+__global__ void k_cp_phi_all(const LsCells* __restrict__ sc, const int* __restrict__ blk) {
+    int k, i, j;
+    const LsCells& S = ls_cell(sc, blk, k, i, j);
+    if (i >= S.NX) return;
+    cp_phi_cell(S.t, S.pos, S.np, S.phi, S.NX, S.P, S.dx, S.dr, i, j);
+}
+
+__global__ void k_surface_all(const LsCells* __restrict__ sc, const int* __restrict__ blk) {
+    int k, i, j;
+    const LsCells& S = ls_cell(sc, blk, k, i, j);
+    if (i >= S.NX) return;
+    surface_cell(S.phi, S.phi_p, S.NX, S.NY, S.P, i, j);
+}
+
+__global__ void k_eik_check_all(const LsCells* __restrict__ sc, const int* __restrict__ blk, int sx, int sy,
+                                int* noop) {
+    int k, i, j;
+    const LsCells& S = ls_cell(sc, blk, k, i, j);
+    if (i >= S.NX) return;
+    const int i_lo = sx > 0 ? 1 : 0, i_hi = sx > 0 ? S.NX - 1 : S.NX - 2;
+    const int j_lo = sy > 0 ? 1 : 0, j_hi = sy > 0 ? S.NY - 1 : S.NY - 2;
+    if (eik_check_cell(S.phi_p, S.emask, S.P, i_lo, i_hi, j_lo, j_hi, sx, sy, S.dx, i, j)) noop[k] = 0;
+}
+
+template <typename T>
+int ls_alloc(T** p, size_t n) {
+    return check_cuda(cudaMalloc((void**)p, (n ? n : 1) * sizeof(T)), "cudaMalloc");
+}
+
+}  // namespace
+
+struct LsBatch {
+    std::vector<Sim*> sims;
+    std::vector<CpScene> cp;     // host copies of the device tables
+    std::vector<EkScene> ek;
+    std::vector<LsCells> cells;
+    CpScene* d_cp = nullptr;
+    EkScene* d_ek = nullptr;
+    LsCells* d_cells = nullptr;
+    int* d_blk = nullptr;
+    int nblk = 0;
+    WaveItem* d_items = nullptr;
+    int nitems = 0;
+    int* d_noop = nullptr;               // per scene: nonzero = no cell would change in this sweep
+    int* d_work = nullptr;               // persistent-CTA counters of the cp and Eikonal sweeps
+    unsigned long long* progress = nullptr;
+    unsigned long long launch = 0;       // progress base of the next sweep
+    int cp_ctas = 0, ek_ctas = 0;
+};
+
+void ls_batch_free(LsBatch* b) {
+    if (!b) return;
+    void* ptrs[] = {b->d_cp, b->d_ek, b->d_cells, b->d_blk, b->d_items, b->d_noop, b->d_work, b->progress};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete b;
+}
+
+// The tables of every scene from its current buffers (particle arrays may
+// have been replaced since the last frame); uploaded when they changed.
+static int ls_batch_refresh(LsBatch* b, cudaStream_t stream) {
+    const int n = (int)b->sims.size();
+    std::vector<CpScene> cp(n);
+    std::vector<EkScene> ek(n);
+    std::vector<LsCells> cells(n);
+    int blk = 0;
+    for (int k = 0; k < n; k++) {
+        Sim* s = b->sims[k];
+        memset((void*)&cp[k], 0, sizeof(CpScene));
+        memset((void*)&ek[k], 0, sizeof(EkScene));
+        memcpy((void*)&cp[k].maps, s->cpmaps->b, sizeof(CpMaps));
+        memcpy((void*)&ek[k].maps, s->ekmaps->b, sizeof(EkMaps));
+        CpArgs& a = cp[k].a;
+        a.pos_df = s->pos_df;
+        a.pos = s->pos;
+        a.xtab = s->cp_tab;
+        a.ytab = s->cp_tab + s->P;
+        a.kc = s->cpc;
+        a.hb_t = s->cp_hb_t;
+        a.hb_p = s->cp_hb_p;
+        a.np = (int)s->np;
+        a.NX = s->NX;
+        a.NY = s->NY;
+        a.P = s->P;
+        a.dx = s->dx;
+        a.dr = s->dr;
+        EkArgs& e = ek[k].a;
+        e.hb = reinterpret_cast<double2*>(s->cp_hb_p);
+        e.NX = s->NX;
+        e.NY = s->NY;
+        e.P = s->P;
+        e.dx = s->dx;
+        e.c2 = 2 * s->dx * s->dx;
+        LsCells& c = cells[k];
+        c = LsCells{s->t, s->pos_df, s->pos, s->cp_tab, s->cp_tab + s->P, s->cpc, s->phi, s->phi_p, s->emask,
+                    s->np, s->NX, s->NY, s->P, blk, (s->NX + 127) / 128, 0, s->dx, s->dr};
+        blk += c.gx * s->NY;
+    }
+    if (memcmp((const void*)cp.data(), (const void*)b->cp.data(), n * sizeof(CpScene)) != 0 ||
+        memcmp((const void*)ek.data(), (const void*)b->ek.data(), n * sizeof(EkScene)) != 0 ||
+        memcmp((const void*)cells.data(), (const void*)b->cells.data(), n * sizeof(LsCells)) != 0) {
+        FS2D_CUDA(cudaMemcpyAsync(b->d_cp, cp.data(), n * sizeof(CpScene), cudaMemcpyHostToDevice, stream));
+        FS2D_CUDA(cudaMemcpyAsync(b->d_ek, ek.data(), n * sizeof(EkScene), cudaMemcpyHostToDevice, stream));
+        FS2D_CUDA(cudaMemcpyAsync(b->d_cells, cells.data(), n * sizeof(LsCells), cudaMemcpyHostToDevice, stream));
+        FS2D_CUDA(cudaStreamSynchronize(stream));   // the host vectors are replaced below
+        b->cp.swap(cp);
+        b->ek.swap(ek);
+        b->cells.swap(cells);
+    }
+    return 0;
+}
+
+LsBatch* ls_batch_create(Sim* const* sims, int n, int device, int* rc_out) {
+    int rc = 0;
+    LsBatch* b = new (std::nothrow) LsBatch();
+    if (!b) {
+        set_error("out of host memory");
+        *rc_out = FS2D_ERR_ALLOC;
+        return nullptr;
+    }
+    b->sims.assign(sims, sims + n);
+    b->cp.resize(n);
+    b->ek.resize(n);
+    b->cells.resize(n);
+    for (int k = 0; k < n; k++) {   // nothing matches: the first refresh uploads
+        memset((void*)&b->cp[k], 0xff, sizeof(CpScene));
+        memset((void*)&b->ek[k], 0xff, sizeof(EkScene));
+        memset((void*)&b->cells[k], 0xff, sizeof(LsCells));
+    }
+    // block map of the per-cell kernels and the work list: strip-major (every
+    // scene's first strip, scenes by decreasing rows, then every second
+    // strip, ...), progress counters numbered scene by scene
+    std::vector<int> blk, first(n), order(n);
+    int pidx = 0;
+    for (int k = 0; k < n; k++) {
+        const Sim* s = sims[k];
+        blk.insert(blk.end(), (size_t)((s->NX + 127) / 128) * s->NY, k);
+        first[k] = pidx;
+        pidx += (s->NY + 31) / 32;
+        order[k] = k;
+    }
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sims[x]->NY > sims[y]->NY; });
+    std::vector<WaveItem> items;
+    for (int st = 0;; st++) {
+        bool any = false;
+        for (int k : order) {
+            if (st < (sims[k]->NY + 31) / 32) {
+                items.push_back(WaveItem{k, st, first[k] + st});
+                any = true;
+            }
+        }
+        if (!any) break;
+    }
+    b->nblk = (int)blk.size();
+    b->nitems = (int)items.size();
+    if (!rc) rc = ls_alloc(&b->d_cp, n);
+    if (!rc) rc = ls_alloc(&b->d_ek, n);
+    if (!rc) rc = ls_alloc(&b->d_cells, n);
+    if (!rc) rc = ls_alloc(&b->d_blk, blk.size());
+    if (!rc) rc = ls_alloc(&b->d_items, items.size());
+    if (!rc) rc = ls_alloc(&b->d_noop, n);
+    if (!rc) rc = ls_alloc(&b->d_work, 4);
+    if (!rc) rc = ls_alloc(&b->progress, items.size());
+    if (!rc && ((uintptr_t)b->d_cp % alignof(CpScene) != 0 || (uintptr_t)b->d_ek % alignof(EkScene) != 0)) {
+        set_error("level-set batch: the tensor map tables are not aligned");
+        rc = FS2D_ERR_CUDA;
+    }
+    if (!rc) rc = check_cuda(cudaMemset(b->d_work, 0, 4 * sizeof(int)), "cudaMemset");
+    if (!rc) rc = check_cuda(cudaMemset(b->progress, 0, items.size() * sizeof(unsigned long long)), "cudaMemset");
+    if (!rc) rc = check_cuda(cudaMemcpy(b->d_blk, blk.data(), blk.size() * sizeof(int), cudaMemcpyHostToDevice),
+                             "cudaMemcpy");
+    if (!rc)
+        rc = check_cuda(cudaMemcpy(b->d_items, items.data(), items.size() * sizeof(WaveItem), cudaMemcpyHostToDevice),
+                        "cudaMemcpy");
+    // persistent CTAs: as many as the SMs hold at once, at most one per item
+    int sms = 1, per_cp = 0, per_ek = 0;
+    if (!rc) {
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+        const void* cps[] = {(const void*)cp_sweep_kernel<1, 1, true>, (const void*)cp_sweep_kernel<-1, 1, true>,
+                             (const void*)cp_sweep_kernel<1, -1, true>, (const void*)cp_sweep_kernel<-1, -1, true>};
+        const void* eks[] = {(const void*)eik_sweep_kernel<1, 1, true>, (const void*)eik_sweep_kernel<-1, 1, true>,
+                             (const void*)eik_sweep_kernel<1, -1, true>, (const void*)eik_sweep_kernel<-1, -1, true>};
+        static std::atomic<unsigned long long> cfg_cp[4] = {{0}, {0}, {0}, {0}}, cfg_ek[4] = {{0}, {0}, {0}, {0}};
+        for (int k = 0; k < 4 && !rc; k++) rc = ensure_smem_attr(cfg_cp[k], device, cps[k], (int)kCpSmem);
+        for (int k = 0; k < 4 && !rc; k++) rc = ensure_smem_attr(cfg_ek[k], device, eks[k], (int)kEkSmem);
+        // every direction's instance must fit the CTA count (a cooperative launch is refused otherwise)
+        per_cp = per_ek = 1 << 30;
+        for (int k = 0; k < 4 && !rc; k++) {
+            int a = 0, e = 0;
+            rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, cps[k], 64, kCpSmem),
+                            "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+            if (!rc)
+                rc = check_cuda(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&e, eks[k], 64, kEkSmem),
+                                "cudaOccupancyMaxActiveBlocksPerMultiprocessor");
+            per_cp = std::min(per_cp, a);
+            per_ek = std::min(per_ek, e);
+        }
+    }
+    if (!rc && (per_cp < 1 || per_ek < 1)) {
+        set_error("level-set batch: the sweep kernels do not fit on an SM");
+        rc = FS2D_ERR_CUDA;
+    }
+    if (rc) {
+        ls_batch_free(b);
+        *rc_out = rc;
+        return nullptr;
+    }
+    b->cp_ctas = std::max(1, std::min(per_cp * sms, b->nitems));
+    b->ek_ctas = std::max(1, std::min(per_ek * sms, b->nitems));
+    *rc_out = 0;
+    return b;
+}
+
+template <int SX, int SY>
+static int ls_launch_cp(LsBatch* b, cudaStream_t stream, int* err) {
+    WaveWork w{b->d_cp, b->d_items, b->nitems, b->d_work, b->progress, (++b->launch) << 24, err, b->d_noop};
+    CpMaps m{};
+    CpArgs a{};
+    void* args[] = {(void*)&m, (void*)&a, (void*)&w};
+    return check_cuda(
+        launch_clustered((const void*)cp_sweep_kernel<SX, SY, true>, b->cp_ctas, 1, 64, kCpSmem, stream, args),
+        "cp_sweep (batch)");
+}
+
+template <int SX, int SY>
+static int ls_launch_ek(LsBatch* b, cudaStream_t stream, int* err) {
+    WaveWork w{b->d_ek, b->d_items, b->nitems, b->d_work + 2, b->progress, (++b->launch) << 24, err, b->d_noop};
+    EkMaps m{};
+    EkArgs a{};
+    void* args[] = {(void*)&m, (void*)&a, (void*)&w};
+    return check_cuda(
+        launch_clustered((const void*)eik_sweep_kernel<SX, SY, true>, b->ek_ctas, 1, 64, kEkSmem, stream, args),
+        "eik_sweep (batch)");
+}
+
+// Between levelset_seed and levelset_finish of every scene: the 16
+// closest-point sweeps, phi and the surface, the 16 Eikonal sweeps, each
+// step one launch for all scenes on `stream`.  Every scene computes what
+// levelset_create computes for it alone (the same cells, strips and order).
+int ls_batch_sweeps(LsBatch* b, cudaStream_t stream, int* err, unsigned long long* launches) {
+    int rc = ls_batch_refresh(b, stream);
+    if (rc) return rc;
+    const int n = (int)b->sims.size();
+    const unsigned nblk = (unsigned)b->nblk;
+    auto count = [&](int k) { if (launches) *launches += (unsigned long long)k; };
+    for (int rep = 0; rep < 4; rep++) {
+        for (int d = 0; d < 4; d++) {
+            FS2D_CUDA(cudaMemsetAsync(b->d_noop, 0xff, n * sizeof(int), stream));
+            k_cp_check_all<<<nblk, 128, 0, stream>>>(b->d_cells, b->d_blk, b->d_noop);
+            if ((rc = check_cuda(cudaGetLastError(), "k_cp_check_all"))) return rc;
+            const int sx = kDirs[d][0], sy = kDirs[d][1];
+            rc = sx > 0 ? (sy > 0 ? ls_launch_cp<1, 1>(b, stream, err) : ls_launch_cp<1, -1>(b, stream, err))
+                        : (sy > 0 ? ls_launch_cp<-1, 1>(b, stream, err) : ls_launch_cp<-1, -1>(b, stream, err));
+            if (rc) return rc;
+            count(2);
+        }
+    }
+    k_cp_phi_all<<<nblk, 128, 0, stream>>>(b->d_cells, b->d_blk);
+    if ((rc = check_cuda(cudaGetLastError(), "k_cp_phi_all"))) return rc;
+    k_surface_all<<<nblk, 128, 0, stream>>>(b->d_cells, b->d_blk);
+    if ((rc = check_cuda(cudaGetLastError(), "k_surface_all"))) return rc;
+    count(2);
+    for (int rep = 0; rep < 4; rep++) {
+        for (int d = 0; d < 4; d++) {
+            const int sx = kDirs[d][0], sy = kDirs[d][1];
+            FS2D_CUDA(cudaMemsetAsync(b->d_noop, 0xff, n * sizeof(int), stream));
+            k_eik_check_all<<<nblk, 128, 0, stream>>>(b->d_cells, b->d_blk, sx, sy, b->d_noop);
+            if ((rc = check_cuda(cudaGetLastError(), "k_eik_check_all"))) return rc;
+            rc = sx > 0 ? (sy > 0 ? ls_launch_ek<1, 1>(b, stream, err) : ls_launch_ek<1, -1>(b, stream, err))
+                        : (sy > 0 ? ls_launch_ek<-1, 1>(b, stream, err) : ls_launch_ek<-1, -1>(b, stream, err));
+            if (rc) return rc;
+            count(2);
+        }
     }
     return 0;
 }

@@ -484,9 +484,10 @@ class Batch:
         _check(load().fs2d_batch_set_schedule(self.h, int(schedule), int(ctas)))
 
     def phase_ms(self):
-        """Wall-clock ms of the last step() of a mixed-precision batch: the
-        scenes' stages before the solve, the joint solve, the stages after it."""
-        ms = (C.c_double * 3)()
+        """ms of the last step() of a mixed-precision batch: wall clock of the
+        scenes' stages before the solve, the joint solve, the stages after it,
+        and the device time of the batched level-set sweeps (within the first)."""
+        ms = (C.c_double * 4)()
         _check(load().fs2d_batch_phase_ms(self.h, ms))
         return list(ms)
 

@@ -266,10 +266,12 @@ int fs2d_batch_sweep_schedule(fs2d_batch* batch, int* schedule, int* ctas, int* 
  * persistent CTAs (at most the SM count).  A scene's results do not depend on
  * either. */
 int fs2d_batch_set_schedule(fs2d_batch* batch, int schedule, int ctas);
-/* Host wall-clock milliseconds of the frames of the last fs2d_batch_step of a
- * mixed-precision batch, summed over its frames: ms[0] the scenes' stages up
- * to their pressure solves, ms[1] the batch's joint pressure solve, ms[2] the
- * remaining stages (zeros for an FP64 batch). */
+/* Milliseconds of the frames of the last fs2d_batch_step of a
+ * mixed-precision batch, summed over its frames (zeros for an FP64 batch),
+ * four values: host wall clock of ms[0] the scenes' stages up to their
+ * pressure solves, ms[1] the batch's joint pressure solve, ms[2] the
+ * remaining stages; ms[3] the device time of the level-set sweeps of all
+ * scenes (part of ms[0]). */
 int fs2d_batch_phase_ms(fs2d_batch* batch, double* ms);
 /* fs2d_forward / fs2d_backward for every scene of a batch (each a closed box:
  * no EMPTY cell, semi-Lagrangian mode), scenes issued concurrently by the
