@@ -51,6 +51,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(ROOT, "fluid-sim_gb300"))
+# Hardware work queues of this process's CUDA context (read when the context is
+# created): a batch drives one stream per scene, and with the default 8 queues
+# streams beyond the eighth share queues and wait behind one another.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = "grid-cell steps/s at 1024^2 (PIC/FLIP step, MIC(0)-PCG to 1e-6 rel res)"
 UNIT = "grid-cell steps/s"
@@ -662,6 +666,7 @@ def main():
                  "concurrency_speedup_rank0": seq_s / (conc_s / args.batch_steps),
                  "gpu_launches_per_batch_step": (l1 - l0) // max(args.batch_steps, 1),
                  "roofline": batch_roofline,
+                 "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
                  "phase_ms_per_batch_step": {"stages_before_solve": round(phases[0] / args.batch_steps, 2),
                                              "joint_pressure_solve": round(phases[1] / args.batch_steps, 2),
                                              "stages_after_solve": round(phases[2] / args.batch_steps, 2),

@@ -419,7 +419,17 @@ int finish(Host* h) {
     if (e) {
         FS2D_CUDA(cudaMemsetAsync(s->err, 0, sizeof(int), s->stream));
         if (e & 1) {
-            set_error("a wavefront sweep timed out waiting for its neighbour strip");
+            const char* kind = (e & (kWaveKindCp << 4))      ? "closest-point"
+                               : (e & (kWaveKindEik << 4))   ? "Eikonal"
+                               : (e & (kWaveKindWave2 << 4)) ? "MIC(0) factor or FP64 MIC(0)"
+                               : (e & (kWaveKindMic32 << 4)) ? "FP32 MIC(0)"
+                                                             : "wavefront";
+            const char* what = (e & 256) ? "its neighbour strip" : (e & 512) ? "its own tile loads" : (e & 1024) ? "its other warp" : "a neighbour";
+            set_error("a %s sweep timed out waiting for %s", kind, what);
+            return FS2D_ERR_TIMEOUT;
+        }
+        if (e & 8) {
+            set_error("the extrapolation timed out waiting between bands");
             return FS2D_ERR_TIMEOUT;
         }
         set_error("non-finite or out-of-domain particle position");

@@ -51,7 +51,7 @@ constexpr int kCpCols = 32;
 constexpr int kCpBoxRows = 33;
 constexpr int kCpSlots = 8;
 constexpr int kCpAhead = 4;        // tiles requested ahead
-constexpr int kCpD = 8;            // gather distance (columns)
+constexpr int kCpD = 8;            // gather distance (columns; 16 measured no faster at 1024^2)
 constexpr int kCpR = 16;           // gather ring slots per row (power of two > kCpD + 1)
 // Chunk of the row below (columns per arrival check): smaller chunks shorten
 // the strip-to-strip lag (measured at 1024^2: 16 and 8 columns gave 9.8 and
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
                 idle = 0;
             } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(a.err))) {
                 if (lane == 0) {
-                    atomicOr(a.err, 1);
+                    atomicOr(a.err, kWaitStrip | (kWaveKindCp << 4));
                     *quit = 1;
                 }
                 break;
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
         while (!mbar_try_wait(bar, parity)) {
             if (++polls > kWaveSpinLimit) {
                 failed = true;
-                atomicOr(a.err, 1);
+                atomicOr(a.err, kWaitTile | (kWaveKindCp << 4));
                 *quit = 1;   // a copy may still be in flight: this CTA takes no further strip
                 break;
             }
@@ -438,7 +438,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
         while (*flag < need) {
             if (++polls > 16 * spin) {
                 failed = true;
-                atomicOr(a.err, 1);
+                atomicOr(a.err, kWaitWarp | (kWaveKindCp << 4));
                 *quit = 1;
                 return;
             }

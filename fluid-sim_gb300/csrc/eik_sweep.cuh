@@ -294,7 +294,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                 idle = 0;
             } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(a.err))) {
                 if (lane == 0) {
-                    atomicOr(a.err, 1);
+                    atomicOr(a.err, kWaitStrip | (kWaveKindEik << 4));
                     *quit = 1;
                 }
                 break;
@@ -326,7 +326,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
             while (!mbar_try_wait(bar, parity)) {
                 if (++polls > kWaveSpinLimit) {
                     failed = true;
-                    atomicOr(a.err, 1);
+                    atomicOr(a.err, kWaitTile | (kWaveKindEik << 4));
                     *quit = 1;   // a copy may still be in flight: this CTA takes no further strip
                     break;
                 }
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
             while (*flag < need) {
                 if (++polls > 16 * spin) {
                     failed = true;
-                    atomicOr(a.err, 1);
+                    atomicOr(a.err, kWaitWarp | (kWaveKindEik << 4));
                     *quit = 1;
                     return;
                 }
@@ -373,7 +373,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                             ok = (lane >> 4) ? ek_w1_is(w, cc) : ek_w0_is(w, cc);
                             if (!ok && (++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(a.err)))) {
                                 failed = true;
-                                atomicOr(a.err, 1);
+                                atomicOr(a.err, kWaitStrip | (kWaveKindEik << 4));
                                 *quit = 1;
                             }
                         }

@@ -27,8 +27,11 @@ constexpr uint32_t kUnknown = 0xFFFFFFFFu;   // extrapolation mask of an unknown
 
 // The device error word and the controls of the wavefront waits share one
 // allocation of kErrWords ints (Sim::err):
-//   err[0]      error bits: 1 a wait gave up (timeout), 2 a non-finite
-//               particle position, 4 a particle outside the grid;
+//   err[0]      error bits: 1 a wait between strips gave up (timeout), 2 a
+//               non-finite particle position, 4 a particle outside the grid,
+//               8 a wait between extrapolation bands gave up (timeout);
+//               with bit 0, the sweep kind (kWaveKind* << 4) and the wait
+//               (256 previous strip, 512 own tile loads, 1024 other warp);
 //   err[1]      kinds of sweep (kWaveKind*) in which strip err[2] withholds
 //               its hand-off to the next strip (0: none).  A test hook
 //               (fs2d_debug_wavefront): the next strip's wait then runs out
@@ -40,6 +43,11 @@ constexpr uint32_t kUnknown = 0xFFFFFFFFu;   // extrapolation mask of an unknown
 constexpr int kErrWords = 8;
 constexpr long long kWaveSpinLimit = 1ll << 22;   // polls before a wait gives up (~0.5 s), by default
 constexpr int kWaveKindCp = 1, kWaveKindEik = 2, kWaveKindWave2 = 4, kWaveKindMic32 = 8;
+// A wait that gave up sets bit 0 of err[0] together with what it waited for
+// (which sweep: kWaveKind* << 4; which wait: kWait*), for the message.
+constexpr int kWaitStrip = 1 | 256;    // the previous strip's hand-off
+constexpr int kWaitTile = 1 | 512;     // the strip's own TMA tile loads
+constexpr int kWaitWarp = 1 | 1024;    // the other warp of the strip's CTA
 
 // Scalars of one pressure solve, kept in device memory so that the PCG loop
 // runs without host round trips.  Finalised by the last block of each

@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 if (moved) {
                     idle = 0;
                 } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(err))) {
-                    if (lane == 0) atomicOr(err, 1);
+                    if (lane == 0) atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
                     break;
                 }
             }
@@ -296,7 +296,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 if (t >= issued) return;
                 if (!poll_tile(t)) {
                     failed = true;
-                    atomicOr(err, 1);
+                    atomicOr(err, kWaitTile | (kWaveKindMic32 << 4));
                     unconfirmed = min(unconfirmed, t);
                 }
             };
@@ -306,7 +306,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 while (*flag < need) {
                     if (++polls > 16 * spin) {
                         failed = true;
-                        atomicOr(err, 1);
+                        atomicOr(err, kWaitWarp | (kWaveKindMic32 << 4));
                         *quit = 1;
                         return;
                     }
@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                                     ok = m32_entry_is(bnd[rr % kM32BndRing], rr);
                                     if (!ok && (++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(err)))) {
                                         failed = true;
-                                        atomicOr(err, 1);
+                                        atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
                                         *quit = 1;
                                     }
                                 }

@@ -26,6 +26,7 @@
 // cells), so one launch per band replaces one launch per layer.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <atomic>
 #include <mutex>
 #include "fs2d_device.cuh"
 
@@ -433,6 +434,30 @@ __global__ void k_tile_max(const int2* __restrict__ tr, size_t n, unsigned int* 
     if (k < n && tr[k].y >= 0) atomicMax(max_layer, (unsigned int)tr[k].y);
 }
 
+// One extrapolation of up to two face grids: every band of kBand layers of
+// every 32x32 tile in one launch.  The deepest layer of each grid
+// (max_layer, written by k_tile_max) is read on the device, so the host
+// neither waits for it nor launches per band.  Work items are (band, tile)
+// pairs in band-major order, taken by the CTAs from an atomic counter; a
+// tile's band needs the previous band of the tile and of its eight
+// neighbours (the halo), whose items come earlier in the list and were taken
+// earlier by running CTAs, so every wait makes progress whatever the grid
+// size and whatever else runs on the GPU.
+struct ExtrapJob {
+    double* a[2];
+    const uint32_t* layer[2];
+    int W[2], H[2];
+    const int2* tile_range[2];
+    int tiles_x[2], tiles_y[2];
+    int ntiles[2];              // tiles of grid 0, of grid 1 (0: no grid 1)
+    const unsigned int* max_layer;
+    unsigned int* work;         // item counter (zero before the launch)
+    int* done;                  // per tile: bands finished (zero before the launch)
+    int* err;                   // bit 3 (8): a wait for a neighbour tile gave up
+    unsigned int band_limit;    // deepest layer to fill
+    long long spin;             // polls before a wait gives up
+};
+
 // Layers [lo, hi] of one 32x32 tile, recomputed in shared memory inside a
 // halo of kBand cells.  Only region cells that can still reach the tile
 // within the band are recomputed: a cell of layer l at L1 distance d from the
@@ -443,80 +468,137 @@ __global__ void k_tile_max(const int2* __restrict__ tr, size_t n, unsigned int* 
 // (d <= kBand - 1).  Kept cells are bucketed by layer, so each layer step
 // visits only its own front.  Layers are held relative to the band in one
 // byte: 0 below lo, 1 + (l - lo) inside, kBand + 1 above hi or unreachable.
+// Face values are read through L2 (other CTAs wrote them in earlier bands).
 //
 // The mean divides by the neighbour count as the reference does; for counts
 // 1, 2 and 4 the quotient equals the product with the exact reciprocal (both
 // are the correctly rounded value of the same real number), so only a count
 // of 3 needs a division.
-__global__ void __launch_bounds__(256) k_extrap_band(double* a, const uint32_t* __restrict__ layer, int W, int H,
-                                                     const int2* __restrict__ tile_range, int tiles_x, int lo, int hi) {
+__global__ void __launch_bounds__(256) k_extrap_bands(const ExtrapJob job) {
     __shared__ double val[kReg * kReg];
     __shared__ unsigned char rel[kReg * kReg];
     __shared__ unsigned short list[kReg * kReg];
     __shared__ int cnt[kBand + 1], cur[kBand];
-    int tx = blockIdx.x, ty = blockIdx.y;
-    int2 tr = tile_range[(size_t)ty * tiles_x + tx];
-    if (tr.y < lo || tr.x > hi) return;
-    const int ox = tx * kTile - kBand, oy = ty * kTile - kBand;
-    if (threadIdx.x <= kBand) cnt[threadIdx.x] = 0;
-    if (threadIdx.x < kBand) cur[threadIdx.x] = 0;
-    __syncthreads();
+    __shared__ unsigned int item_sh;
+    __shared__ int failed_sh;
+    const int ng = job.ntiles[1] > 0 ? 2 : 1;
+    unsigned int depth[2] = {0u, 0u};
+    unsigned int deepest = 0u;
+    for (int g = 0; g < ng; g++) {
+        depth[g] = min(job.max_layer[g], job.band_limit);
+        deepest = max(deepest, depth[g]);
+    }
+    const unsigned int total = (unsigned int)(job.ntiles[0] + job.ntiles[1]);
+    const unsigned int nbands = (deepest + kBand - 1) / kBand;
+    const unsigned long long nitems = (unsigned long long)nbands * total;
     // L1 distance from region cell (rx, ry) to the output tile
     auto tile_dist = [](int rx, int ry) {
         int dx = rx < kBand ? kBand - rx : (rx >= kBand + kTile ? rx - (kBand + kTile - 1) : 0);
         int dy = ry < kBand ? kBand - ry : (ry >= kBand + kTile ? ry - (kBand + kTile - 1) : 0);
         return dx + dy;
     };
-    for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
-        int rx = k % kReg, ry = k / kReg;
-        int gx = ox + rx, gy = oy + ry;
-        uint32_t l = kUnknown;
-        double v = 0.0;
-        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
-            size_t c = (size_t)gy * W + gx;
-            l = layer[c];
-            v = a[c];
-        }
-        const int r = l < (uint32_t)lo ? 0 : (l <= (uint32_t)hi ? 1 + (int)(l - lo) : kBand + 1);
-        rel[k] = (unsigned char)r;
-        val[k] = v;
-        if (r >= 1 && r <= kBand && tile_dist(rx, ry) <= hi - lo + 1 - r) atomicAdd(&cnt[r], 1);
-    }
-    __syncthreads();
-    if (threadIdx.x == 0)
-        for (int b = 1; b <= kBand; b++) cnt[b] += cnt[b - 1];   // cnt[b] = first slot of layer lo + b
-    __syncthreads();
-    for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
-        const int r = rel[k];
-        if (r >= 1 && r <= kBand && tile_dist(k % kReg, k / kReg) <= hi - lo + 1 - r)
-            list[cnt[r - 1] + atomicAdd(&cur[r - 1], 1)] = (unsigned short)k;
-    }
-    for (int L = lo; L <= hi; L++) {
+    if (threadIdx.x == 0) failed_sh = 0;
+    for (;;) {
+        __syncthreads();   // the previous item's shared arrays are no longer read
+        if (threadIdx.x == 0) item_sh = atomicAdd(job.work, 1u);
         __syncthreads();
-        const int b = L - lo;
-        const int rl = b + 1;   // relative layer of L
-        for (int i = cnt[b] + threadIdx.x; i < cnt[b + 1]; i += blockDim.x) {
-            const int k = list[i];
-            double sum = 0.0;
-            int count = 0;
-            // neighbours in the reference's order: x-1, x+1, y-1, y+1
-            if (rel[k - 1] < rl) { sum += val[k - 1]; count++; }
-            if (rel[k + 1] < rl) { sum += val[k + 1]; count++; }
-            if (rel[k - kReg] < rl) { sum += val[k - kReg]; count++; }
-            if (rel[k + kReg] < rl) { sum += val[k + kReg]; count++; }
-            double r;
-            if (count == 3) r = sum / 3.0;
-            else r = sum * (count == 1 ? 1.0 : (count == 2 ? 0.5 : (count == 4 ? 0.25 : 0.0)));
-            val[k] = r;
+        const unsigned long long item = item_sh;
+        if (item >= nitems || failed_sh) break;
+        const int band = (int)(item / total);
+        const int tile = (int)(item % total);
+        const int g = tile < job.ntiles[0] ? 0 : 1;
+        const int t = tile - (g ? job.ntiles[0] : 0);
+        const int tx = t % job.tiles_x[g], ty = t / job.tiles_x[g];
+        const unsigned int lo_u = 1u + (unsigned int)band * kBand;
+        const unsigned int hi_u = min(lo_u + kBand - 1, depth[g]);
+        const int2 tr = job.tile_range[g][t];
+        const bool work = lo_u <= depth[g] && tr.y >= (int)lo_u && tr.x <= (int)hi_u;
+        // wait: the tile's own previous band, and with work also the
+        // neighbours' (thread k < 9 watches tile (tx + k % 3 - 1, ty + k / 3 - 1))
+        if (band > 0 && threadIdx.x < 9) {
+            const int nx = tx + (int)(threadIdx.x % 3) - 1, ny = ty + (int)(threadIdx.x / 3) - 1;
+            const bool watch = (threadIdx.x == 4 || work) && nx >= 0 && ny >= 0 && nx < job.tiles_x[g] &&
+                               ny < job.tiles_y[g];
+            if (watch) {
+                const int* d = job.done + (g ? job.ntiles[0] : 0) + ny * job.tiles_x[g] + nx;
+                long long polls = 0;
+                while (ld_acquire_int(d) < band) {
+                    if (++polls > job.spin) {
+                        atomicOr(job.err, 8);
+                        failed_sh = 1;
+                        break;
+                    }
+                }
+            }
         }
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < kTile * kTile; k += blockDim.x) {
-        int rx = kBand + k % kTile, ry = kBand + k / kTile;
-        int gx = ox + rx, gy = oy + ry;
-        if (gx >= W || gy >= H) continue;
-        const int r = rel[ry * kReg + rx];
-        if (r >= 1 && r <= kBand) a[(size_t)gy * W + gx] = val[ry * kReg + rx];
+        __syncthreads();
+        if (failed_sh) break;   // results are invalid; this CTA takes no further item
+        if (work) {
+            const int lo = (int)lo_u, hi = (int)hi_u;
+            const int W = job.W[g], H = job.H[g];
+            double* a = job.a[g];
+            const uint32_t* __restrict__ layer = job.layer[g];
+            const int ox = tx * kTile - kBand, oy = ty * kTile - kBand;
+            if (threadIdx.x <= kBand) cnt[threadIdx.x] = 0;
+            if (threadIdx.x < kBand) cur[threadIdx.x] = 0;
+            __syncthreads();
+            for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
+                int rx = k % kReg, ry = k / kReg;
+                int gx = ox + rx, gy = oy + ry;
+                uint32_t l = kUnknown;
+                double v = 0.0;
+                if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+                    size_t c = (size_t)gy * W + gx;
+                    l = layer[c];
+                    v = __ldcg(a + c);
+                }
+                const int r = l < (uint32_t)lo ? 0 : (l <= (uint32_t)hi ? 1 + (int)(l - lo) : kBand + 1);
+                rel[k] = (unsigned char)r;
+                val[k] = v;
+                if (r >= 1 && r <= kBand && tile_dist(rx, ry) <= hi - lo + 1 - r) atomicAdd(&cnt[r], 1);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0)
+                for (int b = 1; b <= kBand; b++) cnt[b] += cnt[b - 1];   // cnt[b] = first slot of layer lo + b
+            __syncthreads();
+            for (int k = threadIdx.x; k < kReg * kReg; k += blockDim.x) {
+                const int r = rel[k];
+                if (r >= 1 && r <= kBand && tile_dist(k % kReg, k / kReg) <= hi - lo + 1 - r)
+                    list[cnt[r - 1] + atomicAdd(&cur[r - 1], 1)] = (unsigned short)k;
+            }
+            for (int L = lo; L <= hi; L++) {
+                __syncthreads();
+                const int b = L - lo;
+                const int rl = b + 1;   // relative layer of L
+                for (int i = cnt[b] + threadIdx.x; i < cnt[b + 1]; i += blockDim.x) {
+                    const int k = list[i];
+                    double sum = 0.0;
+                    int count = 0;
+                    // neighbours in the reference's order: x-1, x+1, y-1, y+1
+                    if (rel[k - 1] < rl) { sum += val[k - 1]; count++; }
+                    if (rel[k + 1] < rl) { sum += val[k + 1]; count++; }
+                    if (rel[k - kReg] < rl) { sum += val[k - kReg]; count++; }
+                    if (rel[k + kReg] < rl) { sum += val[k + kReg]; count++; }
+                    double r;
+                    if (count == 3) r = sum / 3.0;
+                    else r = sum * (count == 1 ? 1.0 : (count == 2 ? 0.5 : (count == 4 ? 0.25 : 0.0)));
+                    val[k] = r;
+                }
+            }
+            __syncthreads();
+            for (int k = threadIdx.x; k < kTile * kTile; k += blockDim.x) {
+                int rx = kBand + k % kTile, ry = kBand + k / kTile;
+                int gx = ox + rx, gy = oy + ry;
+                if (gx >= W || gy >= H) continue;
+                const int r = rel[ry * kReg + rx];
+                if (r >= 1 && r <= kBand) a[(size_t)gy * W + gx] = val[ry * kReg + rx];
+            }
+        }
+        __syncthreads();   // every store of this item is issued
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release_int(job.done + tile, band + 1);
+        }
     }
 }
 
@@ -642,14 +724,15 @@ size_t extrap_tiles(int W, int H) { return (size_t)((W + kTile - 1) / kTile) * (
 
 // Array2D::extrapolate on one or two face grids (grid 1 may be absent,
 // a[1] == nullptr).  Scratch: dist[g] holds W*H ints per grid, tile_range
-// extrap_tiles(W,H) entries per grid (grid 1's after grid 0's), max_layer 2
-// counters.  Synchronises `stream` once (to read the deepest layer).
+// extrap_tiles(W,H) entries per grid (grid 1's after grid 0's), max_layer 16
+// words (0-1 the deepest layers, 8 the band kernel's item counter, 12 the
+// error word when there is no handle).  Queues work on `stream` only: the
+// depth is read on the device by the band kernel, one launch.
 int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double* const a[2], uint32_t* const m[2],
                      const int W[2], const int H[2], int band) {
     int ng = a[1] ? 2 : 1;
-    int band_limit = band > 0 ? band : (1 << 28);
-    FS2D_CUDA(cudaMemsetAsync(x.max_layer, 0, 2 * sizeof(unsigned int), stream));
-    int tiles_x[2], tiles_y[2];
+    FS2D_CUDA(cudaMemsetAsync(x.max_layer, 0, 16 * sizeof(unsigned int), stream));
+    int tiles_x[2] = {0, 0}, tiles_y[2] = {0, 0};
     size_t tile_off[2] = {0, 0};
     for (int gi = 0; gi < ng; gi++) {
         tiles_x[gi] = (W[gi] + kTile - 1) / kTile;
@@ -662,18 +745,45 @@ int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double
         XLAUNCH(k_dt_rows, H[gi], 1024, x.dist[gi], m[gi], W[gi], H[gi], tr, tiles_x[gi]);
         XLAUNCH(k_tile_max, blocks_for(nt, 256), 256, tr, nt, x.max_layer + gi);
     }
-    unsigned int hmax[2] = {0, 0};
-    FS2D_CUDA(cudaMemcpyAsync(hmax, x.max_layer, 2 * sizeof(unsigned int), cudaMemcpyDeviceToHost, stream));
-    if (int rcw = wait_stream(s, stream)) return rcw;
+    ExtrapJob job{};
     for (int gi = 0; gi < ng; gi++) {
-        int maxL = (int)std::min<unsigned int>(hmax[gi], (unsigned int)band_limit);
-        for (int lo = 1; lo <= maxL; lo += kBand) {
-            int hi = std::min(lo + kBand - 1, maxL);
-            dim3 grid(tiles_x[gi], tiles_y[gi]);
-            XLAUNCH(k_extrap_band, grid, 256, a[gi], m[gi], W[gi], H[gi], x.tile_range + tile_off[gi], tiles_x[gi],
-                    lo, hi);
-        }
+        job.a[gi] = a[gi];
+        job.layer[gi] = m[gi];
+        job.W[gi] = W[gi];
+        job.H[gi] = H[gi];
+        job.tile_range[gi] = x.tile_range + tile_off[gi];
+        job.tiles_x[gi] = tiles_x[gi];
+        job.tiles_y[gi] = tiles_y[gi];
+        job.ntiles[gi] = tiles_x[gi] * tiles_y[gi];
     }
+    const int total = job.ntiles[0] + job.ntiles[1];
+    // the per-tile band counters live in grid 0's distance map, which the
+    // layers no longer need (every tile count is below W * H)
+    if ((size_t)total > (size_t)W[0] * H[0]) {
+        set_error("extrapolation: %d tiles do not fit the scratch", total);
+        return FS2D_ERR_INVALID;
+    }
+    job.max_layer = x.max_layer;
+    job.work = x.max_layer + 8;
+    job.done = x.dist[0];
+    job.err = s ? s->err : reinterpret_cast<int*>(x.max_layer + 12);
+    job.band_limit = band > 0 ? (unsigned int)band : (1u << 28);
+    job.spin = kWaveSpinLimit;
+    FS2D_CUDA(cudaMemsetAsync(job.done, 0, (size_t)total * sizeof(int), stream));
+    // CTAs: as many as the SMs hold at once, at most one per tile (items
+    // beyond what runs at once are taken by whichever CTA is free)
+    int dev = 0;
+    FS2D_CUDA(cudaGetDevice(&dev));
+    static std::atomic<int> per_dev[64];
+    int occ = (dev >= 0 && dev < 64) ? per_dev[dev].load() : 0;
+    if (occ <= 0) {
+        int sms = 1, per = 0;
+        FS2D_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        FS2D_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_extrap_bands, 256, 0));
+        occ = std::max(1, per * sms);
+        if (dev >= 0 && dev < 64) per_dev[dev].store(occ);
+    }
+    XLAUNCH(k_extrap_bands, std::max(1, std::min(occ, total)), 256, job);
     return 0;
 }
 #undef XLAUNCH
@@ -769,6 +879,16 @@ int g2p(Sim* s) {
 
 using namespace fs2d;
 
+// Status of a handle-less extrapolation from its error word (bit 3: a wait
+// between the bands gave up).
+static int extrap_wait_status(int werr) {
+    if (werr & 8) {
+        set_error("extrapolation: a wait between bands timed out");
+        return FS2D_ERR_TIMEOUT;
+    }
+    return FS2D_OK;
+}
+
 // Array2D::extrapolate (include/Array2D.h:552-591) on caller-owned device
 // buffers; scratch is allocated with cudaMalloc for the duration of the call.
 extern "C" int fs2d_extrapolate(double* values, uint32_t* mask, int width, int height, int band, void* stream) {
@@ -789,9 +909,12 @@ extern "C" int fs2d_extrapolate(double* values, uint32_t* mask, int width, int h
     cudaStream_t st = (cudaStream_t)stream;
     rc = extrapolate_core(nullptr, st, x, aa, mm, W, H, band);
     cudaError_t e = cudaStreamSynchronize(st);
+    int werr = 0;
+    if (!rc && e == cudaSuccess) e = cudaMemcpy(&werr, x.max_layer + 12, sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(buf);
     if (rc) return rc;
-    return check_cuda(e, "fs2d_extrapolate");
+    if ((rc = check_cuda(e, "fs2d_extrapolate"))) return rc;
+    return extrap_wait_status(werr);
 }
 
 // ---------------------------------------------------------------------------
@@ -868,6 +991,9 @@ extern "C" int fs2d_extrapolate_noalloc(double* values, uint32_t* mask, int widt
     cudaStream_t st = (cudaStream_t)stream;
     rc = extrapolate_core(nullptr, st, x, aa, mm, W, H, band);
     cudaError_t e = cudaStreamSynchronize(st);
+    int werr = 0;
+    if (!rc && e == cudaSuccess) e = cudaMemcpy(&werr, x.max_layer + 12, sizeof(int), cudaMemcpyDeviceToHost);
     if (rc) return rc;
-    return check_cuda(e, "fs2d_extrapolate_noalloc");
+    if ((rc = check_cuda(e, "fs2d_extrapolate_noalloc"))) return rc;
+    return extrap_wait_status(werr);
 }

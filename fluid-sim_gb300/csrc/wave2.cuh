@@ -76,7 +76,7 @@ __device__ __forceinline__ bool spin_until_smem(volatile int* flag, int need, in
     long long polls = 0;
     while (*flag < need) {
         if (++polls > 64 * spin || ((polls & 1023) == 0 && wave_failed(err))) {
-            atomicOr(err, 1);
+            atomicOr(err, kWaitWarp | (kWaveKindWave2 << 4));
             return false;
         }
     }
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsign
             unsigned long long v;
             while ((v = ld_acquire(gprev)) < need) {
                 if (++polls > 16 * spin || ((polls & 255) == 0 && wave_failed(err))) {
-                    atomicOr(err, 1);
+                    atomicOr(err, kWaitStrip | (kWaveKindWave2 << 4));
                     v = need;
                     break;
                 }
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsign
                             long long polls = 0;
                             while (c + 1 - eread[w + 1] > kW2EdgeRing - 64) {
                                 if (++polls > spin || wave_failed(err)) {
-                                    atomicOr(err, 1);
+                                    atomicOr(err, kWaitWarp | (kWaveKindWave2 << 4));
                                     break;
                                 }
                                 __nanosleep(20);

@@ -26,6 +26,8 @@ NOT_CONVERGED = 4
 NONFINITE = 5
 TIMEOUT = 6
 KINDS = {"closest_point": 1, "eikonal": 2, "mic_fp64": 4, "mic_fp32": 8}
+# the sweep the timeout message names for each kind
+NAMES = {"closest_point": b"closest-point", "eikonal": b"Eikonal", "mic_fp64": b"FP64 MIC(0)", "mic_fp32": b"FP32 MIC(0)"}
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -74,7 +76,8 @@ def test_wavefront_wait_runs_out_and_the_handle_recovers(kind):
     assert lib.fs2d_debug_wavefront(a.h, C.c_longlong(1 << 12), KINDS[kind], 0) == 0
     rc = lib.fs2d_run_frame(a.h)
     assert rc == TIMEOUT, (kind, rc, lib.fs2d_last_error())
-    assert b"timed out" in lib.fs2d_last_error()
+    msg = lib.fs2d_last_error()
+    assert b"timed out waiting for its neighbour strip" in msg and NAMES[kind] in msg, msg
     assert a.stats()["lastStatus"] == TIMEOUT
     # hold off, default limit; the same frame again from the saved state
     assert lib.fs2d_debug_wavefront(a.h, C.c_longlong(0), 0, 0) == 0
