@@ -24,6 +24,7 @@
 #include <numeric>
 #include <string>
 #include <thread>
+#include <array>
 #include <vector>
 
 #include "fs2d_internal.cuh"
@@ -53,6 +54,18 @@ struct fs2d_batch {
     fs2d::LsBatch* ls = nullptr;
     cudaEvent_t swept = nullptr;          // the batched sweeps are done
     cudaEvent_t ls_t0 = nullptr, ls_t1 = nullptr;
+    // per scene, the device work of its three phases of a frame (before the
+    // batched level-set sweeps, between them and the joint solve, after it)
+    // as CUDA graphs, captured on the phase's second run and replayed after
+    struct PhaseGraph {
+        cudaGraphExec_t exec = nullptr;
+        unsigned long long generation = 0;   // the scene's generation when captured
+        unsigned long long kernels = 0;      // kernels per replay
+        int runs = 0;
+        bool direct = false;                 // capture failed: launch directly
+    };
+    std::vector<std::array<PhaseGraph, 3>> graphs;
+    bool use_graphs = true;
 };
 
 namespace fs2d {
@@ -150,6 +163,53 @@ int on_workers(const std::vector<std::vector<int>>& parts, int device, F fn) {
     return first_error(ws);
 }
 
+// One per-scene phase of a batch frame: `body` queues its device work on
+// the scene's stream (no host synchronisation inside).  The first run
+// launches directly (and fills the caches of kernel attributes), the second
+// captures the work into a graph, later runs replay it; a changed scene
+// (new buffers or parameters) is captured again, and a phase that cannot be
+// captured keeps launching directly.
+template <class Body>
+int run_phase(fs2d_batch* b, int k, int ph, Body&& body) {
+    Sim* s = sim_of(b->sims[k]);
+    fs2d_batch::PhaseGraph& g = b->graphs[k][ph];
+    if (!b->use_graphs || g.direct || g.runs++ == 0) return body();
+    if (g.exec && g.generation == s->generation) {
+        s->launches += g.kernels;
+        return check_cuda(cudaGraphLaunch(g.exec, s->stream), "cudaGraphLaunch");
+    }
+    if (g.exec) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+    }
+    if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        (void)cudaGetLastError();
+        g.direct = true;
+        return body();
+    }
+    const unsigned long long l0 = s->launches;
+    s->capturing = true;
+    int rc = body();
+    s->capturing = false;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(s->stream, &graph);
+    if (!rc && e == cudaSuccess && graph) e = cudaGraphInstantiate(&g.exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (rc || e != cudaSuccess || !g.exec) {
+        // nothing of the capture ran: launch the phase directly, now and from
+        // now on (a real error of the work shows up again there)
+        (void)cudaGetLastError();
+        if (g.exec) cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        s->launches = l0;
+        g.direct = true;
+        return body();
+    }
+    g.generation = s->generation;
+    g.kernels = s->launches - l0;
+    return check_cuda(cudaGraphLaunch(g.exec, s->stream), "cudaGraphLaunch");
+}
+
 // Frames of a mixed-precision batch: the workers queue every scene's stages
 // up to its pressure solve's setup; one pack solve then solves all scenes
 // together on the batch's stream (one launch per kernel of the inner solve
@@ -168,7 +228,7 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
         int rc = on_workers(parts, b->device, [&](int k) {
             st[k] = 0;
             fs2d_sim* p = b->sims[k];
-            int r = frame_levelset(p, 1);
+            int r = run_phase(b, k, 0, [&] { return frame_levelset(p, 1); });
             if (!r) r = check_cuda(cudaEventRecord(b->ready[k], sim_of(p)->stream), "cudaEventRecord");
             return r;
         });
@@ -181,8 +241,12 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
         rc = on_workers(parts, b->device, [&](int k) {
             fs2d_sim* p = b->sims[k];
             int r = check_cuda(cudaStreamWaitEvent(sim_of(p)->stream, b->swept, 0), "cudaStreamWaitEvent");
-            if (!r) r = frame_levelset(p, 2);
-            if (!r) r = frame_stages(p, 1, frame_solve_stage(p) + 1, &st[k], 1);
+            if (!r) r = run_phase(b, k, 1, [&] {
+                int q = frame_levelset(p, 2);
+                if (!q) q = frame_stages(p, 1, frame_solve_stage(p) + 1, &st[k], 1);
+                return q;
+            });
+            if (!r) frame_mark(p, 1);
             if (!r) r = check_cuda(cudaEventRecord(b->ready[k], sim_of(p)->stream), "cudaEventRecord");
             return r;
         });
@@ -191,7 +255,10 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
         FS2D_CUDA(cudaStreamSynchronize(b->stream));   // the scenes' stages before the solve are done
         b->phase_ms[0] += ms_since(t0);
         float ls_ms = 0;
-        cudaEventElapsedTime(&ls_ms, b->ls_t0, b->ls_t1);
+        if (cudaEventElapsedTime(&ls_ms, b->ls_t0, b->ls_t1) != cudaSuccess) {
+            ls_ms = 0;
+            (void)cudaGetLastError();
+        }
         b->phase_ms[3] += ls_ms;
         t0 = clk::now();
         rc = pack_solve(b->pack, b->opt, b->stream, &b->launches, b->err, b->device, nullptr);
@@ -210,7 +277,8 @@ int run_packed(fs2d_batch* b, int w, int nframes) {
         rc = on_workers(parts, b->device, [&](int k) {
             fs2d_sim* p = b->sims[k];
             int r = check_cuda(cudaStreamWaitEvent(sim_of(p)->stream, b->solved, 0), "cudaStreamWaitEvent");
-            if (!r) r = frame_stages(p, frame_solve_stage(p), -1, &st[k], 2);
+            if (!r) r = run_phase(b, k, 2, [&] { return frame_stages(p, frame_solve_stage(p), -1, &st[k], 2); });
+            if (!r) frame_mark(p, 2);
             r = frame_close(p, r, st[k]);
             b->status[k] = r;
             if (r == FS2D_ERR_NOT_CONVERGED) {
@@ -332,6 +400,7 @@ int fs2d_batch_create(const fs2d_config* cfgs, int n, const fs2d_options* opt, i
         }
         if (!rc) rc = pack_tune(b->pack, b->stream, b->err, b->device, &b->launches, &b->sweep_us);
         if (!rc) b->ls = ls_batch_create(ss.data(), n, b->device, &rc);
+        b->graphs.resize(n);
         if (!rc) rc = check_cuda(cudaEventCreateWithFlags(&b->swept, cudaEventDisableTiming), "cudaEventCreate");
         if (!rc) rc = check_cuda(cudaEventCreate(&b->ls_t0), "cudaEventCreate");
         if (!rc) rc = check_cuda(cudaEventCreate(&b->ls_t1), "cudaEventCreate");
@@ -419,6 +488,9 @@ int fs2d_batch_destroy(fs2d_batch* b) {
         if (e) cudaEventDestroy(e);
     if (b->solved) cudaEventDestroy(b->solved);
     fs2d::ls_batch_free(b->ls);
+    for (auto& gs : b->graphs)
+        for (auto& g : gs)
+            if (g.exec) cudaGraphExecDestroy(g.exec);
     for (cudaEvent_t e : {b->swept, b->ls_t0, b->ls_t1})
         if (e) cudaEventDestroy(e);
     if (b->err) cudaFree(b->err);
@@ -443,6 +515,19 @@ int fs2d_batch_set_schedule(fs2d_batch* b, int schedule, int ctas) {
         return FS2D_ERR_INVALID;
     }
     return fs2d::pack_set_schedule(b->pack, schedule, ctas, b->stream);
+}
+
+int fs2d_batch_set_graphs(fs2d_batch* b, int on) {
+    if (!b) return FS2D_ERR_INVALID;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    for (fs2d_sim* p : b->sims) cudaStreamSynchronize(fs2d::sim_of(p)->stream);
+    for (auto& gs : b->graphs)
+        for (auto& g : gs) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g = fs2d_batch::PhaseGraph();
+        }
+    b->use_graphs = on != 0;
+    return FS2D_OK;
 }
 
 int fs2d_batch_phase_ms(fs2d_batch* b, double* ms) {

@@ -81,6 +81,8 @@ void ktimer_collect(Sim* s) {
             auto& acc = s->kt_acc[pr.first];
             acc.first += 1;
             acc.second += ms;
+        } else {
+            (void)cudaGetLastError();
         }
     }
     s->kt_pending.clear();
@@ -174,6 +176,7 @@ struct Host {
     Sim sim;
     std::vector<float> frame_stage_ms;  // numStages per frame
     bool stats_pending = false;
+    bool solve_pending = false;   // a batch frame's solve scalars are on their way to pcg_host
 };
 
 template <typename T>
@@ -201,6 +204,7 @@ const int kPicStages[8] = {FS2D_STAGE_CREATE_WATER_LEVEL_SET, FS2D_STAGE_TRANSFE
                            FS2D_STAGE_UPDATE_PARTICLE_VELOCITIES, FS2D_STAGE_APPLY_ADVECTION};
 
 int alloc_particles(Sim* s, size_t cap) {
+    s->generation++;
     cudaFree(s->pos);
     cudaFree(s->vel);
     cudaFree(s->ent_u);
@@ -286,6 +290,8 @@ int alloc_all(Sim* s) {
     A(pcg, 1);
     s->progress_cap = std::max(s->NX, s->NY) / 32 + 2;
     A(progress, (size_t)s->progress_cap);
+    A(gprogress, (size_t)s->progress_cap);
+    A(gbase, 1);
     A(cp_tab, (size_t)s->P + s->NY);
     A(cpc, 1);
     A(cp_hb_t, (size_t)s->progress_cap * s->P);
@@ -353,7 +359,7 @@ void free_all(Sim* s) {
                     s->m32.pc, s->m32.fa, s->m32.fb, s->m32.fc, s->m32.fd, s->m32.r, s->m32.rp, s->m32.q,
                     s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32,
                     s->pos_df,
-                    s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p, s->phi_p, s->emask};
+                    s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p, s->phi_p, s->emask, s->gprogress, s->gbase};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->pcg_host) cudaFreeHost(s->pcg_host);
@@ -464,6 +470,12 @@ Host* H(fs2d_sim* p) { return reinterpret_cast<Host*>(p); }
 // its two timing events.  With a pack solve in between (a batch), the
 // projection stage is split: `solve_part` 1 runs its FP64 build and FP32
 // setup and stops, 2 takes the finished solve's statistics and goes on.
+// Records a stage-timing event on the handle's stream; inside a stream
+// capture as an event node of the graph, so every replay records it.
+static cudaError_t stage_event(Sim* s, cudaEvent_t e) {
+    return s->capturing ? cudaEventRecordWithFlags(e, s->stream, cudaEventRecordExternal) : cudaEventRecord(e, s->stream);
+}
+
 int frame_stages(fs2d_sim* p, int k0, int k1, int* status, int solve_part) {
     Host* h = H(p);
     Sim* s = &h->sim;
@@ -472,7 +484,7 @@ int frame_stages(fs2d_sim* p, int k0, int k1, int* status, int solve_part) {
     if (k1 < 0) k1 = n;
     for (int k = k0; k < k1; k++) {
         const bool split = solve_part != 0 && st[k] == FS2D_STAGE_APPLY_PROJECTION;
-        if (!(split && solve_part == 2)) FS2D_CUDA(cudaEventRecord(s->ev[2 * k], s->stream));
+        if (!(split && solve_part == 2)) FS2D_CUDA(stage_event(s, s->ev[2 * k]));
         int sst = 0;
         int rc;
         if (split && solve_part == 1) {
@@ -481,13 +493,15 @@ int frame_stages(fs2d_sim* p, int k0, int k1, int* status, int solve_part) {
             if (rc) return rc;
             return 0;   // the pack solve follows
         } else if (split) {
-            rc = mixed_finish(s, &sst);
+            // the solve's scalars are read when the frame closes (no wait here;
+            // frame_mark(p, 2) flags them)
+            rc = mixed_finish_queue(s);
         } else {
             rc = run_stage_impl(s, st[k], &sst);
         }
         if (rc) return rc;
         if (sst) *status = sst;
-        FS2D_CUDA(cudaEventRecord(s->ev[2 * k + 1], s->stream));
+        FS2D_CUDA(stage_event(s, s->ev[2 * k + 1]));
         if (st[k] == FS2D_STAGE_CREATE_WATER_LEVEL_SET) h->stats_pending = true;
     }
     return 0;
@@ -500,14 +514,22 @@ int frame_levelset(fs2d_sim* p, int part) {
     Host* h = H(p);
     Sim* s = &h->sim;
     if (part == 1) {
-        FS2D_CUDA(cudaEventRecord(s->ev[0], s->stream));
+        FS2D_CUDA(stage_event(s, s->ev[0]));
         return levelset_seed(s);
     }
     int rc = levelset_finish(s);
     if (rc) return rc;
-    FS2D_CUDA(cudaEventRecord(s->ev[1], s->stream));
-    h->stats_pending = true;
+    FS2D_CUDA(stage_event(s, s->ev[1]));
     return 0;
+}
+
+// Host bookkeeping of a batch frame's phases (done on every frame, also when
+// the phase's device work was replayed from a graph): 1 the level set's
+// statistics are due at frame close, 2 so are the solve's scalars.
+void frame_mark(fs2d_sim* p, int what) {
+    Host* h = H(p);
+    if (what == 1) h->stats_pending = true;
+    if (what == 2) h->solve_pending = true;
 }
 
 int frame_solve_stage(fs2d_sim* p) {
@@ -522,12 +544,24 @@ int frame_solve_stage(fs2d_sim* p) {
 int frame_close(fs2d_sim* p, int rc, int status) {
     Host* h = H(p);
     Sim* s = &h->sim;
-    if (rc) return rc;
+    if (rc) {
+        h->solve_pending = false;
+        return rc;
+    }
     rc = finish(h);
+    if (h->solve_pending) {   // the frame's solve scalars arrived with finish's wait
+        int sst = 0;
+        mixed_finish_read(s, &sst);
+        if (!status) status = sst;
+        h->solve_pending = false;
+    }
     const int n = num_stages(s);
     for (int k = 0; k < n; k++) {
         float ms = 0;
-        cudaEventElapsedTime(&ms, s->ev[2 * k], s->ev[2 * k + 1]);
+        if (cudaEventElapsedTime(&ms, s->ev[2 * k], s->ev[2 * k + 1]) != cudaSuccess) {
+            ms = 0;
+            (void)cudaGetLastError();   // no stale error for the next call to pick up
+        }
         s->stage_ms[k] = ms;
         h->frame_stage_ms.push_back(ms);
     }
@@ -838,6 +872,7 @@ int fs2d_upload_state(fs2d_sim* p, const fs2d_state* st) {
     if (!p || !st) return FS2D_ERR_INVALID;
     Sim* s = &H(p)->sim;
     FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    s->generation++;
     auto up = [&](void* d, const void* src, size_t bytes) -> int {
         if (!src) return 0;
         return check_cuda(cudaMemcpyAsync(d, src, bytes, cudaMemcpyHostToDevice, s->stream), "upload");
@@ -917,6 +952,7 @@ int fs2d_set_params(fs2d_sim* p, double gx, double gy, double alpha, double dt) 
     s->gy = gy;
     s->alpha = alpha;
     s->dt = dt;
+    s->generation++;
     return FS2D_OK;
 }
 
@@ -1085,6 +1121,7 @@ int fs2d_set_kernel_timing(fs2d_sim* p, const char* patterns) {
     FS2D_CUDA(cudaStreamSynchronize(s->stream));
     ktimer_collect(s);
     s->kt_patterns = patterns ? patterns : "";
+    s->generation++;
     s->kt_match.clear();
     s->kt_acc.clear();
     return FS2D_OK;

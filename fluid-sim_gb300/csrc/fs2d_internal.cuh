@@ -256,6 +256,16 @@ struct Sim {
     unsigned long long* progress = nullptr;
     int progress_cap = 0;
     unsigned long long wave_launch = 0;
+    // wavefront sweeps captured into a CUDA graph (a batch's per-scene
+    // phases): their own progress flags and a device-side base that a
+    // one-thread kernel before each such sweep advances, so every replay
+    // starts from fresh bases
+    bool capturing = false;
+    unsigned long long* gprogress = nullptr;
+    unsigned long long* gbase = nullptr;
+    // bumped whenever buffers, parameters or options change: a captured
+    // phase of an older generation is captured again
+    unsigned long long generation = 0;
 
     // frame statistics and errors
     FrameStats* stats = nullptr;
@@ -397,6 +407,9 @@ int pack_set_schedule(Pack* pk, int schedule, int ctas, cudaStream_t stream);
 // Statistics of the handle's last mixed solve (from its scalars); *status =
 // FS2D_ERR_NOT_CONVERGED when it stopped short of its tolerance.
 int mixed_finish(Sim* s, int* status);
+// mixed_finish in two halves (a batch frame reads the scalars at frame close)
+int mixed_finish_queue(Sim* s);
+void mixed_finish_read(Sim* s, int* status);
 int cp_setup_maps(Sim* s);                // TMA descriptors of the closest-point sweeps
 int update_velocity(Sim* s);              // updateVelocity
 int g2p(Sim* s);                          // updateParticleVelocities
@@ -429,6 +442,7 @@ void rollout_free(Sim* s);
 // ---- frames in parts (capi.cu), for batches that solve their scenes together ----
 int frame_stages(fs2d_sim* p, int k0, int k1, int* status, int solve_part = 0);
 int frame_levelset(fs2d_sim* p, int part);
+void frame_mark(fs2d_sim* p, int what);
 int frame_solve_stage(fs2d_sim* p);   // index of applyProjection in the frame's stage order
 int frame_close(fs2d_sim* p, int rc, int status);
 Sim* sim_of(fs2d_sim* p);

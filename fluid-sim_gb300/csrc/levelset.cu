@@ -693,30 +693,28 @@ LsBatch* ls_batch_create(Sim* const* sims, int n, int device, int* rc_out) {
         memset((void*)&b->ek[k], 0xff, sizeof(EkScene));
         memset((void*)&b->cells[k], 0xff, sizeof(LsCells));
     }
-    // block map of the per-cell kernels and the work list: strip-major (every
-    // scene's first strip, scenes by decreasing rows, then every second
-    // strip, ...), progress counters numbered scene by scene
-    std::vector<int> blk, first(n), order(n);
+    // block map of the per-cell kernels and the work list, critical path
+    // first: a strip's rank is (strips after it) x the strip-to-strip lag
+    // (~45 column steps measured) + its own steps; progress counters are
+    // numbered scene by scene
+    std::vector<int> blk, first(n);
     int pidx = 0;
     for (int k = 0; k < n; k++) {
         const Sim* s = sims[k];
         blk.insert(blk.end(), (size_t)((s->NX + 127) / 128) * s->NY, k);
         first[k] = pidx;
         pidx += (s->NY + 31) / 32;
-        order[k] = k;
     }
-    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return sims[x]->NY > sims[y]->NY; });
+    std::vector<std::pair<long long, WaveItem>> ranked;
+    for (int k = 0; k < n; k++) {
+        const int ns = (sims[k]->NY + 31) / 32;
+        for (int st = 0; st < ns; st++)
+            ranked.push_back({(long long)(ns - 1 - st) * 45 + sims[k]->P + 31, WaveItem{k, st, first[k] + st}});
+    }
+    std::stable_sort(ranked.begin(), ranked.end(), [](const std::pair<long long, WaveItem>& a,
+                                                      const std::pair<long long, WaveItem>& b) { return a.first > b.first; });
     std::vector<WaveItem> items;
-    for (int st = 0;; st++) {
-        bool any = false;
-        for (int k : order) {
-            if (st < (sims[k]->NY + 31) / 32) {
-                items.push_back(WaveItem{k, st, first[k] + st});
-                any = true;
-            }
-        }
-        if (!any) break;
-    }
+    for (const auto& r : ranked) items.push_back(r.second);
     b->nblk = (int)blk.size();
     b->nitems = (int)items.size();
     if (!rc) rc = ls_alloc(&b->d_cp, n);

@@ -181,6 +181,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             const unsigned r_bnd = next_local ? mapa_shared((const void*)bnd, crank + 1) : 0u;
             const unsigned r_used = next_local ? mapa_shared((const void*)bnd_used, crank + 1) : 0u;
             int ts = 0;                                        // next tile to store
+            int confirmed = 0;                                 // stored tiles whose slots are released
             unsigned long long gavail = 0;
             long long idle = 0;
             while (hb < NR || tc < tend || ts < nt) {
@@ -258,6 +259,16 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 }
                 if (moved) {
                     idle = 0;
+                } else if (confirmed < ts) {
+                    // nothing else to do: wait for the newest store to read its
+                    // tile and release its slot now, so the compute warp finds it
+                    // free instead of waiting for the next store
+                    if (lane == 0) {
+                        bulk_wait_read<0>();
+                        *tiles_freed = ts;
+                    }
+                    __syncwarp();
+                    confirmed = ts;
                 } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(err))) {
                     if (lane == 0) atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
                     break;

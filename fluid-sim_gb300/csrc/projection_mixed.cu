@@ -960,7 +960,7 @@ __global__ void k_set_done(const PackScene* __restrict__ sc, int n, int done) {
 
 // Autotuner of the persistent sweep of several scenes: the schedule (the
 // order of the work list: whole scenes as given, by decreasing rows or by
-// decreasing cells, or strip-major) and the number of persistent CTAs
+// decreasing cells, strip-major, or critical path first) and the number of persistent CTAs
 // (all SMs, three quarters, half) are each timed on forward sweeps of the
 // pack (CUDA events, after a warm-up sweep), and the fastest pair is kept.
 // A scene's results do not depend on either choice: its strips are computed
@@ -982,6 +982,28 @@ static std::vector<Mic32Item> pack_schedule(const Pack* pk, int variant) {
             return (long long)pk->scenes[a].NY32 * pk->scenes[a].P32 > (long long)pk->scenes[b].NY32 * pk->scenes[b].P32;
         });
     std::vector<Mic32Item> items;
+    if (variant == 4) {
+        // critical path first: a strip's rank is the time from its start to
+        // the end of its scene's last strip if nothing waits, (strips after
+        // it) x the strip-to-strip lag + its own steps, in column steps (lag
+        // ~66 steps measured); a scene's strips keep their order because the
+        // rank falls along the scene
+        struct Ranked {
+            long long rank;
+            Mic32Item item;
+        };
+        std::vector<Ranked> all;
+        for (int k = 0; k < pk->n; k++) {
+            const PackScene& e = pk->scenes[k];
+            const int ns = e.P32 / kM32Cols;
+            for (int st = 0; st < ns; st++)
+                all.push_back(Ranked{(long long)(ns - 1 - st) * 66 + e.NY32 + 31,
+                                     Mic32Item{k, st, ns, e.x0, e.P32, e.y0, e.NY32, strip0[k] + st}});
+        }
+        std::stable_sort(all.begin(), all.end(), [](const Ranked& a, const Ranked& b) { return a.rank > b.rank; });
+        for (const Ranked& r : all) items.push_back(r.item);
+        return items;
+    }
     if (variant < 3) {
         for (int k : order) {
             const PackScene& e = pk->scenes[k];
@@ -1012,8 +1034,8 @@ static std::vector<Mic32Item> pack_schedule(const Pack* pk, int variant) {
 }
 
 int pack_set_schedule(Pack* pk, int schedule, int ctas, cudaStream_t stream) {
-    if (pk->n < 2 || schedule < 0 || schedule > 3 || ctas < 0) {
-        set_error("schedule %d / %d CTAs: a batch's schedule is 0..3 and its CTA count >= 0", schedule, ctas);
+    if (pk->n < 2 || schedule < 0 || schedule > 4 || ctas < 0) {
+        set_error("schedule %d / %d CTAs: a batch's schedule is 0..4 and its CTA count >= 0", schedule, ctas);
         return FS2D_ERR_INVALID;
     }
     const std::vector<Mic32Item> items = pack_schedule(pk, schedule);
@@ -1035,7 +1057,7 @@ int pack_tune(Pack* pk, cudaStream_t stream, int* err, int device, unsigned long
     int sms = 1;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     std::vector<std::vector<Mic32Item>> schedules;
-    for (int variant = 0; variant < 4; variant++) schedules.push_back(pack_schedule(pk, variant));
+    for (int variant = 0; variant < 5; variant++) schedules.push_back(pack_schedule(pk, variant));
     const int ctas[3] = {sms, sms * 3 / 4, sms / 2};
     cudaEvent_t e0, e1;
     FS2D_CUDA(cudaEventCreate(&e0));
@@ -1082,15 +1104,27 @@ int pack_tune(Pack* pk, cudaStream_t stream, int* err, int device, unsigned long
 }
 
 int mixed_finish(Sim* s, int* status) {
-    FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, s->pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
+    if (int rc = mixed_finish_queue(s)) return rc;
     if (int rcw = wait_stream(s, s->stream)) return rcw;
+    mixed_finish_read(s, status);
+    return 0;
+}
+
+// The solver's scalars to the host, queued on the handle's stream.
+int mixed_finish_queue(Sim* s) {
+    FS2D_CUDA(cudaMemcpyAsync(s->pcg_host, s->pcg, sizeof(PcgScalars), cudaMemcpyDeviceToHost, s->stream));
+    return 0;
+}
+
+// Statistics and status of the solve, once the copy queued by
+// mixed_finish_queue has arrived.
+void mixed_finish_read(Sim* s, int* status) {
     const PcgScalars& o = *s->pcg_host;
     s->last_iters = o.inner_total;
     s->last_outer = o.outer_iters;
     const bool solved = o.rhs_norm > 1e-12;
     s->last_rel_res = o.rhs_norm > 0 ? (solved ? o.r_norm : o.rhs_norm) / o.rhs_norm : 0.0;
     if (status) *status = (solved && o.r_norm > o.tol_abs) ? FS2D_ERR_NOT_CONVERGED : 0;
-    return 0;
 }
 
 int projection_mixed(Sim* s, int* status) { return projection_mixed_rhs(s, nullptr, status); }

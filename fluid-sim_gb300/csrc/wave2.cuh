@@ -85,7 +85,12 @@ __device__ __forceinline__ bool spin_until_smem(volatile int* flag, int need, in
 
 template <class Op, int W, int CH>
 __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsigned long long* progress,
-                                                       unsigned long long base, int* err, const int* skip) {
+                                                       unsigned long long base_host,
+                                                       const unsigned long long* base_dev, int* err,
+                                                       const int* skip) {
+    // progress values of this launch are base + columns (base_dev: a
+    // graph-replayed launch, its base advanced by the kernel before it)
+    const unsigned long long base = base_dev != nullptr ? *base_dev + base_host : base_host;
     typedef typename Op::T T;
     constexpr int NA = Op::NA;
     constexpr int RC = kW2Ring * kW2Tile;  // ring columns per row
@@ -317,6 +322,10 @@ __global__ void __launch_bounds__(32 * W) wave2_kernel(Op op, WaveGeom g, unsign
     cp_async_wait<0>();
 }
 
+// Advances the device base of graph-replayed sweeps by one sweep's worth
+// (progress values are base + columns, columns < 2^24).
+static __global__ void k_wave2_bump(unsigned long long* base) { *base += 1ull << 24; }
+
 // Cooperative launch of the staged wavefront; W warps per CTA.
 template <class Op, int W, int CH>
 int launch_wave2(Sim* s, const Op& op, WaveGeom g, const int* skip) {
@@ -332,8 +341,18 @@ int launch_wave2(Sim* s, const Op& op, WaveGeom g, const int* skip) {
     constexpr size_t smem = wave2_smem_bytes<Op, W, CH>();
     static std::atomic<unsigned long long> configured{0};
     if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)wave2_kernel<Op, W, CH>, (int)smem)) return rc0;
-    unsigned long long base = wave_begin(s);
-    void* args[] = {(void*)&op, (void*)&g, (void*)&s->progress, (void*)&base, (void*)&s->err, (void*)&skip};
+    // direct launch: a host base and the handle's progress flags; inside a
+    // stream capture: the graph's flags and device base, advanced first
+    unsigned long long base = s->capturing ? 0ull : wave_begin(s);
+    const unsigned long long* base_dev = s->capturing ? s->gbase : nullptr;
+    unsigned long long* progress = s->capturing ? s->gprogress : s->progress;
+    if (s->capturing) {
+        s->launches++;
+        k_wave2_bump<<<1, 1, 0, s->stream>>>(s->gbase);
+        if (int rc1 = check_cuda(cudaGetLastError(), "k_wave2_bump")) return rc1;
+    }
+    void* args[] = {(void*)&op, (void*)&g, (void*)&progress, (void*)&base, (void*)&base_dev, (void*)&s->err,
+                    (void*)&skip};
     s->launches++;
     long long kt = ktimer_begin(s, Op::kName);
     int rc = check_cuda(cudaLaunchCooperativeKernel((const void*)wave2_kernel<Op, W, CH>, dim3(nctas), dim3(32 * W),

@@ -106,6 +106,7 @@ SIGNATURES = {
     "fs2d_batch_destroy": (C.c_int, [C.c_void_p]),
     "fs2d_batch_launch_count": (C.c_int, [C.c_void_p, C.POINTER(C.c_ulonglong)]),
     "fs2d_batch_phase_ms": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "fs2d_batch_set_graphs": (C.c_int, [C.c_void_p, C.c_int]),
     "fs2d_batch_set_schedule": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "fs2d_batch_sweep_schedule": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]),
@@ -480,8 +481,13 @@ class Batch:
         return {"schedule": sc.value, "ctas": ct.value, "items": it.value, "sweep_us": us.value}
 
     def set_schedule(self, schedule, ctas=0):
-        """Override the autotuned sweep schedule (0..3) and CTA count."""
+        """Override the autotuned sweep schedule (0..4) and CTA count."""
         _check(load().fs2d_batch_set_schedule(self.h, int(schedule), int(ctas)))
+
+    def set_graphs(self, on):
+        """Replay each scene's per-frame phases from CUDA graphs (default) or
+        launch them directly."""
+        _check(load().fs2d_batch_set_graphs(self.h, 1 if on else 0))
 
     def phase_ms(self):
         """ms of the last step() of a mixed-precision batch: wall clock of the

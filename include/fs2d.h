@@ -262,7 +262,7 @@ int fs2d_batch_launch_count(fs2d_batch* batch, unsigned long long* out);
  * choice, the number of work items and the chosen sweep's time (schedule -1
  * for an FP64 batch).  Any pointer may be NULL. */
 int fs2d_batch_sweep_schedule(fs2d_batch* batch, int* schedule, int* ctas, int* items, double* sweepUs);
-/* Overrides the autotuner: schedule 0..3 and, ctas > 0, the number of
+/* Overrides the autotuner: schedule 0..4 and, ctas > 0, the number of
  * persistent CTAs (at most the SM count).  A scene's results do not depend on
  * either. */
 int fs2d_batch_set_schedule(fs2d_batch* batch, int schedule, int ctas);
@@ -273,6 +273,12 @@ int fs2d_batch_set_schedule(fs2d_batch* batch, int schedule, int ctas);
  * remaining stages; ms[3] the device time of the level-set sweeps of all
  * scenes (part of ms[0]). */
 int fs2d_batch_phase_ms(fs2d_batch* batch, double* ms);
+/* Per-scene work between the batch's joint steps (a mixed-precision batch):
+ * on (default), each scene's three phases of a frame are captured into CUDA
+ * graphs on their second frame and replayed after (captured again when the
+ * scene's state or parameters change); off, launched directly.  Results do
+ * not depend on it. */
+int fs2d_batch_set_graphs(fs2d_batch* batch, int on);
 /* fs2d_forward / fs2d_backward for every scene of a batch (each a closed box:
  * no EMPTY cell, semi-Lagrangian mode), scenes issued concurrently by the
  * batch's workers (all hardware threads up to 16 while the count is not

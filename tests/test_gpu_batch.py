@@ -43,7 +43,7 @@ def test_batch_matches_scenes_run_alone(workers):
     b.close()
 
 
-@pytest.mark.parametrize("schedule,ctas", [(None, 0), (0, 0), (1, 3), (2, 0), (3, 2)])
+@pytest.mark.parametrize("schedule,ctas", [(None, 0), (0, 0), (1, 3), (2, 0), (3, 2), (4, 5)])
 def test_batch_of_wide_scenes_matches_scenes_run_alone(schedule, ctas):
     """Scenes of one to three strips of the FP32 sweeps (strips of 128
     columns): the persistent sweep's work items hand columns over between
@@ -52,7 +52,7 @@ def test_batch_of_wide_scenes_matches_scenes_run_alone(schedule, ctas):
     scs = scenes.batch_dam_breaks(6, seed=11, lo=100, hi=300)
     b = fs2d.Batch(scs, workers=2, seed=30, **OPTS)
     sch = b.sweep_schedule()
-    assert 0 <= sch["schedule"] <= 3 and sch["items"] >= 6 and sch["sweep_us"] > 0
+    assert 0 <= sch["schedule"] <= 4 and sch["items"] >= 6 and sch["sweep_us"] > 0
     if schedule is not None:
         b.set_schedule(schedule, ctas)
         assert b.sweep_schedule()["schedule"] == schedule
@@ -69,6 +69,32 @@ def test_batch_of_wide_scenes_matches_scenes_run_alone(schedule, ctas):
     assert v.runFrame() in (0, 4)
     assert_same(v.get_state(FIELDS), alone(scs[4], 34, 3))
     b.close()
+
+
+def test_graph_replay_matches_direct_launches():
+    """Each scene's per-frame phases replayed from CUDA graphs (captured on
+    the second frame) give the bits of direct launches, also after a scene's
+    state is replaced between steps (its phases are captured again)."""
+    scs = scenes.batch_dam_breaks(4, seed=5, lo=40, hi=90)
+    g = fs2d.Batch(scs, workers=2, seed=50, **OPTS)
+    d = fs2d.Batch(scs, workers=2, seed=50, **OPTS)
+    d.set_graphs(False)
+    g.step(4)
+    d.step(4)
+    for k in range(len(scs)):
+        assert_same(g.scene(k).get_state(FIELDS), d.scene(k).get_state(FIELDS))
+    st = g.scene(1).get_state(["particles", "particleVels"])
+    st["particleVels"] = st["particleVels"] * 0.5
+    g.scene(1).set_state(st)
+    d.scene(1).set_state(st)
+    g.step(3)
+    d.step(3)
+    for k in range(len(scs)):
+        assert_same(g.scene(k).get_state(FIELDS), d.scene(k).get_state(FIELDS))
+        assert g.scene(k).stats()["frames"] == 7
+    assert g.launch_count() > 0
+    g.close()
+    d.close()
 
 
 def test_batch_chooses_its_worker_count():
