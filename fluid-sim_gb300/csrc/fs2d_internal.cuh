@@ -102,14 +102,14 @@ struct PackScene {
     int P32, NY32;           // padded extent (multiples of 128 columns and 32 rows)
     long long off;           // pack offset of the scene's cell (0, 0): y0 * pitch + x0
     int x0, y0;              // pack column and row of that cell
-    int gx, gy, blk0;        // FP32 reductions: gx x gy blocks of row segments, from block blk0
+    int nb32, blk0;          // FP32 kernels: nb32 blocks over the padded P32 x NY region, from block blk0
     int nb64, blk64;         // FP64 refinement kernels: nb64 blocks of 256 cells, from block blk64
     const uint8_t* cell;     // labels (NX x NY)
     const double *A0, *Ax, *Ay, *rhs;
     double *p, *r;           // FP64 pressure and residual
     PcgScalars *outer;       // the handle's FP64 scalars (refinement)
     PcgScalars *inner;       // the handle's FP32 scalars (inner solve)
-    float2* part;            // FP32 reduction partials (gx * gy), in the pack's buffer
+    float2* part;            // FP32 reduction partials (nb32), in the pack's buffer
     double* part64;          // FP64 residual partials (nb64), in the pack's buffer
 };
 

@@ -291,11 +291,17 @@ __device__ __forceinline__ void acc_prod(DF& a, float x, float y) {
     else df_add(a, df_prod(x, y));
 }
 
-// The inner kernels see a scene as row segments of kRC columns: thread t of
-// block (bx, by) takes the four adjacent columns bx*kRC + 4t .. +3 (128-bit
-// accesses; the pack's pitch and every scene's column origin are multiples
-// of 128 floats) of rows by, by + gy, ..., over the scene's padded width
-// P32, whose padding holds zeros.
+// The inner kernels see a scene's padded region (P32 x NY, row-major, the
+// pack's pitch between rows) as a run of float4s: thread t of the scene's
+// block b takes the four adjacent cells 4q .. 4q+3 for q = b*kRT + t,
+// b*kRT + t + nb32*kRT, ... (128-bit accesses: the pack's pitch and every
+// scene's column origin are multiples of 128 floats, and P32 of 4, so a
+// float4 never crosses a row).  The padding holds zeros.
+__device__ __forceinline__ void cell_of(unsigned q, int P32, int& i, int& j) {
+    const unsigned c = 4u * q;   // a region holds fewer than 2^31 cells (checked by pack_check)
+    j = (int)(c / (unsigned)P32);
+    i = (int)(c - (unsigned)j * (unsigned)P32);
+}
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ float4 fma4(float a, float4 x, float4 y) {
@@ -311,23 +317,22 @@ __global__ void __launch_bounds__(kRT) k_dot32(const PackScene* __restrict__ sc,
     PcgScalars* pcg = S.inner;
     if (pcg->done) return;
     const int lb = blockIdx.x - S.blk0;
-    const int bx = lb % S.gx, by = lb / S.gx;
-    const int i = bx * kRC + kRV * threadIdx.x;
+    const unsigned n4 = (unsigned)S.P32 * (unsigned)S.NY / kRV;
     DF a{0.f, 0.f};
-    if (i < S.P32) {
 #pragma unroll 2
-        for (int j = by; j < S.NY; j += S.gy) {
-            const size_t k = (size_t)S.off + (size_t)j * pitch + i;
-            const float4 zz = ld4(z + k), rr = ld4(r + k);
-            acc_prod<PLAIN>(a, zz.x, rr.x);
-            acc_prod<PLAIN>(a, zz.y, rr.y);
-            acc_prod<PLAIN>(a, zz.z, rr.z);
-            acc_prod<PLAIN>(a, zz.w, rr.w);
-        }
+    for (unsigned q = (unsigned)lb * kRT + threadIdx.x; q < n4; q += (unsigned)S.nb32 * kRT) {
+        int i, j;
+        cell_of(q, S.P32, i, j);
+        const size_t k = (size_t)S.off + (size_t)j * pitch + i;
+        const float4 zz = ld4(z + k), rr = ld4(r + k);
+        acc_prod<PLAIN>(a, zz.x, rr.x);
+        acc_prod<PLAIN>(a, zz.y, rr.y);
+        acc_prod<PLAIN>(a, zz.z, rr.z);
+        acc_prod<PLAIN>(a, zz.w, rr.w);
     }
-    df_block_partial<PLAIN>(a, S.part, by * S.gx + bx, sh);
-    if (last_block_of(&pcg->ticket[1], S.gx * S.gy)) {
-        const double s = df_final<PLAIN>(S.part, S.gx * S.gy, sh);
+    df_block_partial<PLAIN>(a, S.part, lb, sh);
+    if (last_block_of(&pcg->ticket[1], S.nb32)) {
+        const double s = df_final<PLAIN>(S.part, S.nb32, sh);
         if (threadIdx.x == 0) {
             if (init) {
                 pcg->sigma = s;
@@ -359,15 +364,16 @@ __global__ void __launch_bounds__(kRT) k_spmv32(const PackScene* __restrict__ sc
     const bool first = pcg->first != 0;
     const float beta = first ? 0.0f : (float)pcg->beta;
     const int lb = blockIdx.x - S.blk0;
-    const int bx = lb % S.gx, by = lb / S.gx;
-    const int i = bx * kRC + kRV * threadIdx.x;
+    const unsigned n4 = (unsigned)S.P32 * (unsigned)S.NY / kRV;
     const int P = pitch;
     // s of one cell or four, from z and s_old (the first iteration: z alone)
     auto s1 = [&](size_t k) { return first ? z[k] : fmaf(beta, s_old[k], z[k]); };
     auto s4 = [&](size_t k) { return first ? ld4(z + k) : fma4(beta, ld4(s_old + k), ld4(z + k)); };
     DF a{0.f, 0.f};
-    if (i < S.P32) {
-        for (int j = by; j < S.NY; j += S.gy) {
+    {
+        for (unsigned q = (unsigned)lb * kRT + threadIdx.x; q < n4; q += (unsigned)S.nb32 * kRT) {
+            int i, j;
+            cell_of(q, S.P32, i, j);
             const size_t k = (size_t)S.off + (size_t)j * P + i;
             const float4 sc0 = s4(k);
             st4(s_new + k, sc0);
@@ -393,9 +399,9 @@ __global__ void __launch_bounds__(kRT) k_spmv32(const PackScene* __restrict__ sc
             acc_prod<PLAIN>(a, out.w, sc0.w);
         }
     }
-    df_block_partial<PLAIN>(a, S.part, by * S.gx + bx, sh);
-    if (last_block_of(&pcg->ticket[2], S.gx * S.gy)) {
-        const double sum = df_final<PLAIN>(S.part, S.gx * S.gy, sh);
+    df_block_partial<PLAIN>(a, S.part, lb, sh);
+    if (last_block_of(&pcg->ticket[2], S.nb32)) {
+        const double sum = df_final<PLAIN>(S.part, S.nb32, sh);
         if (threadIdx.x == 0) {
             if (sum == 0.0) inner_stop(pcg, 1, ctl);
             else pcg->alpha = pcg->sigma / sum;
@@ -414,12 +420,13 @@ __global__ void __launch_bounds__(kRT) k_axpy32(const PackScene* __restrict__ sc
     if (pcg->done) return;
     const float alpha = (float)pcg->alpha;
     const int lb = blockIdx.x - S.blk0;
-    const int bx = lb % S.gx, by = lb / S.gx;
-    const int i = bx * kRC + kRV * threadIdx.x;
+    const unsigned n4 = (unsigned)S.P32 * (unsigned)S.NY / kRV;
     float m = 0.f;
-    if (i < S.P32) {
+    {
 #pragma unroll 2
-        for (int j = by; j < S.NY; j += S.gy) {
+        for (unsigned q = (unsigned)lb * kRT + threadIdx.x; q < n4; q += (unsigned)S.nb32 * kRT) {
+            int i, j;
+            cell_of(q, S.P32, i, j);
             const size_t k = (size_t)S.off + (size_t)j * pitch + i;
             st4(e + k, fma4(alpha, ld4(s + k), ld4(e + k)));
             const float4 rv = fma4(-alpha, ld4(w + k), ld4(r + k));
@@ -431,10 +438,10 @@ __global__ void __launch_bounds__(kRT) k_axpy32(const PackScene* __restrict__ sc
     }
     m = block_max_f(m, sh);
     float* partf = reinterpret_cast<float*>(S.part);
-    if (threadIdx.x == 0) partf[by * S.gx + bx] = m;
-    if (last_block_of(&pcg->ticket[3], S.gx * S.gy)) {
+    if (threadIdx.x == 0) partf[lb] = m;
+    if (last_block_of(&pcg->ticket[3], S.nb32)) {
         float mm = 0.f;
-        for (int k = threadIdx.x; k < S.gx * S.gy; k += blockDim.x) mm = fmaxf(mm, partf[k]);
+        for (int k = threadIdx.x; k < S.nb32; k += blockDim.x) mm = fmaxf(mm, partf[k]);
         mm = block_max_f(mm, sh);
         if (threadIdx.x == 0) {
             pcg->r_norm = mm;
@@ -574,8 +581,9 @@ PackScene scene_entry(Sim* s, int pitch, int x0, int y0) {
     e.x0 = x0;
     e.y0 = y0;
     e.off = (long long)y0 * pitch + x0;
-    e.gx = (e.P32 + kRC - 1) / kRC;
-    e.gy = std::max(1, std::min(s->NY, 1216 / e.gx));
+    // blocks of the FP32 kernels: one per kRC cells of the padded region, at
+    // most 8 per SM of a GB300
+    e.nb32 = (int)std::max(1LL, std::min((long long)e.P32 * s->NY / kRC, 1216LL));
     e.nb64 = (int)blocks_for(s->N, kT);
     e.cell = s->cell;
     e.A0 = s->Adiag;
@@ -602,9 +610,10 @@ int pack_check(const Pack* pk) {
         const PackScene& e = pk->scenes[k];
         const bool inside = e.x0 >= 0 && e.y0 >= 0 && e.x0 % kM32Cols == 0 && e.P32 >= e.NX && e.NY32 >= e.NY &&
                             e.P32 % kM32Cols == 0 && e.NY32 % kM32Rows == 0 && e.x0 + e.P32 <= pk->pitch &&
-                            e.y0 + e.NY32 <= pk->rows && e.off == (long long)e.y0 * pk->pitch + e.x0;
+                            e.y0 + e.NY32 <= pk->rows && e.off == (long long)e.y0 * pk->pitch + e.x0 &&
+                            (long long)e.P32 * e.NY32 < (1LL << 31);
         const bool set = e.cell && e.A0 && e.Ax && e.Ay && e.rhs && e.p && e.r && e.outer && e.inner && e.part &&
-                         e.part64 && e.gx >= 1 && e.gy >= 1 && e.nb64 >= 1;
+                         e.part64 && e.nb32 >= 1 && e.nb64 >= 1;
         if (!inside || !set) {
             set_error("pack: scene %d (%d x %d at %d, %d) does not fit the %d x %d arrays or lacks an array", k,
                       e.NX, e.NY, e.x0, e.y0, pk->pitch, pk->rows);
@@ -628,7 +637,7 @@ int pack_finish(Pack* pk) {
     for (int k = 0; k < pk->n; k++) {
         PackScene& e = pk->scenes[k];
         e.blk0 = (int)blk.size();
-        blk.insert(blk.end(), (size_t)e.gx * e.gy, k);
+        blk.insert(blk.end(), (size_t)e.nb32, k);
         e.blk64 = (int)blk64.size();
         blk64.insert(blk64.end(), (size_t)e.nb64, k);
         const int ns = e.P32 / kM32Cols;

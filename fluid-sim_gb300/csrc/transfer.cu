@@ -317,21 +317,49 @@ __global__ void k_g2p_adjoint(const double2* __restrict__ pos, const double2* __
 
 // Column pass of the L1 distance transform: vertical distance to the nearest
 // known face (mask 0) of the same column, kInf if none.  Written into d.
-__global__ void k_dt_cols(const uint32_t* __restrict__ mask, int* d, int W, int H) {
-    int x = blockIdx.x * blockDim.x + threadIdx.x;
-    if (x >= W) return;
-    int g = kInf;
-    for (int y = 0; y < H; y++) {
-        size_t c = (size_t)y * W + x;
-        g = (mask[c] == 0) ? 0 : (g >= kInf ? kInf : g + 1);
-        d[c] = g;
+// Column pass: d(x, y) = distance along the column to the nearest known
+// face (mask 0), kInf if the column has none: the reference's order-free
+// BFS distance restricted to one column.  Block = 32 columns x 32 row
+// segments; each thread finds the last and the first known face of its
+// segment, the segments of a column exchange them through shared memory
+// (the last known face above the segment, the first known face below it),
+// and each thread writes min(y - above, below - y) for its rows.
+constexpr int kDtSeg = 32;
+__global__ void __launch_bounds__(32 * kDtSeg) k_dt_cols(const uint32_t* __restrict__ mask, int* d, int W, int H) {
+    __shared__ int last_k[kDtSeg][32], first_k[kDtSeg][32];
+    const int cx = threadIdx.x, sg = threadIdx.y;
+    const int x = blockIdx.x * 32 + cx;
+    const int rows = (H + kDtSeg - 1) / kDtSeg;
+    const int y0 = sg * rows, y1 = min(H, y0 + rows);
+    int last = -1, first = -1;
+    if (x < W) {
+        for (int y = y0; y < y1; y++) {
+            if (mask[(size_t)y * W + x] == 0) {
+                if (first < 0) first = y;
+                last = y;
+            }
+        }
     }
-    g = kInf;
-    for (int y = H - 1; y >= 0; y--) {
-        size_t c = (size_t)y * W + x;
-        int v = d[c];
-        g = (g >= kInf) ? v : min(v, g + 1);
-        d[c] = g;
+    last_k[sg][cx] = last;
+    first_k[sg][cx] = first;
+    __syncthreads();
+    if (x >= W) return;
+    int above = -1;   // last known face before this segment
+    for (int k = sg - 1; k >= 0 && above < 0; k--) above = last_k[k][cx];
+    int below = -1;   // first known face after this segment
+    for (int k = sg + 1; k < kDtSeg && below < 0; k++) below = first_k[k][cx];
+    // forward: the last known face at or above y; backward: the first at or below
+    int a = above;
+    for (int y = y0; y < y1; y++) {
+        const size_t c = (size_t)y * W + x;
+        if (mask[c] == 0) a = y;
+        d[c] = a >= 0 ? y - a : kInf;
+    }
+    int bb = below;
+    for (int y = y1 - 1; y >= y0; y--) {
+        const size_t c = (size_t)y * W + x;
+        if (mask[c] == 0) bb = y;
+        if (bb >= 0) d[c] = min(d[c], bb - y);
     }
 }
 
@@ -741,7 +769,7 @@ int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double
         size_t nt = (size_t)tiles_x[gi] * tiles_y[gi];
         int2* tr = x.tile_range + tile_off[gi];
         XLAUNCH(k_tile_init, blocks_for(nt, 256), 256, tr, nt);
-        XLAUNCH(k_dt_cols, blocks_for(W[gi], 128), 128, m[gi], x.dist[gi], W[gi], H[gi]);
+        XLAUNCH(k_dt_cols, (W[gi] + 31) / 32, dim3(32, kDtSeg), m[gi], x.dist[gi], W[gi], H[gi]);
         XLAUNCH(k_dt_rows, H[gi], 1024, x.dist[gi], m[gi], W[gi], H[gi], tr, tiles_x[gi]);
         XLAUNCH(k_tile_max, blocks_for(nt, 256), 256, tr, nt, x.max_layer + gi);
     }
