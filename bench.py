@@ -203,10 +203,31 @@ def cpu_baseline(args, budget_s, max_frames):
     value = args.size * args.size * frames / dt
     info = sim.solver_info()
     sim.close()
+
+    def variant(omp, tol, iters_cap):
+        # one timed frame after one warm-up frame (the reference's own PCG cap of 200 iterations)
+        v = oracle_py.OracleSim(sc, seed=SEED, omp=omp, sl_inplace=0, pcg_tol=tol, pcg_max_iters=iters_cap)
+        v.frame()
+        t = time.perf_counter()
+        v.frame()
+        d = time.perf_counter() - t
+        it = v.solver_info()["iterations"]
+        v.close()
+        return {"value": args.size * args.size / d, "unit": UNIT,
+                "cores": int(os.environ.get("OMP_NUM_THREADS", threads)) if omp else 1,
+                "pcg_tol": tol, "pcg_iterations": it, "s_per_frame": d}
+
+    variants = {}
+    if budget_s > 0:
+        # the serial build (the reference's default configuration, USE_OPENMP off) and the
+        # reference's hard-coded tolerance 1e-12 (OpenMP build)
+        variants["serial_tol_%g" % args.tol] = variant(False, args.tol, 200)
+        variants["openmp_tol_1e-12"] = variant(True, 1e-12, 200)
     return {"value": value, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", threads)), "kind": "port",
             "sample": f"{frames} frame(s) of the same {args.size}^2 workload after 1 warm-up frame, "
                       f"{dt:.1f} s; oracle restatement (C, -O3 -fopenmp, the reference's race-free "
-                      f"OpenMP loops), PCG tol {args.tol:g} (last solve {info['iterations']} iterations)"}
+                      f"OpenMP loops), PCG tol {args.tol:g} (last solve {info['iterations']} iterations)",
+            "variants": variants}
 
 
 def reference_arm(args):
