@@ -427,7 +427,7 @@ int finish(Host* h) {
         if (e & 1) {
             const char* kind = (e & (kWaveKindCp << 4))      ? "closest-point"
                                : (e & (kWaveKindEik << 4))   ? "Eikonal"
-                               : (e & (kWaveKindWave2 << 4)) ? "MIC(0) factor or FP64 MIC(0)"
+                               : (e & (kWaveKindWave2 << 4)) ? "FP64 MIC(0)"
                                : (e & (kWaveKindMic32 << 4)) ? "FP32 MIC(0)"
                                                              : "wavefront";
             const char* what = (e & 256) ? "its neighbour strip" : (e & 512) ? "its own tile loads" : (e & 1024) ? "its other warp" : "a neighbour";

@@ -129,6 +129,7 @@ struct Mic32Item {
 struct Mic32MapsHost {
     alignas(64) unsigned char fwd[4 * 128];
     alignas(64) unsigned char bwd[4 * 128];
+    alignas(64) unsigned char fac[4 * 128];   // the FP32 MIC(0) factor
 };
 
 // TMA descriptors of the closest-point sweeps (see cp_sweep.cuh).

@@ -112,7 +112,19 @@ struct Mic32Args {
     unsigned long long base_host;
     const unsigned long long* base_dev;  // graph-replayed launches: device-memory base (see launch_mic32)
     int* err;
+    float sigma;                         // the factor: MIC(0) safety threshold
 };
+
+// What a sweep computes per cell from its operands v0, v1, v2, the cell on
+// its left (in sweep order) and the cell below:
+//   kM32Solve:  out = v0 - v1 * left - v2 * below   (the triangular solves);
+//   kM32Factor: the FP32 MIC(0) factor pc = 1 / sqrt(e), with v0 = Adiag,
+//               v1 = Ax(i-1,j) (Ax(i-1,j) + tau Ay(i-1,j)), v2 = Ay(i,j-1)
+//               (Ay(i,j-1) + tau Ax(i,j-1)) and e = v0 - v1 left^2 - v2 below^2
+//               (the reference's MIC(0) expression, regrouped), e replaced
+//               by v0 when below sigma v0, and 0 where v0 carries the -0.0
+//               non-fluid marker (also the padding's).
+constexpr int kM32Solve = 0, kM32Factor = 1;
 
 // out = v0 - v1 * left - v2 * below on the cells of sweep order: the forward
 // sweep on q~ = q*pc (v0 = r*pc^2, v1 = fa, v2 = fb), the backward sweep on z
@@ -121,8 +133,9 @@ struct Mic32Args {
 // strips, rounded up to whole clusters, neighbours in a cluster hand their
 // columns over in shared memory; several scenes: a cooperative grid of
 // persistent CTAs, hand-offs through global memory.
-template <bool FWD, bool SEVERAL>
+template <bool FWD, bool SEVERAL, int OP = kM32Solve>
 __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32Maps maps, const Mic32Args a) {
+    static_assert(OP == kM32Solve || FWD, "the factor runs forward");
     if (!SEVERAL && a.skip != nullptr && *a.skip) return;
     const unsigned long long base = a.base_dev != nullptr ? *a.base_dev + a.base_host : a.base_host;
     int* const err = a.err;
@@ -400,12 +413,26 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                         if (lane == 0) left = l0;
                         if (!check || (r >= 0 && r < NR)) {
                             float w[4];
+                            if (OP == kM32Solve) {
 #pragma unroll
-                            for (int m = 0; m < 4; m++) w[m] = fmaf(-m32_get<FWD>(bv, m), o[m], m32_get<FWD>(xv, m));
+                                for (int m = 0; m < 4; m++)
+                                    w[m] = fmaf(-m32_get<FWD>(bv, m), o[m], m32_get<FWD>(xv, m));
 #pragma unroll
-                            for (int m = 0; m < 4; m++) {
-                                o[m] = fmaf(-m32_get<FWD>(av, m), left, w[m]);
-                                left = o[m];
+                                for (int m = 0; m < 4; m++) {
+                                    o[m] = fmaf(-m32_get<FWD>(av, m), left, w[m]);
+                                    left = o[m];
+                                }
+                            } else {
+#pragma unroll
+                                for (int m = 0; m < 4; m++)
+                                    w[m] = fmaf(-(m32_get<FWD>(bv, m) * o[m]), o[m], m32_get<FWD>(xv, m));
+#pragma unroll
+                                for (int m = 0; m < 4; m++) {
+                                    const float ad = m32_get<FWD>(xv, m);
+                                    const float e = fmaf(-(m32_get<FWD>(av, m) * left), left, w[m]);
+                                    o[m] = signbit(ad) ? 0.0f : rsqrtf(e < a.sigma * ad ? ad : e);
+                                    left = o[m];
+                                }
                             }
                             *reinterpret_cast<float4*>(p) = m32_pack<FWD>(o);
                             if (publishes && lane == 31) top_p[r % kM32TopRing] = m32_entry(r, o[3]);
@@ -482,7 +509,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             const int it = *cur_item;
             if (it >= a.nitems) break;
             const Mic32Item item = a.items[it];
-            if (a.scenes[item.scene].inner->done) continue;   // that scene's inner solve stopped
+            if (OP == kM32Solve && a.scenes[item.scene].inner->done) continue;   // that scene's inner solve stopped
             run_strip(item.strip, item.nstrips, item.x0, item.P32, item.y0, item.NY32, item.pidx);
         }
         if (threadIdx.x == 0) {
@@ -525,8 +552,8 @@ struct PackLaunch {
 // graph_sweeps sweeps of one replay, uses the graph's progress counters and
 // the device-memory base plus graph_slot sweeps; slot 0 first advances that
 // base by graph_sweeps, so that every replay gets fresh bases.
-template <bool FWD>
-int launch_mic32(Pack* pk, PackLaunch& L, float* out, int graph_slot = -1, int graph_sweeps = 0) {
+template <bool FWD, int OP = kM32Solve>
+int launch_mic32(Pack* pk, PackLaunch& L, float* out, int graph_slot = -1, int graph_sweeps = 0, float sigma = 0.f) {
     const bool graph = graph_slot >= 0;
     const bool several = pk->n > 1;
     const int nstrips = several ? pk->nitems : pk->scenes[0].P32 / kM32Cols;
@@ -534,7 +561,8 @@ int launch_mic32(Pack* pk, PackLaunch& L, float* out, int graph_slot = -1, int g
         set_error("mic32: %d strips exceed the %d progress counters", nstrips, pk->progress_cap);
         return FS2D_ERR_INVALID;
     }
-    const void* fn = several ? (const void*)mic32_kernel<FWD, true> : (const void*)mic32_kernel<FWD, false>;
+    const void* fn =
+        several ? (const void*)mic32_kernel<FWD, true, OP> : (const void*)mic32_kernel<FWD, false, OP>;
     static std::atomic<unsigned long long> configured[2] = {{0}, {0}};
     if (int rc0 = ensure_smem_attr(configured[several ? 1 : 0], L.device, fn, (int)kM32Smem)) return rc0;
     Mic32Args a{};
@@ -542,12 +570,13 @@ int launch_mic32(Pack* pk, PackLaunch& L, float* out, int graph_slot = -1, int g
     a.pitch = pk->pitch;
     a.P32 = pk->scenes[0].P32;
     a.NY32 = pk->scenes[0].NY32;
-    a.skip = several ? nullptr : &pk->scenes[0].inner->done;
+    a.skip = (several || OP == kM32Factor) ? nullptr : &pk->scenes[0].inner->done;   // every scene needs its factor
     a.items = pk->d_items;
     a.nitems = pk->nitems;
     a.scenes = pk->d_scenes;
     a.work = pk->d_ctl + 2;
     a.err = L.err;
+    a.sigma = sigma;
     if (graph) {
         if (graph_slot == 0) {
             (*L.launches)++;
@@ -562,10 +591,11 @@ int launch_mic32(Pack* pk, PackLaunch& L, float* out, int graph_slot = -1, int g
         a.base_dev = nullptr;
         a.progress = pk->progress;
     }
-    const Mic32Maps& maps = *reinterpret_cast<const Mic32Maps*>(FWD ? pk->maps->fwd : pk->maps->bwd);
+    const Mic32Maps& maps =
+        *reinterpret_cast<const Mic32Maps*>(OP == kM32Factor ? pk->maps->fac : (FWD ? pk->maps->fwd : pk->maps->bwd));
     void* args[] = {(void*)&maps, (void*)&a};
     (*L.launches)++;
-    const char* name = FWD ? "mic32_forward" : "mic32_backward";
+    const char* name = OP == kM32Factor ? "mic32_factor" : (FWD ? "mic32_forward" : "mic32_backward");
     long long kt = L.timer ? ktimer_begin(L.timer, name) : -1;
     cudaError_t e;
     if (several) {

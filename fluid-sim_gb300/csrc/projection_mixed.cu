@@ -11,7 +11,8 @@
 //     preconditioner factor and both triangular solves (strip wavefronts in the
 //     reference's dependency order; the forward solve runs on q~ = q*precon,
 //     so both solves have the form out = v0 - v1*left - v2*below with three
-//     operand arrays, TMA-staged, see mic32_tma.cuh), SpMV and vector updates;
+//     operand arrays, and the factor the form pc = 1/sqrt(v0 - v1*left^2 -
+//     v2*below^2), TMA-staged, see mic32_tma.cuh), SpMV and vector updates;
 //   * inner dot products use exact FP32 products (p + e, e from an FMA),
 //     double-float (FP32 pair) accumulation inside a warp and FP64 across
 //     warps and blocks; norms are maxima (exact in any precision); the
@@ -25,7 +26,6 @@
 #include <vector>
 #include <cudaTypedefs.h>
 #include "fs2d_device.cuh"
-#include "wave2.cuh"
 #include "mic32_tma.cuh"
 
 namespace fs2d {
@@ -75,46 +75,63 @@ __global__ void k_mixed_matrix(const double* __restrict__ A0, const double* __re
     ay[k] = (float)Ay[c];
 }
 
-struct MicFactor32 {
-    static constexpr const char* kName = "wave2_MicFactor32";
-    typedef float T;
-    static constexpr int NA = 5;
-    const float* in[5];  // Adiag(i,j), Ax(i-1,j), Ay(i-1,j), Ay(i,j-1), Ax(i,j-1)
-    float* out;          // precon
-    int pitch;
-    float tau, sigma;
-    __device__ float border(int i, int j) const { return out[(size_t)j * pitch + i]; }
-    __device__ float stored(const float*, float r) const { return r; }
-    __device__ float compute(const float* v, float pl, float pd, int, int) const {
-        const float ad = v[0];
-        if (signbit(ad)) return 0.0f;
-        const float axl = v[1], ayl = v[2], ayd = v[3], axd = v[4];
-        float e = ad - (axl * pl) * (axl * pl) - (ayd * pd) * (ayd * pd) -
-                  tau * (axl * ayl * pl * pl + ayd * axd * pd * pd);
-        if (e < sigma * ad) e = ad;
-        return 1.0f / sqrtf(e);
-    }
-};
-
-// Folded MIC(0) coefficients.  With q~ = q*pc the reference's forward
-// substitution q = (r - Ax(i-1,j)pc(i-1,j)q(i-1,j) - Ay(i,j-1)pc(i,j-1)q(i,j-1))*pc
-// becomes q~ = r*pc^2 - fa*q~(i-1,j) - fb*q~(i,j-1) with fa = Ax(i-1,j)*pc^2,
-// fb = Ay(i,j-1)*pc^2, and the backward substitution
-// z = (q - Ax pc z(i+1,j) - Ay pc z(i,j+1))*pc becomes z = q~ - fc*z(i+1,j) - fd*z(i,j+1)
-// with fc = Ax*pc^2, fd = Ay*pc^2 (pc taken at (i,j)).
-__global__ void k_mixed_coef(const float* __restrict__ ax, const float* __restrict__ ay,
-                             const float* __restrict__ pc, float* fa, float* fb, float* fc, float* fd, int NX, int NY,
-                             int P) {
+// Operands of the FP32 MIC(0) factor sweep (kM32Factor in mic32_tma.cuh),
+// on the reference's loop range (cells 1..NX-1 x 1..NY-1): the left term
+// Ax(i-1,j) (Ax(i-1,j) + tau Ay(i-1,j)) into fa and the lower term
+// Ay(i,j-1) (Ay(i,j-1) + tau Ax(i,j-1)) into fb (both are free until the
+// folded coefficients replace them); 0 on the first row and column.
+__global__ void k_factor_prep(const float* __restrict__ ax, const float* __restrict__ ay, float* fa, float* fb,
+                              float tau, int NX, int NY, int P) {
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     if (c >= (size_t)NX * NY) return;
     int i = (int)(c % NX), j = (int)(c / NX);
     size_t k = (size_t)j * P + i;
-    float p = pc[k];
-    float p2 = p * p;
-    fa[k] = i > 0 ? ax[k - 1] * p2 : 0.0f;
-    fb[k] = j > 0 ? ay[k - P] * p2 : 0.0f;
-    fc[k] = ax[k] * p2;
-    fd[k] = ay[k] * p2;
+    float l = 0.f, d = 0.f;
+    if (i > 0) {
+        const float x = ax[k - 1], y = ay[k - 1];
+        l = x * fmaf(tau, y, x);
+    }
+    if (j > 0) {
+        const float x = ax[k - P], y = ay[k - P];
+        d = y * fmaf(tau, x, y);
+    }
+    fa[k] = l;
+    fb[k] = d;
+}
+
+// Folded MIC(0) coefficients of every scene of a pack (its FP32 blocks).
+// With q~ = q*pc the reference's forward substitution
+// q = (r - Ax(i-1,j)pc(i-1,j)q(i-1,j) - Ay(i,j-1)pc(i,j-1)q(i,j-1))*pc
+// becomes q~ = r*pc^2 - fa*q~(i-1,j) - fb*q~(i,j-1) with fa = Ax(i-1,j)*pc^2,
+// fb = Ay(i,j-1)*pc^2, and the backward substitution
+// z = (q - Ax pc z(i+1,j) - Ay pc z(i,j+1))*pc becomes z = q~ - fc*z(i+1,j) - fd*z(i,j+1)
+// with fc = Ax*pc^2, fd = Ay*pc^2 (pc taken at (i,j)).  Padding cells (pc 0)
+// get zeros.
+__global__ void __launch_bounds__(256) k_mixed_coef(const PackScene* __restrict__ sc, const int* __restrict__ blk,
+                                                    int pitch, const float* __restrict__ ax,
+                                                    const float* __restrict__ ay, const float* __restrict__ pc,
+                                                    float* fa, float* fb, float* fc, float* fd) {
+    const PackScene& S = sc[blk[blockIdx.x]];
+    const int lb = blockIdx.x - S.blk0;
+    const unsigned n = (unsigned)S.P32 * (unsigned)S.NY;
+    for (unsigned c = (unsigned)lb * 256 + threadIdx.x; c < n; c += (unsigned)S.nb32 * 256) {
+        const int j = (int)(c / (unsigned)S.P32), i = (int)(c - (unsigned)j * (unsigned)S.P32);
+        const size_t k = (size_t)S.off + (size_t)j * pitch + i;
+        const float p = pc[k];
+        const float p2 = p * p;
+        fa[k] = i > 0 ? ax[k - 1] * p2 : 0.0f;
+        fb[k] = j > 0 ? ay[k - pitch] * p2 : 0.0f;
+        fc[k] = ax[k] * p2;
+        fd[k] = ay[k] * p2;
+    }
+}
+
+// Every padding cell's Adiag (and the gaps between a batch's scenes) carries
+// the -0.0 non-fluid marker, so the factor sweep leaves pc = 0 there and
+// the SpMV skips them; k_mixed_matrix rewrites the scenes' cells each frame.
+__global__ void k_fill_marker(float* a, size_t n) {
+    size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c < n) a[c] = -0.0f;
 }
 
 // ---- the refinement loop over the scenes of a pack ----
@@ -539,17 +556,21 @@ namespace {
 // Tensor maps of the FP32 MIC(0) sweeps over the pack's arrays.
 int pack_setup_maps(Pack* pk) {
     Mixed32& m = pk->m;
-    Mic32Maps f{}, b{};
+    Mic32Maps f{}, b{}, c{};
     int rc = 0;
     float* fin[3] = {m.rp, m.fa, m.fb};
     float* bin[3] = {m.q, m.fc, m.fd};
+    float* cin[3] = {m.a0, m.fa, m.fb};   // the factor: Adiag and the left / lower terms (prepared in fa, fb)
     for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&f.in[a], fin[a], pk->pitch, pk->rows);
     for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&b.in[a], bin[a], pk->pitch, pk->rows);
+    for (int a = 0; a < 3 && !rc; a++) rc = mic32_make_map(&c.in[a], cin[a], pk->pitch, pk->rows);
     if (!rc) rc = mic32_make_map(&f.out, m.q, pk->pitch, pk->rows);
     if (!rc) rc = mic32_make_map(&b.out, m.z, pk->pitch, pk->rows);
+    if (!rc) rc = mic32_make_map(&c.out, m.pc, pk->pitch, pk->rows);
     if (rc) return rc;
     memcpy(pk->maps->fwd, &f, sizeof(f));
     memcpy(pk->maps->bwd, &b, sizeof(b));
+    memcpy(pk->maps->fac, &c, sizeof(c));
     return 0;
 }
 
@@ -681,7 +702,10 @@ int pack_finish(Pack* pk) {
         set_error("out of host memory");
         return FS2D_ERR_ALLOC;
     }
-    return pack_setup_maps(pk);
+    if (int rcm = pack_setup_maps(pk)) return rcm;
+    const size_t cells = (size_t)pk->pitch * pk->rows;
+    k_fill_marker<<<blocks_for(cells, 256), 256>>>(pk->m.a0, cells);
+    return check_cuda(cudaDeviceSynchronize(), "k_fill_marker");
 }
 
 }  // namespace
@@ -816,13 +840,8 @@ int mixed_setup(Sim* s) {
     const unsigned nb = blocks_for(N, kT);
     Mixed32& m = s->m32;
     FS2D_LAUNCH(s, k_mixed_matrix, nb, kT, 0, s->Adiag, s->Ax, s->Ay, m.a0, m.ax, m.ay, NX, P, N);
-    {
-        MicFactor32 op{{m.a0, m.ax - 1, m.ay - 1, m.ay - P, m.ax - P}, m.pc, P, (float)s->opt.mic_tau,
-                       (float)s->opt.mic_sigma};
-        int rc = launch_wave2<MicFactor32, 2, 16>(s, op, WaveGeom{1, 1, 1, NX - 1, 1, NY - 1}, nullptr);
-        if (rc) return rc;
-    }
-    FS2D_LAUNCH(s, k_mixed_coef, nb, kT, 0, m.ax, m.ay, m.pc, m.fa, m.fb, m.fc, m.fd, NX, NY, P);
+    // the factor itself runs for every scene of the pack at the start of its solve
+    FS2D_LAUNCH(s, k_factor_prep, nb, kT, 0, m.ax, m.ay, m.fa, m.fb, (float)s->opt.mic_tau, NX, NY, P);
     return 0;
 }
 
@@ -905,6 +924,11 @@ static int pack_solve_impl(Pack* pk, const fs2d_options& opt_in, PackLaunch& L) 
     }
     const int max_iters = opt.pcg_max_iters;
     const int batch = 4;
+    // MIC(0) factor of every scene (one forward sweep of the pack), then the
+    // folded coefficients of the triangular solves
+    if (int rcf = launch_mic32<true, kM32Factor>(pk, L, m.pc, -1, 0, (float)opt.mic_sigma)) return rcf;
+    PK_LAUNCH(L, k_mixed_coef, pk->nblk, 256, pk->d_scenes, pk->d_blk, pk->pitch, m.ax, m.ay, m.pc, m.fa, m.fb,
+              m.fc, m.fd);
     FS2D_CUDA(cudaMemsetAsync(pk->d_ctl, 0, 2 * sizeof(int), L.stream));
     PK_LAUNCH(L, k_outer_start, blocks_for(pk->n, 128), 128, pk->d_scenes, pk->n, pk->d_ctl);
     auto poll = [&](int which, int* value) -> int {

@@ -400,7 +400,7 @@ int fs2d_render_export(fs2d_sim* sim, fs2d_render* r);
  * of those kinds withholds its hand-off to the next strip, so that strip's
  * wait runs out (kinds: 1 closest-point sweeps, 2 Eikonal sweeps, 4 FP64
  * MIC(0) factor and solves, counted in blocks of their launch, 8 FP32
- * MIC(0) solves); 0 turns the hold off.  Results of a frame that timed out
+ * MIC(0) factor and solves); 0 turns the hold off.  Results of a frame that timed out
  * are invalid; the handle stays usable. */
 #define FS2D_WAVE_CLOSEST_POINT 1
 #define FS2D_WAVE_EIKONAL       2
