@@ -294,6 +294,7 @@ int alloc_all(Sim* s) {
     A(gbase, 1);
     A(cp_tab, (size_t)s->P + s->NY);
     A(cpc, 1);
+    A(eik_rng, (size_t)s->progress_cap);
     A(cp_hb_t, (size_t)s->progress_cap * s->P);
     A(cp_hb_p, (size_t)s->progress_cap * s->P);
     A(phi_p, (size_t)s->P * s->NY);
@@ -359,7 +360,8 @@ void free_all(Sim* s) {
                     s->m32.pc, s->m32.fa, s->m32.fb, s->m32.fc, s->m32.fd, s->m32.r, s->m32.rp, s->m32.q,
                     s->m32.z, s->m32.w, s->m32.s0, s->m32.s1, s->m32.e, s->pcg32,
                     s->pos_df,
-                    s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p, s->phi_p, s->emask, s->gprogress, s->gbase};
+                    s->cp_tab, s->cpc, s->cp_hb_t, s->cp_hb_p, s->phi_p, s->emask, s->gprogress, s->gbase,
+                    s->eik_rng};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     if (s->pcg_host) cudaFreeHost(s->pcg_host);

@@ -98,6 +98,8 @@ __device__ __forceinline__ bool same_bits(double x, double y) {
 
 struct EkArgs {
     double2* hb;          // strip hand-off rows: [strip][sweep column] = (value, changed)
+    const double* phi;    // the pitched level set the sweep updates (its unchanged columns are read directly)
+    const uint2* rng;     // per strip: the check's column range (null: every strip marches every column)
     unsigned long long* progress;
     unsigned long long base;
     int* err;
@@ -164,7 +166,6 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
   auto run_strip = [&](const EkMaps& maps, const EkArgs& a, const int strip) {
     const int NX = a.NX, NY = a.NY, P = a.P;
     const int nstrips = (NY + kEkRows - 1) / kEkRows;
-    const int nt = P / kEkCols;
     const bool has_next = strip + 1 < nstrips;
     // this strip hands its top row to the next one (unless the test hook holds it back)
     const bool publishes = has_next && !wave_held(a.err, kWaveKindEik, strip);
@@ -175,15 +176,42 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
     const bool prev_local = below_in_grid && crank > 0;        // the previous strip fills this ring
     const bool next_local = publishes && crank + 1 < csize;    // this strip fills the next strip's ring
     const int y0 = SY > 0 ? kEkRows * strip : NY - kEkRows - kEkRows * strip;   // memory row of box row 0
+    // Columns (sweep order) this strip can change: a cell changes only if the
+    // check marked it or an upwind neighbour changed, changes travel right and
+    // up, and cells >= 0 never change, so the strip's changes lie between the
+    // first marked column of this and every earlier strip and its own last
+    // negative column.  The strip marches whole tiles from the one holding
+    // the column before that first column (whose unchanged value is the left
+    // neighbour of the first cell that can change).  Its other columns keep
+    // their values: the successor gets them straight from memory.
+    int A = 0, Bm = P - 1;
+    if (a.rng != nullptr && strip < nstrips) {   // (CTAs past the last strip exist only to round up clusters)
+        unsigned c0 = 0xffffffffu;
+        for (int k = 0; k <= strip; k++) c0 = min(c0, a.rng[k].x);
+        const unsigned lr = a.rng[strip].y;
+        const int last = lr == 0xffffffffu ? -1 : P - 1 - (int)lr;
+        const int first = c0 == 0xffffffffu ? P : (int)c0;
+        if (first <= last) {
+            A = (max(first - 1, 0) / kEkCols) * kEkCols;
+            Bm = last;
+        } else {
+            A = P;   // nothing to march
+            Bm = P - 1;
+        }
+    }
+    const bool march = A <= Bm;
+    const int tA = A / kEkCols;                      // first marched tile
+    const int tB = march ? Bm / kEkCols : tA - 1;    // last marched tile
+    const int jtop = SY > 0 ? y0 + kEkRows - 1 : y0; // memory row of the strip's top row
 
     if (threadIdx.x == 0) {
         for (int k = 0; k < kEkSlots; k++) mbar_init(bars + k, 1);
         fence_mbar_init();
-        *bnd_used = 0;
+        *bnd_used = A / kEkCH;
         *top_done = 0;
         *quit = 0;
-        *tiles_done = 0;
-        *tiles_freed = 0;
+        *tiles_done = tA;
+        *tiles_freed = tA;
     }
     for (int k = threadIdx.x; k < 2 * kEkRing; k += blockDim.x) bnd[k] = ~0ull;      // no column matches
     for (int k = threadIdx.x; k < 2 * kEkTopRing; k += blockDim.x) top[k] = ~0ull;
@@ -192,21 +220,22 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
     if (warp == 1 && active) {
         // ---------------- I/O warp ----------------
         const unsigned long long* gprev = below_in_grid ? a.progress + (strip - 1) : nullptr;
-        int hb = (below_in_grid && !prev_local) ? 0 : P;   // next column of the row below to fetch
+        const int hb_end = march ? Bm + 1 : 0;            // the row below is needed on the marched columns
+        int hb = (below_in_grid && !prev_local && march) ? A : hb_end;   // next column of the row below to fetch
         int tc = 0;                                        // top-row columns forwarded
         const int tend = publishes ? P : 0;
         int rused = 0;                                     // last seen chunk position of the consumer
         const unsigned r_bnd = next_local ? mapa_shared((const void*)bnd, crank + 1) : 0u;
         const unsigned r_used = next_local ? mapa_shared((const void*)bnd_used, crank + 1) : 0u;
-        int ts = 0;
+        int ts = tA;
         unsigned long long gavail = 0;
         long long idle = 0;
-        while (hb < P || tc < tend || ts < nt) {
+        while (hb < hb_end || tc < tend || ts <= tB) {
             bool moved = false;
             // row below from global memory (the previous strip is in another cluster)
             const int hb_lim = (*bnd_used + kEkRingChunks - 2) * kEkCH;   // slots consumed two chunks ago
-            if (hb < P && hb < hb_lim) {
-                const int n = min(min(32, P - hb), hb_lim - hb);
+            if (hb < hb_end && hb < hb_lim) {
+                const int n = min(min(32, hb_end - hb), hb_lim - hb);
                 const unsigned long long need = a.base + (unsigned long long)(hb + n);
                 if (gavail < need) {
                     unsigned long long v = 0;
@@ -233,8 +262,14 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                 const int c = tc + lane;
                 unsigned long long w0 = 0ull, w1 = 0ull;
                 if (c < P) {
-                    w0 = top[2 * (c % kEkTopRing)];
-                    w1 = top[2 * (c % kEkTopRing) + 1];
+                    if (c < A || c > Bm) {   // not marched: the unchanged value in memory
+                        const double v = a.phi[(size_t)jtop * P + (SX > 0 ? c : P - 1 - c)];
+                        w0 = ek_w0(c, v);
+                        w1 = ek_w1(c, v, false);
+                    } else {
+                        w0 = top[2 * (c % kEkTopRing)];
+                        w1 = top[2 * (c % kEkTopRing) + 1];
+                    }
                 }
                 const bool ok = c >= P || (ek_w0_is(w0, c) && ek_w1_is(w1, c));
                 const unsigned bad = __ballot_sync(0xffffffffu, !ok);
@@ -269,7 +304,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                 }
                 if (n < 32) break;
             }
-            if (ts < nt && *tiles_done > ts) {
+            if (ts <= tB && *tiles_done > ts) {
                 if (lane == 0) {
                     const double* src = tiles + (size_t)(ts % kEkSlots) * (kEkCols * kEkRows);
                     const int x = SX > 0 ? ts * kEkCols : P - (ts + 1) * kEkCols;
@@ -311,7 +346,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         auto tile_x = [&](int t) { return SX > 0 ? t * kEkCols : P - (t + 1) * kEkCols; };
         auto bc_of = [&](int c) { return SX > 0 ? (c & 31) : 31 - (c & 31); };
         auto issue = [&](int t) {
-            if (lane == 0 && t < nt) {
+            if (lane == 0 && t <= tB) {
                 unsigned long long* bar = bars + (t % kEkSlots);
                 mbar_expect_tx(bar, kEkTileBytes + kEkMaskBytes);
                 tma_load_2d(tiles + (size_t)(t % kEkSlots) * (kEkCols * kEkRows), &maps.ld, tile_x(t), y0, bar);
@@ -321,7 +356,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         bool failed = false;
         auto wait_tile = [&](int t) {
             unsigned long long* bar = bars + (t % kEkSlots);
-            const unsigned parity = (unsigned)((t / kEkSlots) & 1);
+            const unsigned parity = (unsigned)(((t - tA) / kEkSlots) & 1);   // slot phases count from tile tA
             long long polls = 0;
             while (!mbar_try_wait(bar, parity)) {
                 if (++polls > kWaveSpinLimit) {
@@ -348,7 +383,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         const unsigned long long* bnd_p = const_cast<const unsigned long long*>(bnd);
         unsigned long long* top_p = const_cast<unsigned long long*>(top);
 
-        for (int t = 0; t < kEkAhead; t++) issue(t);
+        for (int t = tA; t < tA + kEkAhead; t++) issue(t);
 
         double o_v = 0.0;     // output of the previous step (the left value)
         bool o_c = false;     // ... and whether the sweep changed it
@@ -360,12 +395,12 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
             for (int u = 0; u < kEkCols; u++) {
                 const int s = t * kEkCols + u;
                 const int c = s - lane;
-                if (below_in_grid && (u % kEkCH) == 0 && s < P) {
+                if (below_in_grid && (u % kEkCH) == 0 && s >= A && s <= Bm) {
                     // lane 0 enters a chunk of the row below: every word of it
                     // must have arrived (one word per lane, one vote)
                     const int cc = s + (lane & (kEkCH - 1));
                     const int wi = 2 * (cc % kEkRing) + (lane >> 4);
-                    bool ok = cc >= P || ((lane >> 4) ? ek_w1_is(bnd_p[wi], cc) : ek_w0_is(bnd_p[wi], cc));
+                    bool ok = cc > Bm || ((lane >> 4) ? ek_w1_is(bnd_p[wi], cc) : ek_w0_is(bnd_p[wi], cc));
                     if (!__all_sync(0xffffffffu, ok)) {
                         long long polls = 0;
                         while (!ok && !failed) {
@@ -381,7 +416,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                     __syncwarp();   // lane 0 reads the words its neighbours validated
                     if (lane == 0) *bnd_used = s / kEkCH;
                 }
-                if (below_in_grid && (!check || s < P)) {
+                if (below_in_grid && (!check || (s >= A && s <= Bm))) {
                     bw0 = bnd_p[2 * (s % kEkRing)];
                     bw1 = bnd_p[2 * (s % kEkRing) + 1];
                 }
@@ -391,7 +426,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                     b_v = below_in_grid ? ek_value(bw0, bw1) : 0.0;
                     b_c = below_in_grid && ek_changed(bw1);
                 }
-                const bool cin = !check || (c >= 0 && c < P);
+                const bool cin = !check || (c >= A && c <= Bm);
                 const int i = SX > 0 ? c : P - 1 - c;
                 double own = 0.0;
                 double* cell = nullptr;
@@ -422,31 +457,31 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
             }
         };
 
-        const int nsteps = P + 31;
-        for (int t = 0; t * kEkCols < nsteps; t++) {
-            if (t < nt) wait_tile(t);
+        const int tEnd = march ? (Bm + 31) / kEkCols : tA - 1;   // the last lane ends 31 columns behind
+        for (int t = tA; t <= tEnd; t++) {
+            if (t <= tB) wait_tile(t);
             if (publishes && t * kEkCols - 31 - *top_done > kEkTopRing / 2)
                 spin_ge(top_done, t * kEkCols - 31 - kEkTopRing / 2);
             __syncwarp();
-            if (t == 0 || t >= nt)
+            if (t == tA || t >= tB)
                 tile_steps(t, BoolTag<true>{});
             else
                 tile_steps(t, BoolTag<false>{});
-            if (t >= 1 && t - 1 < nt) {
+            if (t >= tA + 1 && t - 1 <= tB) {
                 fence_async_smem();
                 __syncwarp();
                 if (lane == 0) *tiles_done = t;
             }
             const int nx = t + kEkAhead;
-            if (nx < nt) {
-                if (nx >= kEkSlots && *tiles_freed < nx - kEkSlots + 1) spin_ge(tiles_freed, nx - kEkSlots + 1);
+            if (nx <= tB) {
+                if (nx - tA >= kEkSlots && *tiles_freed < nx - kEkSlots + 1) spin_ge(tiles_freed, nx - kEkSlots + 1);
                 __syncwarp();
                 issue(nx);
             }
         }
         __syncwarp();
         if (lane == 0) {
-            *tiles_done = nt;
+            *tiles_done = tB + 1;
             if (below_in_grid) *bnd_used = P / kEkCH + kEkRingChunks;
         }
         (void)failed;
@@ -473,6 +508,7 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
         const EkScene* sc = scenes + item.scene;
         EkArgs a = sc->a;
         a.progress = w.progress + (item.pidx - item.strip);
+        a.rng = w.rng != nullptr ? w.rng + (item.pidx - item.strip) : nullptr;
         a.base = w.base;
         a.err = w.err;
         a.skip = nullptr;

@@ -192,6 +192,7 @@ struct WaveWork {
     unsigned long long base;
     int* err;
     const int* skip;                     // per scene
+    const uint2* rng;                    // Eikonal sweeps: per strip (counter order), its column range
 };
 
 }  // namespace fs2d

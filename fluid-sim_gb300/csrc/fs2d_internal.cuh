@@ -210,6 +210,7 @@ struct Sim {
     float4* pos_df = nullptr;         // float-pair particle positions (np_cap)
     float2* cp_tab = nullptr;         // float-pair corner coordinates: P columns, then NY rows
     CpConst* cpc = nullptr;           // constants of the FP32 closest-point decision
+    uint2* eik_rng = nullptr;         // per strip: column range of the current Eikonal sweep (see k_eik_check)
     int* cp_hb_t = nullptr;           // closest-point strip hand-off rows (progress_cap x P)
     float4* cp_hb_p = nullptr;
     CpMapsHost* cpmaps = nullptr;

@@ -223,12 +223,55 @@ __device__ __forceinline__ bool eik_check_cell(const double* __restrict__ phi, u
     mask[c] = ch ? 1 : 0;
     return ch;
 }
-__global__ void k_eik_check(const double* __restrict__ phi, uint8_t* mask, int NX, int NY, int P, int i_lo,
-                            int i_hi, int j_lo, int j_hi, int sx, int sy, double dx, int* noop) {
+// Range of an Eikonal sweep strip (rows of one 32-row strip in sweep order):
+// x = the first sweep column whose cell the check marked, y = P - 1 - the last
+// sweep column holding a negative cell the sweep may update (both 0xffffffff
+// when there is none).  One row per block: a block minimum, then one atomic.
+__device__ __forceinline__ void eik_range_add(uint2* rng, int strip, unsigned first_marked, unsigned last_neg_rev) {
+    __shared__ unsigned sm[2][4];
+    const unsigned fm = __reduce_min_sync(0xffffffffu, first_marked);
+    const unsigned ln = __reduce_min_sync(0xffffffffu, last_neg_rev);
+    const int wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        sm[0][wid] = fm;
+        sm[1][wid] = ln;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned a = 0xffffffffu, b = 0xffffffffu;
+        for (int k = 0; k < nw; k++) {
+            a = min(a, sm[0][k]);
+            b = min(b, sm[1][k]);
+        }
+        if (a != 0xffffffffu) atomicMin(&rng[strip].x, a);
+        if (b != 0xffffffffu) atomicMin(&rng[strip].y, b);
+    }
+}
+
+// The range terms of cell (i, j) for eik_range_add (i >= NX: none).
+__device__ __forceinline__ void eik_range_terms(const double* __restrict__ phi, bool marked, int NX, int P, int i_lo,
+                                                int i_hi, int j_lo, int j_hi, int sx, int i, int j, unsigned& fm,
+                                                unsigned& ln) {
+    fm = ln = 0xffffffffu;
+    if (i >= NX || i < i_lo || i > i_hi || j < j_lo || j > j_hi) return;
+    const unsigned c = (unsigned)(sx > 0 ? i : P - 1 - i);   // sweep column
+    if (marked) fm = c;
+    if (phi[(size_t)j * P + i] < 0) ln = (unsigned)(P - 1) - c;
+}
+
+__global__ void __launch_bounds__(128) k_eik_check(const double* __restrict__ phi, uint8_t* mask, int NX, int NY,
+                                                   int P, int i_lo, int i_hi, int j_lo, int j_hi, int sx, int sy,
+                                                   double dx, int* noop, uint2* rng) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     int j = blockIdx.y;
-    if (i >= NX) return;
-    if (eik_check_cell(phi, mask, P, i_lo, i_hi, j_lo, j_hi, sx, sy, dx, i, j)) *noop = 0;
+    bool marked = false;
+    if (i < NX) {
+        marked = eik_check_cell(phi, mask, P, i_lo, i_hi, j_lo, j_hi, sx, sy, dx, i, j);
+        if (marked) *noop = 0;
+    }
+    unsigned fm, ln;
+    eik_range_terms(phi, marked, NX, P, i_lo, i_hi, j_lo, j_hi, sx, i, j, fm, ln);
+    eik_range_add(rng, (sy > 0 ? j : NY - 1 - j) / 32, fm, ln);
 }
 
 // Min-smoothing pass (src/FluidSim2D.cpp:904-919): Jacobi, interior cells.
@@ -366,6 +409,8 @@ static int launch_eik_sweep_dir(Sim* s, const WaveGeom& g, const int* skip) {
     if (int rc0 = ensure_smem_attr(configured, s->device, (const void*)eik_sweep_kernel<SX, SY, false>, (int)kEkSmem)) return rc0;
     EkArgs a;
     a.hb = reinterpret_cast<double2*>(s->cp_hb_p);
+    a.phi = s->phi_p;
+    a.rng = s->eik_rng;
     a.progress = s->progress;
     a.base = wave_begin(s);
     a.err = s->err;
@@ -512,8 +557,9 @@ int levelset_create(Sim* s) {
             int i_lo = sx > 0 ? 1 : 0, i_hi = sx > 0 ? NX - 1 : NX - 2;
             int j_lo = sy > 0 ? 1 : 0, j_hi = sy > 0 ? NY - 1 : NY - 2;
             FS2D_CUDA(cudaMemsetAsync(noop, 0xff, sizeof(int), s->stream));
+            FS2D_CUDA(cudaMemsetAsync(s->eik_rng, 0xff, (size_t)((NY + 31) / 32) * sizeof(uint2), s->stream));
             FS2D_LAUNCH(s, k_eik_check, g2, 128, 0, s->phi_p, s->emask, NX, NY, P, i_lo, i_hi, j_lo, j_hi, sx, sy,
-                        s->dx, noop);
+                        s->dx, noop, s->eik_rng);
             WaveGeom g{sx, sy, i_lo, i_hi, j_lo, j_hi};
             if ((rc = launch_eik_sweep(s, g, noop))) return rc;
         }
@@ -540,7 +586,7 @@ struct LsCells {
     size_t np;
     int NX, NY, P;
     int blk0, gx;
-    int unused;   // no padding: the host compares tables byte by byte
+    int pidx0;    // the scene's first strip in the work list's counters (also no padding: tables are compared byte by byte)
     double dx, dr;
 };
 
@@ -578,14 +624,20 @@ __global__ void k_surface_all(const LsCells* __restrict__ sc, const int* __restr
     surface_cell(S.phi, S.phi_p, S.NX, S.NY, S.P, i, j);
 }
 
-__global__ void k_eik_check_all(const LsCells* __restrict__ sc, const int* __restrict__ blk, int sx, int sy,
-                                int* noop) {
+__global__ void __launch_bounds__(128) k_eik_check_all(const LsCells* __restrict__ sc, const int* __restrict__ blk,
+                                                       int sx, int sy, int* noop, uint2* rng) {
     int k, i, j;
     const LsCells& S = ls_cell(sc, blk, k, i, j);
-    if (i >= S.NX) return;
     const int i_lo = sx > 0 ? 1 : 0, i_hi = sx > 0 ? S.NX - 1 : S.NX - 2;
     const int j_lo = sy > 0 ? 1 : 0, j_hi = sy > 0 ? S.NY - 1 : S.NY - 2;
-    if (eik_check_cell(S.phi_p, S.emask, S.P, i_lo, i_hi, j_lo, j_hi, sx, sy, S.dx, i, j)) noop[k] = 0;
+    bool marked = false;
+    if (i < S.NX) {
+        marked = eik_check_cell(S.phi_p, S.emask, S.P, i_lo, i_hi, j_lo, j_hi, sx, sy, S.dx, i, j);
+        if (marked) noop[k] = 0;
+    }
+    unsigned fm, ln;
+    eik_range_terms(S.phi_p, marked, S.NX, S.P, i_lo, i_hi, j_lo, j_hi, sx, i, j, fm, ln);
+    eik_range_add(rng, S.pidx0 + (sy > 0 ? j : S.NY - 1 - j) / 32, fm, ln);
 }
 
 template <typename T>
@@ -597,6 +649,7 @@ int ls_alloc(T** p, size_t n) {
 
 struct LsBatch {
     std::vector<Sim*> sims;
+    std::vector<int> first;      // per scene: its first strip's counter (progress, ranges)
     std::vector<CpScene> cp;     // host copies of the device tables
     std::vector<EkScene> ek;
     std::vector<LsCells> cells;
@@ -608,6 +661,7 @@ struct LsBatch {
     WaveItem* d_items = nullptr;
     int nitems = 0;
     int* d_noop = nullptr;               // per scene: nonzero = no cell would change in this sweep
+    uint2* d_rng = nullptr;              // per strip (counter order): the Eikonal sweep's column range
     int* d_work = nullptr;               // persistent-CTA counters of the cp and Eikonal sweeps
     unsigned long long* progress = nullptr;
     unsigned long long launch = 0;       // progress base of the next sweep
@@ -616,7 +670,7 @@ struct LsBatch {
 
 void ls_batch_free(LsBatch* b) {
     if (!b) return;
-    void* ptrs[] = {b->d_cp, b->d_ek, b->d_cells, b->d_blk, b->d_items, b->d_noop, b->d_work, b->progress};
+    void* ptrs[] = {b->d_cp, b->d_ek, b->d_cells, b->d_blk, b->d_items, b->d_noop, b->d_work, b->progress, b->d_rng};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete b;
@@ -652,6 +706,7 @@ static int ls_batch_refresh(LsBatch* b, cudaStream_t stream) {
         a.dr = s->dr;
         EkArgs& e = ek[k].a;
         e.hb = reinterpret_cast<double2*>(s->cp_hb_p);
+        e.phi = s->phi_p;
         e.NX = s->NX;
         e.NY = s->NY;
         e.P = s->P;
@@ -659,7 +714,7 @@ static int ls_batch_refresh(LsBatch* b, cudaStream_t stream) {
         e.c2 = 2 * s->dx * s->dx;
         LsCells& c = cells[k];
         c = LsCells{s->t, s->pos_df, s->pos, s->cp_tab, s->cp_tab + s->P, s->cpc, s->phi, s->phi_p, s->emask,
-                    s->np, s->NX, s->NY, s->P, blk, (s->NX + 127) / 128, 0, s->dx, s->dr};
+                    s->np, s->NX, s->NY, s->P, blk, (s->NX + 127) / 128, b->first[k], s->dx, s->dr};
         blk += c.gx * s->NY;
     }
     if (memcmp((const void*)cp.data(), (const void*)b->cp.data(), n * sizeof(CpScene)) != 0 ||
@@ -697,7 +752,9 @@ LsBatch* ls_batch_create(Sim* const* sims, int n, int device, int* rc_out) {
     // first: a strip's rank is (strips after it) x the strip-to-strip lag
     // (~45 column steps measured) + its own steps; progress counters are
     // numbered scene by scene
-    std::vector<int> blk, first(n);
+    std::vector<int> blk;
+    std::vector<int>& first = b->first;
+    first.assign(n, 0);
     int pidx = 0;
     for (int k = 0; k < n; k++) {
         const Sim* s = sims[k];
@@ -725,6 +782,7 @@ LsBatch* ls_batch_create(Sim* const* sims, int n, int device, int* rc_out) {
     if (!rc) rc = ls_alloc(&b->d_noop, n);
     if (!rc) rc = ls_alloc(&b->d_work, 4);
     if (!rc) rc = ls_alloc(&b->progress, items.size());
+    if (!rc) rc = ls_alloc(&b->d_rng, items.size());
     if (!rc && ((uintptr_t)b->d_cp % alignof(CpScene) != 0 || (uintptr_t)b->d_ek % alignof(EkScene) != 0)) {
         set_error("level-set batch: the tensor map tables are not aligned");
         rc = FS2D_ERR_CUDA;
@@ -777,7 +835,8 @@ LsBatch* ls_batch_create(Sim* const* sims, int n, int device, int* rc_out) {
 
 template <int SX, int SY>
 static int ls_launch_cp(LsBatch* b, cudaStream_t stream, int* err) {
-    WaveWork w{b->d_cp, b->d_items, b->nitems, b->d_work, b->progress, (++b->launch) << 24, err, b->d_noop};
+    WaveWork w{b->d_cp, b->d_items, b->nitems, b->d_work, b->progress, (++b->launch) << 24, err, b->d_noop,
+               nullptr};
     CpMaps m{};
     CpArgs a{};
     void* args[] = {(void*)&m, (void*)&a, (void*)&w};
@@ -788,7 +847,8 @@ static int ls_launch_cp(LsBatch* b, cudaStream_t stream, int* err) {
 
 template <int SX, int SY>
 static int ls_launch_ek(LsBatch* b, cudaStream_t stream, int* err) {
-    WaveWork w{b->d_ek, b->d_items, b->nitems, b->d_work + 2, b->progress, (++b->launch) << 24, err, b->d_noop};
+    WaveWork w{b->d_ek, b->d_items, b->nitems, b->d_work + 2, b->progress, (++b->launch) << 24, err, b->d_noop,
+               b->d_rng};
     EkMaps m{};
     EkArgs a{};
     void* args[] = {(void*)&m, (void*)&a, (void*)&w};
@@ -828,7 +888,8 @@ int ls_batch_sweeps(LsBatch* b, cudaStream_t stream, int* err, unsigned long lon
         for (int d = 0; d < 4; d++) {
             const int sx = kDirs[d][0], sy = kDirs[d][1];
             FS2D_CUDA(cudaMemsetAsync(b->d_noop, 0xff, n * sizeof(int), stream));
-            k_eik_check_all<<<nblk, 128, 0, stream>>>(b->d_cells, b->d_blk, sx, sy, b->d_noop);
+            FS2D_CUDA(cudaMemsetAsync(b->d_rng, 0xff, (size_t)b->nitems * sizeof(uint2), stream));
+            k_eik_check_all<<<nblk, 128, 0, stream>>>(b->d_cells, b->d_blk, sx, sy, b->d_noop, b->d_rng);
             if ((rc = check_cuda(cudaGetLastError(), "k_eik_check_all"))) return rc;
             rc = sx > 0 ? (sy > 0 ? ls_launch_ek<1, 1>(b, stream, err) : ls_launch_ek<1, -1>(b, stream, err))
                         : (sy > 0 ? ls_launch_ek<-1, 1>(b, stream, err) : ls_launch_ek<-1, -1>(b, stream, err));
