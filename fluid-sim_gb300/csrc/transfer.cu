@@ -470,7 +470,8 @@ __global__ void k_tile_max(const int2* __restrict__ tr, size_t n, unsigned int* 
 // tile's band needs the previous band of the tile and of its eight
 // neighbours (the halo), whose items come earlier in the list and were taken
 // earlier by running CTAs, so every wait makes progress whatever the grid
-// size and whatever else runs on the GPU.
+// size and whatever else runs on the GPU.  Only items of bands a tile works
+// in wait or report (done[t] = 1 + the last working band finished).
 struct ExtrapJob {
     double* a[2];
     const uint32_t* layer[2];
@@ -541,20 +542,32 @@ __global__ void __launch_bounds__(256) k_extrap_bands(const ExtrapJob job) {
         const unsigned int hi_u = min(lo_u + kBand - 1, depth[g]);
         const int2 tr = job.tile_range[g][t];
         const bool work = lo_u <= depth[g] && tr.y >= (int)lo_u && tr.x <= (int)hi_u;
-        // wait: the tile's own previous band, and with work also the
-        // neighbours' (thread k < 9 watches tile (tx + k % 3 - 1, ty + k / 3 - 1))
+        // A tile works only in the bands its layer range [tr.x, tr.y] (up to
+        // the depth) spans; an item without work neither waits nor reports.
+        // A working item needs, of itself and each neighbour (the halo), every
+        // working band before its own: it waits until that tile's done count
+        // covers min(band - 1, its last working band), when that is one of its
+        // working bands (thread k < 9 watches tile (tx + k % 3 - 1, ty + k / 3 - 1)).
+        if (!work) continue;
         if (band > 0 && threadIdx.x < 9) {
             const int nx = tx + (int)(threadIdx.x % 3) - 1, ny = ty + (int)(threadIdx.x / 3) - 1;
-            const bool watch = (threadIdx.x == 4 || work) && nx >= 0 && ny >= 0 && nx < job.tiles_x[g] &&
-                               ny < job.tiles_y[g];
-            if (watch) {
-                const int* d = job.done + (g ? job.ntiles[0] : 0) + ny * job.tiles_x[g] + nx;
-                long long polls = 0;
-                while (ld_acquire_int(d) < band) {
-                    if (++polls > job.spin) {
-                        atomicOr(job.err, 8);
-                        failed_sh = 1;
-                        break;
+            if (nx >= 0 && ny >= 0 && nx < job.tiles_x[g] && ny < job.tiles_y[g]) {
+                const int n = ny * job.tiles_x[g] + nx;
+                const int2 trn = job.tile_range[g][n];
+                const int top = min(trn.y, (int)depth[g]);   // the neighbour's last layer to fill
+                if (trn.y >= 1 && trn.x <= top) {
+                    const int b_lo = (trn.x - 1) / kBand, b_hi = (top - 1) / kBand;
+                    const int need = min(band - 1, b_hi);
+                    if (need >= b_lo) {
+                        const int* d = job.done + (g ? job.ntiles[0] : 0) + n;
+                        long long polls = 0;
+                        while (ld_acquire_int(d) < need + 1) {
+                            if (++polls > job.spin) {
+                                atomicOr(job.err, 8);
+                                failed_sh = 1;
+                                break;
+                            }
+                        }
                     }
                 }
             }
