@@ -17,9 +17,10 @@
 //     step and the result one 128-bit store;
 //   * operand tiles of 128 columns x 32 rows come into shared memory by the
 //     Tensor Memory Accelerator (cp.async.bulk.tensor, completion on an
-//     mbarrier) two tiles ahead, into a ring of four tiles per operand array;
-//     results overwrite operand 0 and each finished tile leaves by a TMA
-//     store;
+//     mbarrier), into a ring of four tiles per operand array; results
+//     overwrite operand 0 and each finished tile leaves by a TMA store, after
+//     which the next tile's loads go into its ring tile (up to three tiles
+//     ahead of the computing front);
 //   * strips hand their last column to the next strip.  The grid is launched
 //     as clusters of up to 8 CTAs: inside a cluster the column goes straight
 //     into the next strip's shared ring (distributed shared memory), across
@@ -27,9 +28,10 @@
 //     (st.release / ld.acquire).  Every ring entry carries its row in the same
 //     64-bit word as its value, so an entry is valid exactly when its tag
 //     matches and no flag or fence orders the two.  A second warp per CTA
-//     does all of that traffic and the tile stores, so the compute warp only
-//     touches its own shared memory and issues the tile loads.  All CTAs of a
-//     cluster meet at a cluster barrier before any of them exits.
+//     does all of that traffic and issues every tile load and store, so the
+//     compute warp only touches its own shared memory and waits on the tiles'
+//     mbarriers.  All CTAs of a cluster meet at a cluster barrier before any
+//     of them exits.
 // The arrays are padded to whole strips and tiles (pitch a multiple of 128
 // columns, rows a multiple of 32) and the recurrence runs over the whole
 // padded grid: cells outside the reference's loop ranges (border rows and
@@ -56,7 +58,7 @@ constexpr int kM32Rows = 32;                         // rows per tile (row-count
 constexpr int kM32Slots = 4;                         // tiles in each operand's ring
 constexpr int kM32RingRows = kM32Slots * kM32Rows;
 constexpr int kM32NA = 3;                            // operand arrays per sweep
-constexpr int kM32CH = 16;                           // rows per arrival check of the left column
+constexpr int kM32CH = 32;                           // rows per arrival check of the left column (one per tile)
 constexpr int kM32BndChunks = 16;
 constexpr int kM32BndRing = kM32BndChunks * kM32CH;  // ring of the left column, rows
 constexpr int kM32TopRing = 256;                     // ring of the strip's last column, rows
@@ -64,7 +66,7 @@ constexpr int kM32TileFloats = kM32Cols * kM32Rows;
 constexpr unsigned kM32TileBytes = kM32TileFloats * 4;
 constexpr int kM32ArrayFloats = kM32RingRows * kM32Cols;
 constexpr size_t kM32Smem =
-    (size_t)kM32NA * kM32ArrayFloats * 4 + (kM32BndRing + kM32TopRing) * 8 + 8 * 4 + 8 * kM32Slots;
+    (size_t)kM32NA * kM32ArrayFloats * 4 + (kM32BndRing + kM32TopRing) * 8 + 16 * 4 + 8 * kM32Slots;
 
 // Tensor maps of one sweep: operands in[0..2] (results are written over
 // in[0]'s tile in shared memory) and the output; box 128 x 32.
@@ -152,25 +154,34 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
     volatile int* top_done = ctr + 1;       // rows of the last column forwarded by the I/O warp
     volatile int* quit = ctr + 2;           // compute warp gave up (timeout)
     volatile int* tiles_done = ctr + 3;     // tiles whose results are complete in shared memory
-    volatile int* tiles_freed = ctr + 4;    // tiles whose TMA store has finished reading shared memory
+    volatile int* tiles_issued = ctr + 4;   // tiles whose loads the I/O warp has issued
     volatile int* cur_item = ctr + 5;       // several scenes: the CTA's current work item
-    unsigned long long* bars = reinterpret_cast<unsigned long long*>(const_cast<int*>(ctr) + 8);
+    // loads issued into each ring tile since the launch (kept across work items):
+    // load number m of ring tile k completes phase m of mbarrier k
+    volatile int* slot_loads = ctr + 8;
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(const_cast<int*>(ctr) + 16);
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const long long spin = wave_spin(err);
     const unsigned crank = SEVERAL ? 0u : cluster_ctarank(), csize = SEVERAL ? 1u : cluster_nctarank();
-    // completed phases of each slot's mbarrier (compute warp), kept across work items
-    unsigned phases[kM32Slots] = {0u, 0u, 0u, 0u};
-
     if (threadIdx.x == 0) {
-        for (int k = 0; k < kM32Slots; k++) mbar_init(bars + k, 1);
+        for (int k = 0; k < kM32Slots; k++) {
+            mbar_init(bars + k, 1);
+            slot_loads[k] = 0;
+        }
         fence_mbar_init();
     }
+    // bit k: parity of the first load of ring tile k in the next strip
+    auto slot_parities = [&]() {
+        unsigned b = 0;
+        for (int k = 0; k < kM32Slots; k++) b |= (unsigned)(slot_loads[k] & 1) << k;
+        return b;
+    };
 
     // One strip of one scene: `strip` of `nstrips`, the scene's padded region
     // at pack column x0, row y0, P32 x NR; progress counter `pidx` (the previous
-    // strip's is pidx - 1).
-    auto run_strip = [&](int strip, int nstrips, int x0, int P32, int y0, int NR, int pidx) {
+    // strip's is pidx - 1); pbits: slot_parities() before the strip.
+    auto run_strip = [&](int strip, int nstrips, int x0, int P32, int y0, int NR, int pidx, unsigned pbits) {
         const int nt = NR / kM32Rows;                           // tiles per strip
         const bool has_next = strip + 1 < nstrips;
         // this strip hands its last column to the next one (unless the test hook holds it back)
@@ -194,10 +205,11 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             const unsigned r_bnd = next_local ? mapa_shared((const void*)bnd, crank + 1) : 0u;
             const unsigned r_used = next_local ? mapa_shared((const void*)bnd_used, crank + 1) : 0u;
             int ts = 0;                                        // next tile to store
-            int confirmed = 0;                                 // stored tiles whose slots are released
+            int rd = 0;                                        // stores that have read their ring tiles
+            int tl = 0;                                        // next tile to load
             unsigned long long gavail = 0;
             long long idle = 0;
-            while (hb < NR || tc < tend || ts < nt) {
+            while (hb < NR || tc < tend || ts < nt || tl < nt) {
                 bool moved = false;
                 // left column from global memory (the previous strip is in another cluster)
                 const int hb_lim = (*bnd_used + kM32BndChunks - 2) * kM32CH;   // slots consumed two chunks ago
@@ -257,71 +269,94 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 if (ts < nt && *tiles_done > ts) {
                     // results of tile ts are complete (the compute warp fenced them
                     // for the async proxy before publishing tiles_done).  The warp
-                    // does not wait for this store to read its tile: once every
-                    // store but the newest has read its tile, tiles < ts are free
-                    // (the compute warp reuses a slot two tiles after its store)
+                    // does not wait for this store to read its tile, only for the
+                    // stores before it
                     if (lane == 0) {
                         tma_store_2d(&maps.out, xbox, tile_y(ts), ring + (size_t)(ts & (kM32Slots - 1)) * kM32TileFloats);
                         bulk_commit();
                         bulk_wait_read<1>();
-                        *tiles_freed = ts;
                     }
                     __syncwarp();
                     ts++;
+                    rd = ts - 1;
+                    moved = true;
+                }
+                // operand tiles in: tile tl goes into the ring tile of tile
+                // tl - kM32Slots, free once that tile's store has read it (the
+                // store went out after the compute warp finished the tile)
+                while (tl < nt && tl - kM32Slots < rd) {
+                    if (lane == 0) {
+                        const int k = tl & (kM32Slots - 1);
+                        mbar_expect_tx(bars + k, kM32NA * kM32TileBytes);
+                        float* dst = ring + (size_t)k * kM32TileFloats;
+#pragma unroll
+                        for (int q = 0; q < kM32NA; q++)
+                            tma_load_2d(dst + (size_t)q * kM32ArrayFloats, &maps.in[q], xbox, tile_y(tl), bars + k);
+                        *tiles_issued = tl + 1;
+                    }
+                    __syncwarp();
+                    tl++;
                     moved = true;
                 }
                 if (moved) {
                     idle = 0;
-                } else if (confirmed < ts) {
+                } else if (rd < ts) {
                     // nothing else to do: wait for the newest store to read its
-                    // tile and release its slot now, so the compute warp finds it
-                    // free instead of waiting for the next store
-                    if (lane == 0) {
-                        bulk_wait_read<0>();
-                        *tiles_freed = ts;
-                    }
+                    // tile, so that the next load into its ring tile goes out now
+                    if (lane == 0) bulk_wait_read<0>();
                     __syncwarp();
-                    confirmed = ts;
+                    rd = ts;
                 } else if (++idle > 16 * spin || *quit || ((idle & 1023) == 0 && wave_failed(err))) {
-                    if (lane == 0) atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
+                    if (lane == 0) {
+                        atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
+                        *quit = 1;
+                    }
                     break;
                 }
             }
-            if (lane == 0) bulk_wait_all();
+            if (lane == 0) {
+                bulk_wait_all();
+                // no load may still be writing into the ring when the CTA moves on or
+                // exits: wait (bounded) for the newest load of every ring tile, then
+                // count this strip's loads
+                for (int k = 0; k < kM32Slots; k++) {
+                    const int n = tl > k ? (tl - 1 - k) / kM32Slots + 1 : 0;
+                    if (n > 0) {
+                        const unsigned par = (unsigned)(slot_loads[k] + n - 1) & 1u;
+                        long long polls = 0;
+                        while (!mbar_try_wait(bars + k, par) && ++polls <= kWaveSpinLimit) {
+                        }
+                    }
+                    slot_loads[k] += n;
+                }
+            }
             __syncwarp();
         } else {
             // ---------------- compute warp ----------------
             bool failed = false;
-            int issued = 0;         // tiles whose loads were issued (none after a failure)
-            int unconfirmed = nt;   // first tile whose wait gave up
-            auto issue = [&](int t) {
-                if (t < nt && !failed) {
-                    if (lane == 0) {
-                        unsigned long long* bar = bars + (t & (kM32Slots - 1));
-                        mbar_expect_tx(bar, kM32NA * kM32TileBytes);
-                        float* dst = ring + (size_t)(t & (kM32Slots - 1)) * kM32TileFloats;
-#pragma unroll
-                        for (int k = 0; k < kM32NA; k++)
-                            tma_load_2d(dst + (size_t)k * kM32ArrayFloats, &maps.in[k], xbox, tile_y(t), bar);
-                    }
-                    issued = t + 1;
-                }
-            };
-            // slot phases: tile t of this strip is load number phases[slot] of its slot
-            auto poll_tile = [&](int t) -> bool {
-                const int k = t & (kM32Slots - 1);
-                long long polls = 0;
-                while (!mbar_try_wait(bars + k, phases[k] & 1u))
-                    if (++polls > kWaveSpinLimit) return false;
-                phases[k]++;
-                return true;
-            };
+            // tile t of this strip is the (t / kM32Slots)-th load of its ring tile
+            // in this strip, issued by the I/O warp
             auto wait_tile = [&](int t) {
-                if (t >= issued) return;
-                if (!poll_tile(t)) {
-                    failed = true;
-                    atomicOr(err, kWaitTile | (kWaveKindMic32 << 4));
-                    unconfirmed = min(unconfirmed, t);
+                if (failed) return;   // after one timeout the results are invalid: do not wait again
+                long long polls = 0;
+                while (*tiles_issued <= t) {
+                    if (++polls > 16 * spin || *quit) {
+                        failed = true;
+                        atomicOr(err, kWaitWarp | (kWaveKindMic32 << 4));
+                        *quit = 1;
+                        return;
+                    }
+                }
+                const int k = t & (kM32Slots - 1);
+                const unsigned par = ((pbits >> k) ^ (unsigned)(t / kM32Slots)) & 1u;
+                polls = 0;
+                while (!mbar_try_wait(bars + k, par)) {
+                    if (++polls > kWaveSpinLimit) {
+                        failed = true;
+                        atomicOr(err, kWaitTile | (kWaveKindMic32 << 4));
+                        *quit = 1;
+                        return;
+                    }
                 }
             };
             auto spin_ge = [&](volatile int* flag, int need) {  // bounded wait on an I/O-warp counter
@@ -336,8 +371,6 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                     }
                 }
             };
-            issue(0);
-            issue(1);
 
             // the lane's float4 in every ring row: box columns 4l .. 4l+3 (the
             // backward sweep's box is mirrored: its sweep column 4l is box column
@@ -370,8 +403,9 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                     const int r0 = t * kM32Rows - lane;
                     load_next(cell_ptr(r0 < 0 ? 0 : r0));
                 }
-                // one chunk of the left column per group: a rolled loop over the
-                // tile's two chunks with each chunk's steps unrolled
+                // the left column arrives in chunks of kM32CH rows (one per tile):
+                // a rolled loop over the tile's chunks with each chunk's steps
+                // unrolled
 #pragma unroll 1
                 for (int g = 0; g < kM32Rows; g += kM32CH) {
 #pragma unroll
@@ -453,17 +487,11 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 else
                     tile_steps(t, BoolTag<false>{});
                 // tile t-1 is finished for every lane: hand it to the I/O warp for its
-                // TMA store; the slot of tile t-2 is reused for tile t+2 once that
-                // tile's store has read it
+                // TMA store (after which its ring tile takes the loads of tile t+3)
                 if (t >= 1 && t - 1 < nt) {
                     fence_async_smem();
                     __syncwarp();
                     if (lane == 0) *tiles_done = t;
-                }
-                if (t + 2 < nt) {
-                    if (t >= 2 && *tiles_freed < t - 1) spin_ge(tiles_freed, t - 1);
-                    __syncwarp();
-                    issue(t + 2);
                 }
             }
             __syncwarp();
@@ -471,10 +499,6 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 *tiles_done = nt;
                 if (left_in_grid) *bnd_used = NR / kM32CH + kM32BndChunks;
             }
-            // a tile whose wait gave up may still be arriving: wait for it (and the
-            // tiles issued after it) once more, so no copy into this CTA's shared
-            // memory is in flight when it moves on or exits
-            for (int t = unconfirmed; t < issued; t++) (void)poll_tile(t);
         }
     };
     // rings and counters of a strip: no row matches, nothing done
@@ -484,7 +508,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             *top_done = 0;
             *quit = 0;
             *tiles_done = 0;
-            *tiles_freed = 0;
+            *tiles_issued = 0;
         }
         for (int k = threadIdx.x; k < kM32BndRing; k += blockDim.x) bnd[k] = ~0ull;
         for (int k = threadIdx.x; k < kM32TopRing; k += blockDim.x) top[k] = ~0ull;
@@ -495,7 +519,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
         const int nstrips = a.P32 / kM32Cols;
         reset_rings();
         cluster_sync_all();   // every ring and counter of the cluster is initialised
-        if (strip < nstrips) run_strip(strip, nstrips, 0, a.P32, 0, a.NY32, strip);   // the grid is rounded up to whole clusters
+        if (strip < nstrips) run_strip(strip, nstrips, 0, a.P32, 0, a.NY32, strip, 0u);   // the grid is rounded up to whole clusters
         cluster_sync_all();   // no CTA leaves while a neighbour may still touch its shared memory
     } else {
         // persistent: items are taken in list order and a strip's previous strip
@@ -505,12 +529,14 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             __syncthreads();   // the previous item is finished by both warps
             if (threadIdx.x == 0) *cur_item = atomicAdd(&a.work[0], 1);
             reset_rings();
+            // the previous item's loads are counted and this item's not yet issued
+            const unsigned pbits = slot_parities();
             __syncthreads();
             const int it = *cur_item;
             if (it >= a.nitems) break;
             const Mic32Item item = a.items[it];
             if (OP == kM32Solve && a.scenes[item.scene].inner->done) continue;   // that scene's inner solve stopped
-            run_strip(item.strip, item.nstrips, item.x0, item.P32, item.y0, item.NY32, item.pidx);
+            run_strip(item.strip, item.nstrips, item.x0, item.P32, item.y0, item.NY32, item.pidx, pbits);
         }
         if (threadIdx.x == 0) {
             __threadfence();
