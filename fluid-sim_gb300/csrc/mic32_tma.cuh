@@ -396,13 +396,11 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
 
             // One tile group of 32 steps.  CHECK: some lane's row may lie outside
             // [0, NR) (first and last groups); a compile-time flag, so that the
-            // steady-state groups carry no per-step range tests.
+            // steady-state groups carry no per-step range tests (and the checking
+            // groups only selects and predicated stores).
             auto tile_steps = [&](int t, auto check_tag) {
                 constexpr bool check = decltype(check_tag)::value;
-                {
-                    const int r0 = t * kM32Rows - lane;
-                    load_next(cell_ptr(r0 < 0 ? 0 : r0));
-                }
+                load_next(cell_ptr(t * kM32Rows - lane));
                 // the left column arrives in chunks of kM32CH rows (one per tile):
                 // a rolled loop over the tile's chunks with each chunk's steps
                 // unrolled
@@ -437,15 +435,20 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                             if (lane == 0) *bnd_used = s / kM32CH;
                         }
                         const float4 xv = x_n, av = a_n, bv = b_n;
-                        float* const p = cell_ptr(r < 0 ? 0 : r);
+                        // a row outside [0, NR) (first and last groups) is computed on
+                        // whatever its ring row holds (the index wraps inside the ring),
+                        // kept at 0 and not stored, so that no branch surrounds the step;
+                        // it only feeds rows outside [0, NR) of the lanes to its right
+                        const bool valid = !check || (r >= 0 && r < NR);
+                        float* const p = cell_ptr(r);
                         // next step's operands (row r + 1), loaded before this step's store
-                        if (!check || (r + 1 >= 0 && r + 1 < NR)) load_next(cell_ptr(r + 1 < 0 ? 0 : r + 1));
+                        load_next(cell_ptr(r + 1));
                         float left = __shfl_up_sync(0xffffffffu, o[3], 1);
                         const float l0 = left_in_grid ? m32_entry_value(bn) : 0.0f;
                         // next step's entry (same chunk; a new chunk is read after its check)
                         if (u8 + 1 != kM32CH) bn = bnd_p[(s + 1) % kM32BndRing];
                         if (lane == 0) left = l0;
-                        if (!check || (r >= 0 && r < NR)) {
+                        {
                             float w[4];
                             if (OP == kM32Solve) {
 #pragma unroll
@@ -468,8 +471,12 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                                     left = o[m];
                                 }
                             }
-                            *reinterpret_cast<float4*>(p) = m32_pack<FWD>(o);
-                            if (publishes && lane == 31) top_p[r % kM32TopRing] = m32_entry(r, o[3]);
+                            if (check) {
+#pragma unroll
+                                for (int m = 0; m < 4; m++) o[m] = valid ? o[m] : 0.0f;
+                            }
+                            if (valid) *reinterpret_cast<float4*>(p) = m32_pack<FWD>(o);
+                            if (publishes && lane == 31 && valid) top_p[r % kM32TopRing] = m32_entry(r, o[3]);
                         }
                     }
                 }
