@@ -402,14 +402,21 @@ __global__ void __launch_bounds__(64) eik_sweep_kernel(const __grid_constant__ E
                     const int wi = 2 * (cc % kEkRing) + (lane >> 4);
                     bool ok = cc > Bm || ((lane >> 4) ? ek_w1_is(bnd_p[wi], cc) : ek_w0_is(bnd_p[wi], cc));
                     if (!__all_sync(0xffffffffu, ok)) {
+                        // the whole warp polls in step until every word is there (lanes
+                        // leaving a polling loop one by one would leave the warp diverged
+                        // for the steps after it)
                         long long polls = 0;
-                        while (!ok && !failed) {
+                        while (!failed) {
                             const unsigned long long w = bnd[wi];
-                            ok = (lane >> 4) ? ek_w1_is(w, cc) : ek_w0_is(w, cc);
-                            if (!ok && (++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(a.err)))) {
+                            ok = cc > Bm || ((lane >> 4) ? ek_w1_is(w, cc) : ek_w0_is(w, cc));
+                            if (__all_sync(0xffffffffu, ok)) break;
+                            const bool give_up = ++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(a.err));
+                            if (__any_sync(0xffffffffu, give_up)) {
                                 failed = true;
-                                atomicOr(a.err, kWaitStrip | (kWaveKindEik << 4));
-                                *quit = 1;
+                                if (lane == 0) {
+                                    atomicOr(a.err, kWaitStrip | (kWaveKindEik << 4));
+                                    *quit = 1;
+                                }
                             }
                         }
                     }

@@ -416,13 +416,21 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                             const int rr = s + (lane & (kM32CH - 1));
                             bool ok = rr >= NR || m32_entry_is(bnd_p[rr % kM32BndRing], rr);
                             if (!__all_sync(0xffffffffu, ok)) {
+                                // the whole warp polls in step until every entry is there:
+                                // lanes leaving a polling loop one by one would leave the warp
+                                // diverged for the steps after it (measured: a group of steps
+                                // five times as long)
                                 long long polls = 0;
-                                while (!ok && !failed) {
-                                    ok = m32_entry_is(bnd[rr % kM32BndRing], rr);
-                                    if (!ok && (++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(err)))) {
+                                while (!failed) {
+                                    ok = rr >= NR || m32_entry_is(bnd[rr % kM32BndRing], rr);
+                                    if (__all_sync(0xffffffffu, ok)) break;
+                                    const bool give_up = ++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(err));
+                                    if (__any_sync(0xffffffffu, give_up)) {
                                         failed = true;
-                                        atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
-                                        *quit = 1;
+                                        if (lane == 0) {
+                                            atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
+                                            *quit = 1;
+                                        }
                                     }
                                 }
                             }
