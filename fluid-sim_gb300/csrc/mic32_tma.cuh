@@ -58,13 +58,17 @@ constexpr int kM32Rows = 32;                         // rows per tile (row-count
 constexpr int kM32Slots = 4;                         // tiles in each operand's ring
 constexpr int kM32RingRows = kM32Slots * kM32Rows;
 constexpr int kM32NA = 3;                            // operand arrays per sweep
-constexpr int kM32CH = 32;                           // rows per arrival check of the left column (one per tile)
+constexpr int kM32CH = kM32Rows;                     // rows per arrival check of the left column (one per tile)
+constexpr int kM32Unroll = 32;                       // steps per unrolled body of a tile's step loop
 constexpr int kM32BndChunks = 16;
 constexpr int kM32BndRing = kM32BndChunks * kM32CH;  // ring of the left column, rows
 constexpr int kM32TopRing = 256;                     // ring of the strip's last column, rows
 constexpr int kM32TileFloats = kM32Cols * kM32Rows;
 constexpr unsigned kM32TileBytes = kM32TileFloats * 4;
 constexpr int kM32ArrayFloats = kM32RingRows * kM32Cols;
+static_assert((kM32BndRing & (kM32BndRing - 1)) == 0 && (kM32TopRing & (kM32TopRing - 1)) == 0 &&
+                  (kM32Slots & (kM32Slots - 1)) == 0,
+              "ring sizes are powers of two (indices are masked)");
 constexpr size_t kM32Smem =
     (size_t)kM32NA * kM32ArrayFloats * 4 + (kM32BndRing + kM32TopRing) * 8 + 16 * 4 + 8 * kM32Slots;
 
@@ -154,7 +158,6 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
     volatile int* top_done = ctr + 1;       // rows of the last column forwarded by the I/O warp
     volatile int* quit = ctr + 2;           // compute warp gave up (timeout)
     volatile int* tiles_done = ctr + 3;     // tiles whose results are complete in shared memory
-    volatile int* tiles_issued = ctr + 4;   // tiles whose loads the I/O warp has issued
     volatile int* cur_item = ctr + 5;       // several scenes: the CTA's current work item
     // loads issued into each ring tile since the launch (kept across work items):
     // load number m of ring tile k completes phase m of mbarrier k
@@ -226,7 +229,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                         __syncwarp();   // lane 0's acquire orders the reads below
                         const int r = hb + lane;
                         if (lane < avail)
-                            bnd[r % kM32BndRing] = m32_entry(r, __ldcg(out + (size_t)mrow(r) * pitch + xprev));
+                            bnd[r & (kM32BndRing - 1)] = m32_entry(r, __ldcg(out + (size_t)mrow(r) * pitch + xprev));
                         __syncwarp();
                         hb += avail;
                         moved = true;
@@ -236,7 +239,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                 // memory, every complete run of up to 128 rows at once
                 for (int rep = 0; rep < 4 && tc < tend; rep++) {
                     const int r = tc + lane;
-                    const unsigned long long e = r < NR ? top[r % kM32TopRing] : 0ull;
+                    const unsigned long long e = r < NR ? top[r & (kM32TopRing - 1)] : 0ull;
                     const bool ok = r >= NR || m32_entry_is(e, r);
                     const unsigned bad = __ballot_sync(0xffffffffu, !ok);
                     int n = bad ? __ffs(bad) - 1 : 32;
@@ -252,7 +255,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                     }
                     if (n > 0) {
                         if (next_local) {
-                            if (lane < n) st_cluster_u64(r_bnd + 8u * (unsigned)(r % kM32BndRing), e);
+                            if (lane < n) st_cluster_u64(r_bnd + 8u * (unsigned)(r & (kM32BndRing - 1)), e);
                             __syncwarp();
                         } else {
                             if (lane < n) out[(size_t)mrow(r) * pitch + xlast] = m32_entry_value(e);
@@ -292,7 +295,6 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
 #pragma unroll
                         for (int q = 0; q < kM32NA; q++)
                             tma_load_2d(dst + (size_t)q * kM32ArrayFloats, &maps.in[q], xbox, tile_y(tl), bars + k);
-                        *tiles_issued = tl + 1;
                     }
                     __syncwarp();
                     tl++;
@@ -335,23 +337,15 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             // ---------------- compute warp ----------------
             bool failed = false;
             // tile t of this strip is the (t / kM32Slots)-th load of its ring tile
-            // in this strip, issued by the I/O warp
+            // in this strip, issued by the I/O warp once the ring tile is free (the
+            // mbarrier's phase cannot complete before)
             auto wait_tile = [&](int t) {
                 if (failed) return;   // after one timeout the results are invalid: do not wait again
-                long long polls = 0;
-                while (*tiles_issued <= t) {
-                    if (++polls > 16 * spin || *quit) {
-                        failed = true;
-                        atomicOr(err, kWaitWarp | (kWaveKindMic32 << 4));
-                        *quit = 1;
-                        return;
-                    }
-                }
                 const int k = t & (kM32Slots - 1);
                 const unsigned par = ((pbits >> k) ^ (unsigned)(t / kM32Slots)) & 1u;
-                polls = 0;
+                long long polls = 0;
                 while (!mbar_try_wait(bars + k, par)) {
-                    if (++polls > kWaveSpinLimit) {
+                    if (++polls > kWaveSpinLimit || ((polls & 1023) == 0 && *quit)) {
                         failed = true;
                         atomicOr(err, kWaitTile | (kWaveKindMic32 << 4));
                         *quit = 1;
@@ -400,48 +394,45 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             // groups only selects and predicated stores).
             auto tile_steps = [&](int t, auto check_tag) {
                 constexpr bool check = decltype(check_tag)::value;
-                load_next(cell_ptr(t * kM32Rows - lane));
-                // the left column arrives in chunks of kM32CH rows (one per tile):
-                // a rolled loop over the tile's chunks with each chunk's steps
-                // unrolled
-#pragma unroll 1
-                for (int g = 0; g < kM32Rows; g += kM32CH) {
-#pragma unroll
-                    for (int u8 = 0; u8 < kM32CH; u8++) {
-                        const int s = t * kM32Rows + g + u8;
-                        const int r = s - lane;
-                        if (left_in_grid && u8 == 0 && (!check || s < NR)) {
-                            // lane 0 enters a chunk of the left column: every row
-                            // of it must have arrived (one entry per lane, one vote)
-                            const int rr = s + (lane & (kM32CH - 1));
-                            bool ok = rr >= NR || m32_entry_is(bnd_p[rr % kM32BndRing], rr);
-                            if (!__all_sync(0xffffffffu, ok)) {
-                                // the whole warp polls in step until every entry is there:
-                                // lanes leaving a polling loop one by one would leave the warp
-                                // diverged for the steps after it (measured: a group of steps
-                                // five times as long)
-                                long long polls = 0;
-                                while (!failed) {
-                                    ok = rr >= NR || m32_entry_is(bnd[rr % kM32BndRing], rr);
-                                    if (__all_sync(0xffffffffu, ok)) break;
-                                    const bool give_up = ++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(err));
-                                    if (__any_sync(0xffffffffu, give_up)) {
-                                        failed = true;
-                                        if (lane == 0) {
-                                            atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
-                                            *quit = 1;
-                                        }
-                                    }
+                const int s0 = t * kM32Rows;
+                load_next(cell_ptr(s0 - lane));
+                if (left_in_grid && (!check || s0 < NR)) {
+                    // lane 0 enters the tile's chunk of the left column: every row of
+                    // it must have arrived (one entry per lane, one vote)
+                    const int rr = s0 + lane;
+                    bool ok = rr >= NR || m32_entry_is(bnd_p[rr & (kM32BndRing - 1)], rr);
+                    if (!__all_sync(0xffffffffu, ok)) {
+                        // the whole warp polls in step until every entry is there:
+                        // lanes leaving a polling loop one by one would leave the warp
+                        // diverged for the steps after it (measured: a group of steps
+                        // five times as long)
+                        long long polls = 0;
+                        while (!failed) {
+                            ok = rr >= NR || m32_entry_is(bnd[rr & (kM32BndRing - 1)], rr);
+                            if (__all_sync(0xffffffffu, ok)) break;
+                            const bool give_up = ++polls > 16 * spin || ((polls & 1023) == 0 && wave_failed(err));
+                            if (__any_sync(0xffffffffu, give_up)) {
+                                failed = true;
+                                if (lane == 0) {
+                                    atomicOr(err, kWaitStrip | (kWaveKindMic32 << 4));
+                                    *quit = 1;
                                 }
                             }
-                            __syncwarp();   // lane 0 reads the entries its neighbours validated
-                            bn = bnd_p[s % kM32BndRing];
-                            // earlier chunks are read: their slots may be refilled (a
-                            // plain store suffices, every value read from them was
-                            // consumed by arithmetic before this store issues, and a
-                            // refill lands at least two chunks behind it)
-                            if (lane == 0) *bnd_used = s / kM32CH;
                         }
+                    }
+                    __syncwarp();   // lane 0 reads the entries its neighbours validated
+                    bn = bnd_p[s0 & (kM32BndRing - 1)];
+                    // earlier chunks are read: their slots may be refilled (a plain
+                    // store suffices, every value read from them was consumed by
+                    // arithmetic before this store issues, and a refill lands at
+                    // least two chunks behind it)
+                    if (lane == 0) *bnd_used = s0 / kM32CH;
+                }
+#pragma unroll kM32Unroll
+                for (int u = 0; u < kM32Rows; u++) {
+                    {
+                        const int s = s0 + u;
+                        const int r = s - lane;
                         const float4 xv = x_n, av = a_n, bv = b_n;
                         // a row outside [0, NR) (first and last groups) is computed on
                         // whatever its ring row holds (the index wraps inside the ring),
@@ -453,8 +444,9 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                         load_next(cell_ptr(r + 1));
                         float left = __shfl_up_sync(0xffffffffu, o[3], 1);
                         const float l0 = left_in_grid ? m32_entry_value(bn) : 0.0f;
-                        // next step's entry (same chunk; a new chunk is read after its check)
-                        if (u8 + 1 != kM32CH) bn = bnd_p[(s + 1) % kM32BndRing];
+                        // next step's entry (after the tile's last step a stale one: the
+                        // next tile reads its first entry again after its check)
+                        bn = bnd_p[(s + 1) & (kM32BndRing - 1)];
                         if (lane == 0) left = l0;
                         {
                             float w[4];
@@ -484,7 +476,7 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
                                 for (int m = 0; m < 4; m++) o[m] = valid ? o[m] : 0.0f;
                             }
                             if (valid) *reinterpret_cast<float4*>(p) = m32_pack<FWD>(o);
-                            if (publishes && lane == 31 && valid) top_p[r % kM32TopRing] = m32_entry(r, o[3]);
+                            if (publishes && lane == 31 && valid) top_p[r & (kM32TopRing - 1)] = m32_entry(r, o[3]);
                         }
                     }
                 }
@@ -523,7 +515,6 @@ __global__ void __launch_bounds__(64) mic32_kernel(const __grid_constant__ Mic32
             *top_done = 0;
             *quit = 0;
             *tiles_done = 0;
-            *tiles_issued = 0;
         }
         for (int k = threadIdx.x; k < kM32BndRing; k += blockDim.x) bnd[k] = ~0ull;
         for (int k = threadIdx.x; k < kM32TopRing; k += blockDim.x) top[k] = ~0ull;
