@@ -57,6 +57,11 @@ constexpr int kCpR = 16;           // gather ring slots per row (power of two > 
 // the strip-to-strip lag (measured at 1024^2: 16 and 8 columns gave 9.8 and
 // 8.9 ms of sweeps per frame, 4 columns no better than 8).
 constexpr int kCpCH = 8;
+// steps per unrolled body of a tile's step loop: one chunk of the row below
+// for a scene per launch (the chunk check then falls on the body's first
+// step); half of that in the persistent launches over many small scenes
+template <bool SEVERAL>
+__host__ __device__ constexpr int cp_unroll() { return SEVERAL ? kCpCH / 2 : kCpCH; }
 constexpr int kCpBndChunks = 128 / kCpCH;
 constexpr int kCpTopRing = 256;
 constexpr int kCpTileInts = kCpBoxRows * kCpCols;
@@ -270,6 +275,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
 
   // One strip of one scene (the whole grid of a launch per scene, or one
   // work item of a launch over several scenes).
+  constexpr int kCpUnroll = cp_unroll<SEVERAL>();
   auto run_strip = [&](const CpMaps& maps, const CpArgs& a, const int strip) {
     const int NX = a.NX, NY = a.NY, P = a.P;
     const int nstrips = (NY + 31) / 32;
@@ -446,11 +452,16 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
     };
     // gathers of step s: the particle position of column s - lane + kCpD of
     // the lane's row (lane 31 also of the row above the strip)
+    // (every lane copies, zero-filled where its cell has no particle or lies
+    // outside the strip, so that no branch surrounds the gather; a ring slot
+    // is only read for a cell with a particle)
     auto gather = [&](int s) {
         const int g = s - lane + kCpD;
-        if (rowvalid && g >= 0 && g < P) {
-            const int e = at(g, brow);
-            if (e >= 0 && e < a.np) cp_async16(gring + lane * kCpR + (g & (kCpR - 1)), a.pos_df + e);
+        const bool in = rowvalid && g >= 0 && g < P;
+        const int e = at(in ? g : 0, brow);   // a word of the tile ring either way
+        const bool has = in && e >= 0 && e < a.np;
+        cp_async16_zfill(gring + lane * kCpR + (g & (kCpR - 1)), a.pos_df + (has ? e : 0), has ? 16u : 0u);
+        if (in) {
             if (lane == 31) {
                 const int e2 = at(g, urow);
                 if (e2 >= 0 && e2 < a.np) cp_async16(gring + 32 * kCpR + (g & (kCpR - 1)), a.pos_df + e2);
@@ -469,7 +480,7 @@ __global__ void __launch_bounds__(64) cp_sweep_kernel(const __grid_constant__ Cp
 
     auto tile_steps = [&](int t, auto check_tag) {
         constexpr bool check = decltype(check_tag)::value;
-#pragma unroll 4
+#pragma unroll kCpUnroll
         for (int u = 0; u < kCpCols; u++) {
             const int s = t * kCpCols + u;
             const int c = s - lane;
