@@ -33,6 +33,8 @@ Besides the headline keys the line carries:
   batch           256 dam breaks of uneven sizes advanced together (split
                   over the ranks when N > 1);
   batch_adjoint   the rollouts of 32 closed boxes of uneven sizes;
+  grid3d          the 3D container kernels (include/fs3d.h) on a 512^3 MAC
+                  grid against the HBM copy peak;
   e2e             the headline through the C ABI with host buffers;
   cpu_baseline    the CPU oracle port timed on the host's cores.
 Each extra line has a flag that switches it off (e.g. --adjoint-size 0).
@@ -80,6 +82,92 @@ KERNEL_BYTES_PER_CELL = {"mic32": 16, "mic32_forward": 16, "mic32_backward": 16,
 DOMINANT = tuple(KERNEL_BYTES_PER_CELL)
 
 
+def bench_grid3d(n, local, peak, reps=5):
+    """The 3D containers of include/fs3d.h (the reference's Array3D and
+    MACGrid3D methods) on an n^3 MAC grid and n^3 arrays of N(0,1) doubles:
+    each kernel timed with CUDA events on its stream after one untimed
+    launch, mean of `reps`; every array is larger than the L2 cache.
+    Algorithmic bytes (each array element read or written once): velDiv
+    32 B per cell (u, v, w in, div out), vel 48 B per cell (vec3d out),
+    velU 48 B per u face, setMultiplyAdd and += 24 B per element,
+    innerProduct 16 B, infiniteNorm 8 B; velInterp (all three components)
+    at n^3/8 random points is reported in points/s.  GB300's FP64 rate
+    bounds several of them, so each entry also gives the FP64 instructions
+    per unit (velDiv 5 additions, vel 3, velU 6 in the interior, the halving
+    and quartering being exact integer exponent steps; setMultiplyAdd 2, +=
+    1, innerProduct 1 fused multiply-add, infiniteNorm 0: integer compares)
+    and the FP64 rate they imply."""
+    import ctypes as C
+    import torch
+    import fs2d
+
+    lib = fs2d.load()
+    dev = f"cuda:{local}"
+    gen = torch.Generator(device=dev).manual_seed(7)
+    f64 = dict(dtype=torch.float64, device=dev)
+    A = fs2d.Array3D
+    u = torch.randn((n, n, n + 1), generator=gen, **f64)
+    v = torch.randn((n, n + 1, n), generator=gen, **f64)
+    w = torch.randn((n + 1, n, n), generator=gen, **f64)
+    mac = fs2d.MACGrid3D(A(u.data_ptr(), n + 1, n, n), A(v.data_ptr(), n, n + 1, n), A(w.data_ptr(), n, n, n + 1),
+                         n, n, n)
+    cells = n ** 3
+    x, y = torch.randn(cells, generator=gen, **f64), torch.randn(cells, generator=gen, **f64)
+    out1 = torch.empty(cells, **f64)
+    out3 = torch.empty(3 * (n + 1) * n * n, **f64)
+    npts = cells // 8
+    pts = torch.rand((npts, 3), generator=gen, **f64) * n
+    pout = torch.empty(3 * npts, **f64)
+    ax, ay, ao = (A(t.data_ptr(), n, n, n) for t in (x, y, out1))
+    res = C.c_double()
+    stream = torch.cuda.Stream()
+    sp = C.c_void_p(stream.cuda_stream)
+    faces = (n + 1) * n * n
+    # name: (call, algorithmic bytes, FP64 instructions)
+    calls = {
+        "velDiv": (lambda: lib.fs3d_mac_vel_div(C.byref(mac), C.c_void_p(out1.data_ptr()), sp), 32 * cells,
+                   5 * cells),
+        "vel": (lambda: lib.fs3d_mac_vel(C.byref(mac), C.c_void_p(out3.data_ptr()), sp), 48 * cells, 3 * cells),
+        "velU": (lambda: lib.fs3d_mac_face_vel(C.byref(mac), 0, C.c_void_p(out3.data_ptr()), sp), 48 * faces,
+                 6 * faces),
+        "setMultiplyAdd": (lambda: lib.fs3d_set_multiply_add(C.byref(ao), C.byref(ax), 0.5, C.byref(ay), sp),
+                           24 * cells, 2 * cells),
+        "add": (lambda: lib.fs3d_add(C.byref(ao), C.byref(ay), sp), 24 * cells, cells),
+        "innerProduct": (lambda: lib.fs3d_inner_product(C.byref(ax), C.byref(ay), C.byref(res), sp), 16 * cells,
+                         cells),
+        "infiniteNorm": (lambda: lib.fs3d_infinite_norm(C.byref(ax), C.byref(res), sp), 8 * cells, 0),
+        "velInterp": (lambda: lib.fs3d_mac_vel_interp(C.byref(mac), 3, C.c_void_p(pts.data_ptr()), npts,
+                                                      C.c_void_p(pout.data_ptr()), sp), None, None),
+    }
+    out = {"grid": [n, n, n], "points": npts, "peak_gbs": peak,
+           "timing": "CUDA events on the call's stream, one untimed call first, mean of %d; every array larger than "
+                     "the L2 cache; innerProduct and infiniteNorm include the copy of the scalar to the host" % reps}
+    torch.cuda.synchronize()
+    for name, (fn, nbytes, fp64) in calls.items():
+        rc = fn()
+        if rc != 0:
+            raise RuntimeError(f"fs3d {name}: {lib.fs2d_last_error().decode()}")
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            rc = fn()
+            if rc != 0:
+                raise RuntimeError(f"fs3d {name}: {lib.fs2d_last_error().decode()}")
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        entry = {"ms": round(ms, 4)}
+        if nbytes:
+            gbs = nbytes / (ms * 1e-3) / 1e9
+            entry.update(gbs=round(gbs, 1), frac=round(gbs / peak, 4),
+                         fp64_tops=round(fp64 / (ms * 1e-3) / 1e12, 3))
+        else:
+            entry["points_per_s"] = npts / (ms * 1e-3)
+        out[name] = entry
+    return out
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -99,6 +187,7 @@ def parse():
     ap.add_argument("--sl-steps", type=int, default=10, help="steps of the semi-Lagrangian 1024^2 variant (0: skip)")
     ap.add_argument("--batch-adjoint-steps", type=int, default=16)
     ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--grid3d-size", type=int, default=512, help="3D container kernels on an n^3 MAC grid (0: skip)")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-baseline sampling")
     ap.add_argument("--no-oracle-error", action="store_true",
@@ -753,6 +842,18 @@ def main():
                                    "pair"}
         ba.close()
 
+    # ---- the 3D containers (include/fs3d.h) ----
+    grid3d = None
+    if args.grid3d_size > 0 and rank == 0:
+        try:
+            peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"])
+        except (OSError, ValueError, KeyError):
+            peak = 6800.0
+        try:
+            grid3d = bench_grid3d(args.grid3d_size, local, peak)
+        except RuntimeError as e:   # reported in the line, not a failed headline
+            grid3d = {"error": str(e)}
+
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -767,6 +868,7 @@ def main():
         "adjoint": adjoint,
         "batch": batch,
         "batch_adjoint": batch_adjoint,
+        "grid3d": grid3d,
         "gpu_launches": launches,
         "clocks": clk,
         "roofline": roofline,

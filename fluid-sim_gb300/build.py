@@ -34,6 +34,7 @@ UNITS = {
     "render.cu": ["--fmad=false"],
     "adjoint.cu": ["--fmad=false"],
     "batch.cu": [],
+    "grid3d.cu": ["--fmad=false"],
 }
 
 
@@ -46,7 +47,7 @@ def nvcc():
 
 def _headers():
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))] + \
-        [os.path.join(ROOT, "include", "fs2d.h")]
+        [os.path.join(ROOT, "include", h) for h in ("fs2d.h", "fs3d.h")]
 
 
 def _stale(out, deps):

@@ -67,7 +67,22 @@ class Stats(C.Structure):
                 ("irOuterIterations", C.c_int), ("pcgRelResidual", C.c_double), ("lastStatus", C.c_int)]
 
 
-# Every entry point declared in include/fs2d.h, with its ctypes signature.
+class Array3D(C.Structure):
+    """fs3d_array (include/fs3d.h): the reference's Array3D<double> layout with
+    a device data pointer."""
+    _fields_ = [("data", C.c_void_p), ("NX", C.c_int), ("NY", C.c_int), ("NZ", C.c_int)]
+
+
+class MACGrid3D(C.Structure):
+    """fs3d_mac (include/fs3d.h): the reference's MACGrid3D layout."""
+    _fields_ = [("u", Array3D), ("v", Array3D), ("w", Array3D),
+                ("sizeX", C.c_int), ("sizeY", C.c_int), ("sizeZ", C.c_int)]
+
+
+FS3D_AXES = {"u": 0, "v": 1, "w": 2, "uvw": 3}
+
+# Every entry point declared in include/fs2d.h and include/fs3d.h, with its
+# ctypes signature.
 SIGNATURES = {
     "fs2d_default_options": (None, [C.POINTER(Options)]),
     "fs2d_create": (C.c_int, [C.POINTER(Config), C.POINTER(Options), C.POINTER(C.c_void_p)]),
@@ -122,6 +137,17 @@ SIGNATURES = {
     "fs2d_extrapolate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "fs2d_extrapolate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "fs2d_get_kernel_times": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    "fs3d_add": (C.c_int, [C.POINTER(Array3D), C.POINTER(Array3D), C.c_void_p]),
+    "fs3d_set_multiply_add": (C.c_int, [C.POINTER(Array3D), C.POINTER(Array3D), C.c_double, C.POINTER(Array3D),
+                                        C.c_void_p]),
+    "fs3d_inner_product": (C.c_int, [C.POINTER(Array3D), C.POINTER(Array3D), C.POINTER(C.c_double), C.c_void_p]),
+    "fs3d_infinite_norm": (C.c_int, [C.POINTER(Array3D), C.POINTER(C.c_double), C.c_void_p]),
+    "fs3d_tricubic": (C.c_int, [C.POINTER(Array3D), C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
+    "fs3d_mac_vel": (C.c_int, [C.POINTER(MACGrid3D), C.c_void_p, C.c_void_p]),
+    "fs3d_mac_face_vel": (C.c_int, [C.POINTER(MACGrid3D), C.c_int, C.c_void_p, C.c_void_p]),
+    "fs3d_mac_vel_interp": (C.c_int, [C.POINTER(MACGrid3D), C.c_int, C.c_void_p, C.c_size_t, C.c_void_p,
+                                      C.c_void_p]),
+    "fs3d_mac_vel_div": (C.c_int, [C.POINTER(MACGrid3D), C.c_void_p, C.c_void_p]),
 }
 
 _lib = None

@@ -17,7 +17,11 @@ Two kinds of artefacts:
                               ``-O2 -ffp-contract=off`` — the parity build;
     - ``libfs2d_ref_avx.so``  the reference's Release configuration on x86:
                               ``-O3 -mavx -mfma -DUSE_AVX_SIMD`` (timing);
-    - ``libfs2d_ref_omp.so``  the same plus ``-fopenmp`` (USE_OPENMP=ON).
+    - ``libfs2d_ref_omp.so``  the same plus ``-fopenmp`` (USE_OPENMP=ON);
+    - ``libfs3d_ref.so``      the header-only 3D containers
+                              (``include/Array3D.h``, ``include/MACGrid3D.h``)
+                              behind ``oracle/ref3d_capi.cpp``, serial,
+                              ``-O2 -ffp-contract=off``.
 """
 from __future__ import annotations
 
@@ -47,17 +51,17 @@ def _stale(out, inputs):
 
 def build_restatement(force=False):
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "restate", "fs2d_oracle.c")
-    deps = [src, os.path.join(HERE, "restate", "fs2d_oracle.h"),
-            os.path.join(HERE, "..", "include", "fs2d.h")]
+    srcs = [os.path.join(HERE, "restate", "fs2d_oracle.c"), os.path.join(HERE, "restate", "fs3d_oracle.c")]
+    deps = srcs + [os.path.join(HERE, "restate", "fs2d_oracle.h"), os.path.join(HERE, "restate", "fs3d_oracle.h"),
+                   os.path.join(HERE, "..", "include", "fs2d.h")]
     jobs = []
     plain = os.path.join(BUILD, "liboracle.so")
     omp = os.path.join(BUILD, "liboracle_omp.so")
     common = ["gcc", "-std=c11", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
     if force or _stale(plain, deps):
-        jobs.append(common + ["-O2", src, "-o", plain, "-lm"])
+        jobs.append(common + ["-O2", *srcs, "-o", plain, "-lm"])
     if force or _stale(omp, deps):
-        jobs.append(common + ["-O3", "-DNDEBUG", "-fopenmp", src, "-o", omp, "-lm"])
+        jobs.append(common + ["-O3", "-DNDEBUG", "-fopenmp", *srcs, "-o", omp, "-lm"])
     with ThreadPoolExecutor(max_workers=2) as ex:
         list(ex.map(_run, jobs))
     return plain
@@ -106,7 +110,15 @@ def build_reference(force=False, path=None):
         outs.append(out)
         if force or _stale(out, deps):
             jobs.append(base + flags + srcs + ["-o", out])
-    with ThreadPoolExecutor(max_workers=3) as ex:
+    # the 3D containers are header-only: one wrapper translation unit
+    src3 = os.path.join(HERE, "ref3d_capi.cpp")
+    out3 = os.path.join(REF_OUT, "libfs3d_ref.so")
+    outs.append(out3)
+    deps3 = [src3, os.path.join(inc, "Array3D.h"), os.path.join(inc, "MACGrid3D.h")] + \
+        [os.path.join(shim, f) for f in os.listdir(shim)]
+    if force or _stale(out3, deps3):
+        jobs.append(base + ["-O2", "-ffp-contract=off", "-I", noavx, src3, "-o", out3])
+    with ThreadPoolExecutor(max_workers=4) as ex:
         list(ex.map(_run, jobs))
     return outs
 

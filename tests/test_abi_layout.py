@@ -1,7 +1,7 @@
-"""The structs of include/fs2d.h as a C compiler lays them out, against the
-ctypes mirrors in fluid-sim_gb300/fs2d.py (no GPU): same size, and every field
-at the same offset.  A mismatch here would corrupt every call that passes
-the struct."""
+"""The structs of include/fs2d.h and include/fs3d.h as a C compiler lays
+them out, against the ctypes mirrors in fluid-sim_gb300/fs2d.py (no GPU):
+same size, and every field at the same offset.  A mismatch here would
+corrupt every call that passes the struct."""
 import os
 import shutil
 import subprocess
@@ -12,14 +12,16 @@ import fs2d
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 STRUCTS = {"fs2d_config": fs2d.Config, "fs2d_options": fs2d.Options, "fs2d_state": fs2d.State,
-           "fs2d_stats": fs2d.Stats, "fs2d_render": fs2d.Render}
+           "fs2d_stats": fs2d.Stats, "fs2d_render": fs2d.Render, "fs3d_array": fs2d.Array3D,
+           "fs3d_mac": fs2d.MACGrid3D}
 
 
 def c_layout(tmp_path):
     gcc = shutil.which("gcc")
     if gcc is None:
         pytest.skip("gcc not available")
-    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "fs2d.h"', "int main(void) {"]
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "fs2d.h"', '#include "fs3d.h"',
+             "int main(void) {"]
     for cname, py in STRUCTS.items():
         lines.append(f'    printf("{cname} sizeof %zu\\n", sizeof({cname}));')
         for fname, _ in py._fields_:

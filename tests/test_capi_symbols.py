@@ -1,5 +1,6 @@
 """The C-ABI library loads without a GPU and exports every entry point
-declared in include/fs2d.h (no compute calls are made here)."""
+declared in include/fs2d.h and include/fs3d.h (no compute calls are made
+here)."""
 import os
 import re
 
@@ -9,9 +10,12 @@ ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 
 
 def declared_symbols():
-    text = open(os.path.join(ROOT, "include", "fs2d.h")).read()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(fs2d_[a-z_0-9]+)\s*\(", text)))
+    syms = set()
+    for h in ("fs2d.h", "fs3d.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        syms |= set(re.findall(r"\b(fs[23]d_[a-z_0-9]+)\s*\(", text))
+    return sorted(syms)
 
 
 def test_header_declares_entry_points():
