@@ -713,6 +713,14 @@ int fs2d_create(const fs2d_config* cfg, const fs2d_options* opt, fs2d_sim** out)
         return rc;
     }
     s->stats_host->volume = s->orig_volume;
+    // waterVolume before the first createWaterLevelSet is origWaterVolume (src/FluidSim2D.cpp:71-72)
+    rc = check_cuda(cudaMemcpy(&s->stats->volume, &s->orig_volume, sizeof(double), cudaMemcpyHostToDevice),
+                    "upload volume");
+    if (rc) {
+        free_all(s);
+        delete h;
+        return rc;
+    }
     *out = reinterpret_cast<fs2d_sim*>(h);
     return FS2D_OK;
 }
@@ -742,6 +750,73 @@ int fs2d_run_stage(fs2d_sim* p, int stage) {
 int fs2d_render_export(fs2d_sim* p, fs2d_render* r) {
     if (!p || !r) return FS2D_ERR_INVALID;
     return render_export(&H(p)->sim, r);
+}
+
+// Particle reseeding (include/fs2d.h): plan on the device (counts, removals,
+// requests), one wait for the two totals, the new arrays written into
+// scratch and copied over the handle's (grown first when they do not fit).
+int fs2d_reseed(fs2d_sim* p, int minPerCell, int maxPerCell, unsigned int seed, fs2d_reseed_stats* out) {
+    if (!p || minPerCell < 0 || minPerCell > 64 || maxPerCell < 0 || (maxPerCell > 0 && maxPerCell < minPerCell)) {
+        set_error("fs2d_reseed: need 0 <= minPerCell <= 64 and maxPerCell == 0 or >= minPerCell");
+        return FS2D_ERR_INVALID;
+    }
+    Sim* s = &H(p)->sim;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    const size_t N = s->N, np = s->np;
+    // the scans below run over np + 1 particle words
+    const size_t scan_need = std::max(N, np) / 4096 + 4;
+    if (scan_need > s->scan_tmp_n) {
+        cudaFree(s->scan_tmp);
+        s->scan_tmp = nullptr;
+        s->scan_tmp_n = 0;
+        int rc = dalloc(&s->scan_tmp, scan_need);
+        if (rc) return rc;
+        s->scan_tmp_n = scan_need;
+    }
+    s->generation++;
+    DevScratch mem;
+    ReseedScratch x{mem.get<uint32_t>(N + 1), mem.get<uint32_t>(N + 1), mem.get<uint32_t>(N + 1),
+                    mem.get<uint32_t>(N + 1), mem.get<uint32_t>(np + 1), mem.get<uint32_t>(np + 1)};
+    if (!x.cnt || !x.start || !x.fill || !x.spawn || !x.bucket || !x.keep) {
+        set_error("fs2d_reseed: out of device memory for scratch");
+        return FS2D_ERR_ALLOC;
+    }
+    size_t n_keep = 0, n_add = 0;
+    int rc = reseed_plan(s, x, minPerCell, maxPerCell, &n_keep, &n_add);
+    if (rc) return rc;
+    const size_t n = n_keep + n_add;
+    double2* npos = mem.get<double2>(n);
+    double2* nvel = mem.get<double2>(n);
+    if (!npos || !nvel) {
+        set_error("fs2d_reseed: out of device memory for %zu particles", n);
+        return FS2D_ERR_ALLOC;
+    }
+    if ((rc = reseed_write(s, x, seed, npos, nvel))) return rc;
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    if (n > s->np_cap && (rc = alloc_particles(s, n + n / 4))) return rc;
+    if (n) {
+        FS2D_CUDA(cudaMemcpyAsync(s->pos, npos, n * sizeof(double2), cudaMemcpyDeviceToDevice, s->stream));
+        FS2D_CUDA(cudaMemcpyAsync(s->vel, nvel, n * sizeof(double2), cudaMemcpyDeviceToDevice, s->stream));
+    }
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    s->np = n;
+    if (out) {
+        out->removed = np - n_keep;
+        out->added = n_add;
+        out->numParticles = n;
+    }
+    return FS2D_OK;
+}
+
+int fs2d_set_volume_correction(fs2d_sim* p, double rate) {
+    if (!p || !(rate >= 0.0 && rate <= 1.0)) {
+        set_error("fs2d_set_volume_correction: need 0 <= rate <= 1");
+        return FS2D_ERR_INVALID;
+    }
+    Sim* s = &H(p)->sim;
+    s->volume_rate = rate;
+    s->generation++;   // captured phases take the rate by value
+    return FS2D_OK;
 }
 
 int fs2d_solve_pressure(fs2d_sim* p, const uint8_t* cell, const double* phi, const double* u, const double* v,

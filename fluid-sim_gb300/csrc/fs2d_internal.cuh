@@ -289,6 +289,7 @@ struct Sim {
     long long frames = 0;
     double current_time = 0;
     double orig_volume = 0;
+    double volume_rate = 0;   // fs2d_set_volume_correction (0: off)
     int last_iters = 0;
     int last_outer = 0;
     double last_rel_res = 0;
@@ -430,6 +431,18 @@ size_t extrap_tiles(int W, int H);
 int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double* const a[2], uint32_t* const m[2],
                      const int W[2], const int H[2], int band);
 int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n);
+
+// Particle reseeding (fs2d_reseed): scratch of N + 1 (cells) or np + 1
+// (particles) words each.
+struct ReseedScratch {
+    uint32_t *cnt, *start, *fill, *spawn;   // per cell
+    uint32_t *bucket, *keep;                // per particle
+};
+// Counts and plans on the handle's stream, then waits: *n_keep survivors,
+// *n_add new particles.
+int reseed_plan(Sim* s, const ReseedScratch& x, int min_per_cell, int max_per_cell, size_t* n_keep, size_t* n_add);
+// Writes the survivors and the new particles into npos / nvel (n_keep + n_add entries).
+int reseed_write(Sim* s, const ReseedScratch& x, unsigned seed, double2* npos, double2* nvel);
 
 // ---- transposes of the particle transfers (transfer.cu) ----
 int p2g_adjoint(Sim* s, double* ubar, double* vbar, double* wu, double* wv, double2* velbar);

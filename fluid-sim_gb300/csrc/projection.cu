@@ -34,7 +34,8 @@ constexpr int kT = 256;
 __global__ void k_build(const uint8_t* __restrict__ cell, const double* __restrict__ phi,
                         const double* __restrict__ u, const double* __restrict__ v, int NX, int NY, double scaleA,
                         double scale, double* Adiag, double* Ax, double* Ay, double* rhs, double* r, double* p,
-                        double* partial, PcgScalars* pcg, double tol) {
+                        double* partial, PcgScalars* pcg, double tol, const FrameStats* __restrict__ stats,
+                        double vol0, double vol_rate, double dt) {
     __shared__ double sh[32];
     size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
     size_t N = (size_t)NX * NY;
@@ -60,6 +61,11 @@ __global__ void k_build(const uint8_t* __restrict__ cell, const double* __restri
             if (rgt == kSolid) b += scale * (u1 - 0);
             if (d == kSolid) b -= scale * (v0 - 0);
             if (up == kSolid) b += scale * (v1 - 0);
+            // volume correction (fs2d_set_volume_correction; not in the reference)
+            if (vol_rate != 0.0) {
+                const double vol = stats->volume;
+                if (vol > 0.0) b += vol_rate * ((vol0 - vol) / vol0) / dt;
+            }
         }
         // non-fluid cells carry -0.0: a marker the MIC(0) factor reads from its
         // staged operands (fluid cells hold the reference's value, >= +0.0)
@@ -424,7 +430,8 @@ static int projection_pcg(Sim* s, int* status);
 int projection_build(Sim* s) {
     const double scaleA = s->dt / (s->rho * s->dx * s->dx);
     FS2D_LAUNCH(s, k_build, blocks_for(s->N, kT), kT, 0, s->cell, s->phi, s->u, s->v, s->NX, s->NY, scaleA,
-                1.0 / s->dx, s->Adiag, s->Ax, s->Ay, s->rhs, s->r, s->p, s->partial, s->pcg, s->opt.pcg_tol);
+                1.0 / s->dx, s->Adiag, s->Ax, s->Ay, s->rhs, s->r, s->p, s->partial, s->pcg, s->opt.pcg_tol,
+                s->stats, s->orig_volume, s->volume_rate, s->dt);
     return 0;
 }
 

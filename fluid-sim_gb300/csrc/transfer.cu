@@ -731,6 +731,98 @@ __global__ void k_scan_add(uint32_t* out, size_t n, const uint32_t* __restrict__
     }
 }
 
+// ---- particle reseeding (fs2d_reseed; the reference lists it as a TODO, README.md:13-18) ----
+
+// The cell a particle is counted in: (int)(x/dx), (int)(y/dx) clamped into the grid.
+__device__ __forceinline__ size_t rs_cell(double2 p, double dx, int NX, int NY) {
+    const int i = iclamp((int)(p.x / dx), 0, NX - 1), j = iclamp((int)(p.y / dx), 0, NY - 1);
+    return (size_t)j * NX + i;
+}
+
+// splitmix64's finaliser; the jitter of new particle m of cell c takes 53
+// bits of it for each axis, scaled into [0, 1)
+__device__ __forceinline__ unsigned long long rs_mix(unsigned long long z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_rs_count(const double2* __restrict__ pos, size_t np, double dx, int NX, int NY, uint32_t* cnt,
+                           uint32_t* keep) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    atomicAdd(&cnt[rs_cell(pos[e], dx, NX, NY)], 1u);
+    keep[e] = 1u;
+}
+
+// Buckets of particle indices per cell (in arbitrary order within a bucket).
+__global__ void k_rs_fill(const double2* __restrict__ pos, size_t np, double dx, int NX, int NY,
+                          const uint32_t* __restrict__ start, uint32_t* fill, uint32_t* bucket) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    const size_t c = rs_cell(pos[e], dx, NX, NY);
+    bucket[start[c] + atomicAdd(&fill[c], 1u)] = (uint32_t)e;
+}
+
+// Per cell: where it holds more than maxPC particles, its bucket is sorted
+// by particle index and all but the first maxPC are dropped; a FLUID cell
+// with fewer than minPC asks for the difference.
+__global__ void k_rs_cells(const uint8_t* __restrict__ cell, const uint32_t* __restrict__ cnt,
+                           const uint32_t* __restrict__ start, uint32_t* bucket, size_t N, int minPC, int maxPC,
+                           uint32_t* keep, uint32_t* spawn) {
+    const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const uint32_t k = cnt[c];
+    if (maxPC > 0 && k > (uint32_t)maxPC) {
+        uint32_t* b = bucket + start[c];
+        for (uint32_t m = 1; m < k; m++) {   // insertion sort: buckets hold a few particles
+            const uint32_t key = b[m];
+            uint32_t q = m;
+            while (q > 0 && b[q - 1] > key) {
+                b[q] = b[q - 1];
+                q--;
+            }
+            b[q] = key;
+        }
+        for (uint32_t m = (uint32_t)maxPC; m < k; m++) keep[b[m]] = 0u;
+    }
+    spawn[c] = (cell[c] == kFluid && k < (uint32_t)minPC) ? (uint32_t)minPC - k : 0u;
+}
+
+// Survivors, in particle order, to the start of the new arrays (keep holds
+// the exclusive scan of the keep flags, np + 1 entries).
+__global__ void k_rs_compact(const double2* __restrict__ pos, const double2* __restrict__ vel, size_t np,
+                             const uint32_t* __restrict__ keep, double2* npos, double2* nvel) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np || keep[e + 1] == keep[e]) return;
+    npos[keep[e]] = pos[e];
+    nvel[keep[e]] = vel[e];
+}
+
+// New particles of each cell after the survivors (spawn holds the exclusive
+// scan of the per-cell requests, N + 1 entries), moving with the bilinear
+// grid velocity at their position.
+__global__ void k_rs_spawn(const uint32_t* __restrict__ spawn, size_t N, int NX, int NY, double dx, size_t n_keep,
+                           unsigned seed, const double* __restrict__ u, const double* __restrict__ v, double2* npos,
+                           double2* nvel) {
+    const size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const uint32_t first = spawn[c], n = spawn[c + 1] - first;
+    const int i = (int)(c % NX), j = (int)(c / NX);
+    for (uint32_t m = 0; m < n; m++) {
+        const unsigned long long key =
+            (unsigned long long)seed * 0x9E3779B97F4A7C15ull + (unsigned long long)c * 0x100000001B3ull + m;
+        const double jx = (double)(rs_mix(key) >> 11) * 0x1.0p-53;
+        const double jy = (double)(rs_mix(key ^ 0xD6E8FEB86659FD93ull) >> 11) * 0x1.0p-53;
+        const double px = ((double)i + jx) * dx, py = ((double)j + jy) * dx;
+        const size_t d = n_keep + first + m;
+        npos[d] = make_double2(px, py);
+        nvel[d] = make_double2(extract(u, nullptr, px / dx, py / dx - 0.5, NX + 1, NY),
+                               extract(v, nullptr, px / dx - 0.5, py / dx, NX, NY + 1));
+    }
+}
+
 }  // namespace
 
 // In-place exclusive scan of data[0..n); data[n] receives the total.
@@ -743,6 +835,48 @@ int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n) {
     FS2D_LAUNCH(s, k_scan_blocks, (unsigned)nb, kScanBlock, 0, data, data, n, s->scan_tmp);
     FS2D_LAUNCH(s, k_scan_sums, 1, 1024, 0, s->scan_tmp, (int)nb, data + n);
     FS2D_LAUNCH(s, k_scan_add, (unsigned)nb, kScanBlock, 0, data, n, s->scan_tmp);
+    return 0;
+}
+
+int reseed_plan(Sim* s, const ReseedScratch& x, int min_per_cell, int max_per_cell, size_t* n_keep, size_t* n_add) {
+    const size_t N = s->N, np = s->np;
+    const int T = 256;
+    FS2D_CUDA(cudaMemsetAsync(x.cnt, 0, (N + 1) * sizeof(uint32_t), s->stream));
+    FS2D_CUDA(cudaMemsetAsync(x.fill, 0, (N + 1) * sizeof(uint32_t), s->stream));
+    FS2D_CUDA(cudaMemsetAsync(x.keep, 0, (np + 1) * sizeof(uint32_t), s->stream));
+    if (np) FS2D_LAUNCH(s, k_rs_count, blocks_for(np, T), T, 0, s->pos, np, s->dx, s->NX, s->NY, x.cnt, x.keep);
+    FS2D_CUDA(cudaMemcpyAsync(x.start, x.cnt, (N + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, s->stream));
+    int rc = exclusive_scan_u32(s, x.start, N);
+    if (rc) return rc;
+    if (np)
+        FS2D_LAUNCH(s, k_rs_fill, blocks_for(np, T), T, 0, s->pos, np, s->dx, s->NX, s->NY, x.start, x.fill,
+                    x.bucket);
+    FS2D_LAUNCH(s, k_rs_cells, blocks_for(N, T), T, 0, s->cell, x.cnt, x.start, x.bucket, N, min_per_cell,
+                max_per_cell, x.keep, x.spawn);
+    if ((rc = exclusive_scan_u32(s, x.keep, np))) return rc;
+    if ((rc = exclusive_scan_u32(s, x.spawn, N))) return rc;
+    uint32_t totals[2] = {0, 0};
+    FS2D_CUDA(cudaMemcpyAsync(&totals[0], x.keep + np, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaMemcpyAsync(&totals[1], x.spawn + N, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    *n_keep = totals[0];
+    *n_add = totals[1];
+    return 0;
+}
+
+int reseed_write(Sim* s, const ReseedScratch& x, unsigned seed, double2* npos, double2* nvel) {
+    const size_t N = s->N, np = s->np;
+    const int T = 256;
+    size_t n_keep = 0;
+    {
+        uint32_t t = 0;
+        FS2D_CUDA(cudaMemcpyAsync(&t, x.keep + np, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));
+        FS2D_CUDA(cudaStreamSynchronize(s->stream));
+        n_keep = t;
+    }
+    if (np) FS2D_LAUNCH(s, k_rs_compact, blocks_for(np, T), T, 0, s->pos, s->vel, np, x.keep, npos, nvel);
+    FS2D_LAUNCH(s, k_rs_spawn, blocks_for(N, T), T, 0, x.spawn, N, s->NX, s->NY, s->dx, n_keep, seed, s->u, s->v,
+                npos, nvel);
     return 0;
 }
 

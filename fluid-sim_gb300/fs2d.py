@@ -67,6 +67,10 @@ class Stats(C.Structure):
                 ("irOuterIterations", C.c_int), ("pcgRelResidual", C.c_double), ("lastStatus", C.c_int)]
 
 
+class ReseedStats(C.Structure):
+    _fields_ = [("removed", C.c_size_t), ("added", C.c_size_t), ("numParticles", C.c_size_t)]
+
+
 class Array3D(C.Structure):
     """fs3d_array (include/fs3d.h): the reference's Array3D<double> layout with
     a device data pointer."""
@@ -137,6 +141,8 @@ SIGNATURES = {
     "fs2d_extrapolate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "fs2d_extrapolate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "fs2d_get_kernel_times": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
+    "fs2d_reseed": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint, C.POINTER(ReseedStats)]),
+    "fs2d_set_volume_correction": (C.c_int, [C.c_void_p, C.c_double]),
     "fs3d_add": (C.c_int, [C.POINTER(Array3D), C.POINTER(Array3D), C.c_void_p]),
     "fs3d_set_multiply_add": (C.c_int, [C.POINTER(Array3D), C.POINTER(Array3D), C.c_double, C.POINTER(Array3D),
                                         C.c_void_p]),
@@ -376,6 +382,16 @@ class FluidSim2D:
         r.waterCount, r.solidCount, r.pressureCount = (C.pointer(c) for c in counts)
         _check(load().fs2d_render_export(self.h, C.byref(r)))
         return tuple(c.value for c in counts)
+
+    def reseed(self, minPerCell, maxPerCell, seed=0):
+        """Particle reseeding (fs2d_reseed; the reference lists it as a TODO)."""
+        st = ReseedStats()
+        _check(load().fs2d_reseed(self.h, minPerCell, maxPerCell, seed, C.byref(st)))
+        return {"removed": st.removed, "added": st.added, "numParticles": st.numParticles}
+
+    def set_volume_correction(self, rate):
+        """Volume correction in the projection (fs2d_set_volume_correction)."""
+        _check(load().fs2d_set_volume_correction(self.h, rate))
 
     def set_params(self, gravityX, gravityY, picFlipAlpha, dt):
         _check(load().fs2d_set_params(self.h, gravityX, gravityY, picFlipAlpha, dt))

@@ -392,6 +392,40 @@ typedef struct fs2d_render {
 } fs2d_render;
 int fs2d_render_export(fs2d_sim* sim, fs2d_render* r);
 
+/* Particle reseeding and volume correction.  The reference lists both as
+ * features it needs and does not have (README.md:13-18: "the fluid
+ * simulation doesn't conserve volume very well"); it records the water
+ * volume at creation (origWaterVolume, src/FluidSim2D.cpp:71-72) but never
+ * uses it.  Both are off unless called, and then deterministic: the same
+ * state and arguments give the same bits on every run.
+ *
+ * fs2d_reseed: call between frames.  Particles are counted per cell at
+ * (int)(x/dx), (int)(y/dx), clamped into the grid.  In every cell holding
+ * more than maxPerCell particles (maxPerCell > 0), those after the first
+ * maxPerCell in particle order are removed; every FLUID cell (labels of the
+ * last createWaterLevelSet) holding fewer than minPerCell gets new particles
+ * up to minPerCell, at ((i + jx) dx, (j + jy) dx) with jx, jy in [0, 1)
+ * drawn from a 64-bit mix of (seed, cell, k), moving with the bilinear grid
+ * velocity there (the PIC part of updateParticleVelocities).  Survivors
+ * keep their order; new particles follow in row-major cell order.  0 <=
+ * minPerCell <= 64, maxPerCell == 0 (no removal) or minPerCell <=
+ * maxPerCell.  `out` (may be NULL) receives the counts. */
+typedef struct fs2d_reseed_stats {
+    size_t removed;
+    size_t added;
+    size_t numParticles;   /* after reseeding */
+} fs2d_reseed_stats;
+int fs2d_reseed(fs2d_sim* sim, int minPerCell, int maxPerCell, unsigned int seed, fs2d_reseed_stats* out);
+
+/* fs2d_set_volume_correction: from the next applyProjection on, every FLUID
+ * cell's right-hand side gets rate * ((V0 - V) / V0) / dt added, V the
+ * waterVolume of the frame's createWaterLevelSet (the volume at creation
+ * before the first one) and V0 origWaterVolume: the pressure solve then
+ * targets a uniform divergence that gives back the fraction `rate` of the
+ * relative volume error per step.  rate 0 (the default) turns it off and
+ * leaves every stage as the reference's; 0 <= rate <= 1. */
+int fs2d_set_volume_correction(fs2d_sim* sim, double rate);
+
 /* Test hook of the failure path of the wavefront sweeps (no reference
  * counterpart).  Every wait of a sweep on its neighbour strip is bounded: it
  * gives up after `polls` polls (<= 0: the default, about half a second),

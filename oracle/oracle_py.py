@@ -51,7 +51,8 @@ class State(C.Structure):
 
 class OrOptions(C.Structure):
     _fields_ = [("mic_tau", C.c_double), ("mic_sigma", C.c_double), ("pcg_tol", C.c_double),
-                ("pcg_max_iters", C.c_int), ("sl_inplace", C.c_int), ("extrapolate_band", C.c_int)]
+                ("pcg_max_iters", C.c_int), ("sl_inplace", C.c_int), ("extrapolate_band", C.c_int),
+                ("volume_rate", C.c_double)]
 
 
 def make_config(scene):
@@ -177,6 +178,9 @@ def get_oracle_lib(omp=False):
         lib.or_tricubic.restype = C.c_double
         lib.or_tricubic.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.c_double, C.c_double]
         lib.or_extrapolate.argtypes = [C.POINTER(C.c_double), C.c_int, C.c_int, C.POINTER(C.c_uint32), C.c_int]
+        lib.or_reseed.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint, C.POINTER(C.c_size_t)]
+        lib.or_reseed_jitter.argtypes = [C.c_uint, C.c_size_t, C.c_uint, C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double)]
         _libs[key] = lib
     return _libs[key]
 
@@ -213,7 +217,8 @@ def default_or_options(**kw):
 
 class OracleSim(_SimBase):
     """The C restatement.  Options: mic_tau, mic_sigma, pcg_tol,
-    pcg_max_iters, sl_inplace (1 = reference semantics), extrapolate_band."""
+    pcg_max_iters, sl_inplace (1 = reference semantics), extrapolate_band,
+    volume_rate (0 = reference semantics)."""
     prefix = "or_"
 
     def __init__(self, scene, seed=None, omp=False, **opts):
@@ -239,6 +244,12 @@ class OracleSim(_SimBase):
 
     def set_params(self, gx, gy, alpha, dt):
         self.lib.or_set_params(self.h, gx, gy, alpha, dt)
+
+    def reseed(self, min_per_cell, max_per_cell, seed):
+        """Particle reseeding (an option the reference lacks; see or_reseed)."""
+        out = (C.c_size_t * 2)()
+        self.lib.or_reseed(self.h, min_per_cell, max_per_cell, seed, out)
+        return {"removed": int(out[0]), "added": int(out[1]), "numParticles": self.num_particles()}
 
 
 class RefSim(_SimBase):

@@ -219,6 +219,7 @@ void or_default_options(or_options* o) {
     o->pcg_max_iters = 200;
     o->sl_inplace = 1;
     o->extrapolate_band = 0;
+    o->volume_rate = 0.0;
 }
 
 or_sim* or_create(const fs2d_config* cfg, const or_options* opt, int use_seed, unsigned seed) {
@@ -619,6 +620,9 @@ static void apply_projection(or_sim* s) {
                 if (cell[c + 1] == CELL_SOLID) rhs[c] += scale * (u1 - 0);
                 if (cell[c - NX] == CELL_SOLID) rhs[c] -= scale * (v0 - 0);
                 if (cell[c + NX] == CELL_SOLID) rhs[c] += scale * (v1 - 0);
+                /* volume correction (an option; not in the reference) */
+                if (s->opt.volume_rate != 0.0 && s->waterVolume > 0.0)
+                    rhs[c] += s->opt.volume_rate * ((s->origWaterVolume - s->waterVolume) / s->origWaterVolume) / s->dt;
             }
         }
     }
@@ -795,6 +799,80 @@ static int apply_advection(or_sim* s) {
 /* ------------------------------------------------------------------ */
 /* Frame / stage drivers                                              */
 /* ------------------------------------------------------------------ */
+
+/* ------------------------------------------------------------------ */
+/* particle reseeding (an option; not in the reference)                */
+/* ------------------------------------------------------------------ */
+
+static uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+void or_reseed_jitter(unsigned seed, size_t c, unsigned m, double* jx, double* jy) {
+    uint64_t key = (uint64_t)seed * 0x9E3779B97F4A7C15ull + (uint64_t)c * 0x100000001B3ull + (uint64_t)m;
+    *jx = (double)(mix64(key) >> 11) * 0x1.0p-53;
+    *jy = (double)(mix64(key ^ 0xD6E8FEB86659FD93ull) >> 11) * 0x1.0p-53;
+}
+
+static size_t particle_cell(const or_sim* s, double x, double y) {
+    int i = clampi((int)(x / s->dx), 0, s->NX - 1), j = clampi((int)(y / s->dx), 0, s->NY - 1);
+    return (size_t)j * s->NX + i;
+}
+
+void or_reseed(or_sim* s, int minPerCell, int maxPerCell, unsigned seed, size_t* out) {
+    const int NX = s->NX, NY = s->NY;
+    const size_t N = (size_t)NX * NY;
+    uint32_t* cnt = (uint32_t*)xcalloc(N, sizeof(uint32_t));
+    uint32_t* seen = (uint32_t*)xcalloc(N, sizeof(uint32_t));
+    for (size_t e = 0; e < s->np; e++) cnt[particle_cell(s, s->pos[2 * e], s->pos[2 * e + 1])]++;
+    size_t add = 0;
+    for (size_t c = 0; c < N; c++)
+        if (s->cell[c] == CELL_FLUID && cnt[c] < (uint32_t)minPerCell) add += (uint32_t)minPerCell - cnt[c];
+    double* pos = (double*)xcalloc(2 * (s->np + add), sizeof(double));
+    double* vel = (double*)xcalloc(2 * (s->np + add), sizeof(double));
+    size_t n = 0, removed = 0;
+    for (size_t e = 0; e < s->np; e++) {
+        size_t c = particle_cell(s, s->pos[2 * e], s->pos[2 * e + 1]);
+        if (maxPerCell > 0 && seen[c] >= (uint32_t)maxPerCell) {
+            seen[c]++;
+            removed++;
+            continue;
+        }
+        seen[c]++;
+        pos[2 * n] = s->pos[2 * e];
+        pos[2 * n + 1] = s->pos[2 * e + 1];
+        vel[2 * n] = s->vel[2 * e];
+        vel[2 * n + 1] = s->vel[2 * e + 1];
+        n++;
+    }
+    const double dx = s->dx;
+    for (size_t c = 0; c < N; c++) {
+        if (s->cell[c] != CELL_FLUID || cnt[c] >= (uint32_t)minPerCell) continue;
+        const int i = (int)(c % NX), j = (int)(c / NX);
+        for (unsigned m = 0; m < (uint32_t)minPerCell - cnt[c]; m++) {
+            double jx, jy;
+            or_reseed_jitter(seed, c, m, &jx, &jy);
+            const double px = ((double)i + jx) * dx, py = ((double)j + jy) * dx;
+            pos[2 * n] = px;
+            pos[2 * n + 1] = py;
+            vel[2 * n] = linear_extract(s->u, NX + 1, NY, px / dx, py / dx - 0.5);
+            vel[2 * n + 1] = linear_extract(s->v, NX, NY + 1, px / dx - 0.5, py / dx);
+            n++;
+        }
+    }
+    free(s->pos);
+    free(s->vel);
+    s->pos = pos;
+    s->vel = vel;
+    s->np = n;
+    free(cnt);
+    free(seen);
+    out[0] = removed;
+    out[1] = add;
+}
 
 int or_run_stage(or_sim* s, int stage) {
     switch (stage) {

@@ -36,6 +36,9 @@ typedef struct or_options {
     int pcg_max_iters;     /* reference 200 */
     int sl_inplace;        /* 1: the reference's in-place advection; 0: double-buffered */
     int extrapolate_band;  /* 0: all BFS layers (reference); k > 0: layers <= k only */
+    double volume_rate;    /* volume correction (not in the reference, which lists it as a TODO): 0 off;
+                              r > 0 adds r * ((V0 - V) / V0) / dt to the projection's right-hand side of
+                              every fluid cell (V the frame's waterVolume, V0 origWaterVolume) */
 } or_options;
 
 typedef struct or_sim or_sim;
@@ -55,6 +58,20 @@ void or_stats(or_sim* s, double* out);
 /* out[0] = PCG iterations of the last solve, out[1] = ||r||inf/||b||inf at exit */
 void or_solver_info(or_sim* s, double* out);
 void or_set_params(or_sim* s, double gx, double gy, double alpha, double dt);
+
+/* Particle reseeding (not in the reference, which lists it as a TODO):
+ * particles counted per cell at (int)(x/dx), (int)(y/dx) clamped into the
+ * grid; in every cell with more than maxPerCell (> 0) particles those after
+ * the first maxPerCell in index order are removed; every FLUID cell with
+ * fewer than minPerCell gets new particles up to minPerCell, in row-major
+ * cell order, at ((i + jx) dx, (j + jy) dx) with jx, jy in [0, 1) from
+ * or_reseed_jitter, and the bilinear grid velocity there (the PIC part of
+ * updateParticleVelocities).  Survivors keep their order, new particles
+ * follow.  out[0] = removed, out[1] = added. */
+void or_reseed(or_sim* s, int minPerCell, int maxPerCell, unsigned seed, size_t* out);
+/* the jitter of new particle m of cell c: bits of a 64-bit mix (splitmix64's
+ * finaliser) of (seed, c, m), 53 of them scaled into [0, 1) */
+void or_reseed_jitter(unsigned seed, size_t c, unsigned m, double* jx, double* jy);
 
 /* Building blocks, exposed for unit tests. */
 double or_tricubic(const double* data, int NX, int NY, double px, double py);

@@ -1,0 +1,130 @@
+"""Particle reseeding (fs2d_reseed) and volume correction
+(fs2d_set_volume_correction) on the GPU against the oracle restatement.
+
+The reference lists both as missing (README.md:13-18); the oracle's rules
+(or_reseed and the volume_rate option of oracle/restate/fs2d_oracle.c,
+pinned by tests/test_reseed_volume_oracle.py) are the specification:
+
+* reseeding from the oracle's own state gives the same particles and
+  velocities bit for bit, including a reseed that grows the handle's
+  particle buffers, after which whole frames still follow the oracle;
+* frames of the FP64 path with volume correction follow the oracle with the
+  same option (labels identical, fields within 1e-6 of their largest value);
+* in mixed precision the correction halves the volume drift of the
+  semi-Lagrangian dam break, as it does in the oracle;
+* out-of-range arguments are refused.
+"""
+import numpy as np
+import pytest
+
+import oracle_py as O
+import scenes
+
+fs2d = pytest.importorskip("fs2d")
+pytestmark = pytest.mark.gpu
+
+FLUID = 1
+
+
+def same(a, b):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def oracle_after(sc, frames, **opts):
+    o = O.OracleSim(sc, seed=3, sl_inplace=0, **opts)
+    for _ in range(frames):
+        o.frame()
+    return o
+
+
+def close_fields(a, b, fields=("p", "u", "v", "particles", "particleVels"), tol=1e-6):
+    for f in fields:
+        scale = np.abs(b[f]).max() + 1e-30
+        err = np.abs(a[f] - b[f]).max()
+        assert err <= tol * scale, (f, err, scale)
+
+
+@pytest.mark.parametrize("lo,hi", [(3, 6), (0, 3), (5, 0), (4, 4)])
+def test_reseed_matches_oracle(lo, hi):
+    sc = scenes.pic_dam_break_disk(48)
+    orc = oracle_after(sc, 6)
+    sim = fs2d.FluidSim2D(sc, seed=3)
+    sim.set_state(orc.get_state())
+    got, want = sim.reseed(lo, hi, 11), orc.reseed(lo, hi, 11)
+    assert got == want
+    a, b = sim.get_state(["particles", "particleVels"]), orc.get_state()
+    assert same(a["particles"], b["particles"])
+    assert same(a["particleVels"], b["particleVels"])
+    sim.close()
+
+
+def test_reseed_growing_the_buffers_then_frames_follow_the_oracle():
+    sc = scenes.pic_dam_break_disk(64)
+    orc = oracle_after(sc, 4)
+    sim = fs2d.FluidSim2D(sc, seed=3)
+    sim.set_state(orc.get_state())
+    n0 = sim.num_particles()
+    got, want = sim.reseed(9, 12, 4), orc.reseed(9, 12, 4)
+    assert got == want and got["numParticles"] > 1.5 * n0   # beyond the handle's spare capacity
+    for frame in range(3):
+        sim.runFrame()
+        orc.frame()
+        a, b = sim.get_state(), orc.get_state()
+        assert same(a["cell"], b["cell"]), frame
+        close_fields(a, b)
+    sim.close()
+
+
+def test_volume_correction_frames_follow_the_oracle():
+    sc = scenes.pic_dam_break_disk(64)   # dx = 1/64: the water volume is exact in any summation order
+    sim = fs2d.FluidSim2D(sc, seed=3)
+    sim.set_volume_correction(0.1)
+    orc = O.OracleSim(sc, seed=3, sl_inplace=0, volume_rate=0.1)
+    plain = O.OracleSim(sc, seed=3, sl_inplace=0)
+    for frame in range(8):
+        sim.runFrame()
+        orc.frame()
+        plain.frame()
+        a, b = sim.get_state(), orc.get_state()
+        assert same(a["cell"], b["cell"]), frame
+        close_fields(a, b)
+    # the option changed the solution
+    assert np.abs(plain.get_state()["p"] - b["p"]).max() > 1e-3 * np.abs(b["p"]).max()
+    sim.close()
+
+
+def drift(sim, v0, frames):
+    worst = 0.0
+    for _ in range(frames):
+        sim.runFrame()
+        worst = max(worst, abs(sim.stats()["waterVolume"] - v0) / v0)
+    return worst
+
+
+def test_volume_correction_mixed_reduces_drift():
+    sc = scenes.sl_dam_break(64)
+    v0 = float((np.asarray(sc["cells"]) == FLUID).sum()) * sc["dx"] ** 2
+    plain = fs2d.FluidSim2D(sc, seed=3, precision="mixed", pcg_tol=1e-6)
+    corrected = fs2d.FluidSim2D(sc, seed=3, precision="mixed", pcg_tol=1e-6)
+    corrected.set_volume_correction(0.05)
+    d0, d1 = drift(plain, v0, 120), drift(corrected, v0, 120)
+    assert d0 > 0.1 and d1 < 0.5 * d0, (d0, d1)
+    plain.close()
+    corrected.close()
+
+
+def test_out_of_range_arguments_are_refused():
+    sim = fs2d.FluidSim2D(scenes.sl_dam_break(32), seed=1)
+    lib = fs2d.load()
+    assert lib.fs2d_reseed(sim.h, 65, 0, 0, None) == 1
+    assert lib.fs2d_reseed(sim.h, 4, 3, 0, None) == 1
+    assert lib.fs2d_reseed(sim.h, -1, 0, 0, None) == 1
+    assert lib.fs2d_set_volume_correction(sim.h, -0.1) == 1
+    assert lib.fs2d_set_volume_correction(sim.h, 1.5) == 1
+    assert lib.fs2d_set_volume_correction(sim.h, float("nan")) == 1
+    # nothing changed: a reseed that neither adds nor removes keeps the particles
+    before = sim.get_state(["particles"])["particles"]
+    assert sim.reseed(0, 0, 0) == {"removed": 0, "added": 0, "numParticles": len(before) // 2}
+    assert same(sim.get_state(["particles"])["particles"], before)
+    sim.close()
