@@ -853,7 +853,7 @@ int reseed_plan(Sim* s, const ReseedScratch& x, int min_per_cell, int max_per_ce
                     x.bucket);
     FS2D_LAUNCH(s, k_rs_cells, blocks_for(N, T), T, 0, s->cell, x.cnt, x.start, x.bucket, N, min_per_cell,
                 max_per_cell, x.keep, x.spawn);
-    if ((rc = exclusive_scan_u32(s, x.keep, np))) return rc;
+    if (np && (rc = exclusive_scan_u32(s, x.keep, np))) return rc;   // np == 0: keep[0] = 0 from the memset
     if ((rc = exclusive_scan_u32(s, x.spawn, N))) return rc;
     uint32_t totals[2] = {0, 0};
     FS2D_CUDA(cudaMemcpyAsync(&totals[0], x.keep + np, sizeof(uint32_t), cudaMemcpyDeviceToHost, s->stream));

@@ -114,6 +114,18 @@ def test_volume_correction_mixed_reduces_drift():
     corrected.close()
 
 
+def test_reseed_without_particles_or_fluid():
+    """A scene with no fluid: nothing to count, keep or add."""
+    sc = scenes.dam_break(24, mode=scenes.PICFLIP, extent=(0.0, 0.0))
+    sim = fs2d.FluidSim2D(sc, seed=1)
+    assert sim.num_particles() == 0
+    assert sim.reseed(4, 8, 1) == {"removed": 0, "added": 0, "numParticles": 0}
+    sim.set_volume_correction(0.5)
+    assert sim.runFrame() == 0
+    assert np.all(sim.get_state(["p"])["p"] == 0)
+    sim.close()
+
+
 def test_out_of_range_arguments_are_refused():
     sim = fs2d.FluidSim2D(scenes.sl_dam_break(32), seed=1)
     lib = fs2d.load()
