@@ -312,11 +312,50 @@ def cpu_baseline(args, budget_s, max_frames):
         # reference's hard-coded tolerance 1e-12 (OpenMP build)
         variants["serial_tol_%g" % args.tol] = variant(False, args.tol, 200)
         variants["openmp_tol_1e-12"] = variant(True, 1e-12, 200)
-    return {"value": value, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", threads)), "kind": "port",
-            "sample": f"{frames} frame(s) of the same {args.size}^2 workload after 1 warm-up frame, "
-                      f"{dt:.1f} s; oracle restatement (C, -O3 -fopenmp, the reference's race-free "
-                      f"OpenMP loops), PCG tol {args.tol:g} (last solve {info['iterations']} iterations)",
-            "variants": variants}
+    out = {"value": value, "unit": UNIT, "cores": int(os.environ.get("OMP_NUM_THREADS", threads)), "kind": "port",
+           "sample": f"{frames} frame(s) of the same {args.size}^2 workload after 1 warm-up frame, "
+                     f"{dt:.1f} s; oracle restatement (C, -O3 -fopenmp, the reference's race-free "
+                     f"OpenMP loops), PCG tol {args.tol:g} (last solve {info['iterations']} iterations)",
+           "variants": variants}
+    if getattr(args, "grid3d_size", 0) > 0:
+        out["grid3d"] = cpu_grid3d(128)
+    return out
+
+
+def cpu_grid3d(n):
+    """The 3D containers' methods on the host (the oracle's C restatement of
+    include/Array3D.h and include/MACGrid3D.h, serial like the reference's
+    headers): per-unit rates on an n^3 MAC grid, beside the device's
+    `grid3d` line.  Best of 3 for each."""
+    import numpy as np
+    import oracle3d
+    R = oracle3d.restated
+    rng = np.random.default_rng(7)
+    size = (n, n, n)
+    u, v, w = (rng.standard_normal(k) for k in ((n + 1) * n * n, n * (n + 1) * n, n * n * (n + 1)))
+    a, b = rng.standard_normal(n ** 3), rng.standard_normal(n ** 3)
+    pts = rng.random((n ** 3 // 8, 3)) * n
+
+    def best(fn):
+        t = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            fn()
+            t.append(time.perf_counter() - t0)
+        return min(t)
+
+    cells = n ** 3
+    res = {"grid": [n, n, n], "kind": "port", "cores": 1,
+           "sample": f"oracle restatement (C, -O2, serial) on a {n}^3 MAC grid and {n}^3 arrays of N(0,1) "
+                     f"doubles, {len(pts)} random points; best of 3 per method"}
+    res["velDiv_cells_per_s"] = cells / best(lambda: R.mac_vel_div(u, v, w, size))
+    res["vel_cells_per_s"] = cells / best(lambda: R.mac_vel(u, v, w, size))
+    res["velU_faces_per_s"] = (n + 1) * n * n / best(lambda: R.mac_face_vel(u, v, w, size, "u"))
+    res["setMultiplyAdd_elements_per_s"] = cells / best(lambda: R.set_multiply_add(a, 0.5, b, size))
+    res["innerProduct_elements_per_s"] = cells / best(lambda: R.inner_product(a, b, size))
+    res["infiniteNorm_elements_per_s"] = cells / best(lambda: R.infinite_norm(a, size))
+    res["velInterp_points_per_s"] = len(pts) / best(lambda: R.mac_vel_interp(u, v, w, size, "uvw", pts))
+    return res
 
 
 def reference_arm(args):
