@@ -11,6 +11,7 @@
 // it, which makes its result depend on the loop order; a parallel GPU
 // cannot reproduce that, and the oracle provides both variants.
 #include <cuda_runtime.h>
+#include <cstring>
 #include "fs2d_device.cuh"
 
 namespace fs2d {
@@ -92,6 +93,54 @@ int sl_advect(Sim* s) {
 int apply_gravity(Sim* s) {
     size_t n = s->NU > s->NV ? s->NU : s->NV;
     FS2D_LAUNCH(s, k_gravity, blocks_for(n, 256), 256, 0, s->u, s->NU, s->dt * s->gx, s->v, s->NV, s->dt * s->gy);
+    return 0;
+}
+
+namespace {
+
+// applyAdvection's CFL check (src/FluidSim2D.cpp:571-585): c = (vx + vy) *
+// dt / dx.  For c > 0 the order of the bit patterns is the order of the
+// values, so an integer maximum finds the largest c and an integer minimum
+// the first particle that reaches it, whatever the thread order.
+__device__ __forceinline__ double cfl_of(double2 v, double dt, double dx) { return (v.x + v.y) * dt / dx; }
+
+__global__ void k_cfl_max(const double2* __restrict__ vel, size_t np, double dt, double dx,
+                          unsigned long long* best) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    const double c = cfl_of(vel[e], dt, dx);
+    if (c > 0.0) atomicMax(best, (unsigned long long)__double_as_longlong(c));
+}
+
+__global__ void k_cfl_first(const double2* __restrict__ vel, size_t np, double dt, double dx,
+                            const unsigned long long* __restrict__ best, unsigned long long* first) {
+    const size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (e >= np) return;
+    const double c = cfl_of(vel[e], dt, dx);
+    if (c > 0.0 && (unsigned long long)__double_as_longlong(c) == *best) atomicMin(first, (unsigned long long)e);
+}
+
+}  // namespace
+
+int cfl_check(Sim* s, double* cfl, long long* particle) {
+    // two words of the reduction scratch: the best bit pattern (0: none) and its first particle
+    unsigned long long* w = reinterpret_cast<unsigned long long*>(s->partial);
+    FS2D_CUDA(cudaMemsetAsync(w, 0, sizeof(unsigned long long), s->stream));
+    FS2D_CUDA(cudaMemsetAsync(w + 1, 0xff, sizeof(unsigned long long), s->stream));
+    if (s->np) {
+        FS2D_LAUNCH(s, k_cfl_max, blocks_for(s->np, 256), 256, 0, s->vel, s->np, s->dt, s->dx, w);
+        FS2D_LAUNCH(s, k_cfl_first, blocks_for(s->np, 256), 256, 0, s->vel, s->np, s->dt, s->dx, w, w + 1);
+    }
+    unsigned long long h[2] = {0, 0};
+    FS2D_CUDA(cudaMemcpyAsync(h, w, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    if (h[0] == 0) {
+        *cfl = 0.0;
+        *particle = -1;
+    } else {
+        std::memcpy(cfl, &h[0], sizeof(double));
+        *particle = (long long)h[1];
+    }
     return 0;
 }
 

@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 #include <algorithm>
+#include <atomic>
 #include <new>
 #include <string>
 #include <vector>
@@ -179,10 +180,27 @@ struct Host {
     bool solve_pending = false;   // a batch frame's solve scalars are on their way to pcg_host
 };
 
+// fs2d_debug_fail_alloc: < 0 no injection; otherwise the number of device
+// allocations that still succeed before every further one fails.
+std::atomic<long long> g_alloc_budget{-1};
+
+bool injected_alloc_failure() {
+    long long b = g_alloc_budget.load();
+    while (b >= 0) {
+        if (b == 0) return true;
+        if (g_alloc_budget.compare_exchange_weak(b, b - 1)) return false;
+    }
+    return false;
+}
+
 template <typename T>
 int dalloc(T** p, size_t n) {
     *p = nullptr;
     if (n == 0) n = 1;
+    if (injected_alloc_failure()) {
+        set_error("cudaMalloc of %zu bytes failed: injected by fs2d_debug_fail_alloc", n * sizeof(T));
+        return FS2D_ERR_ALLOC;
+    }
     cudaError_t e = cudaMalloc((void**)p, n * sizeof(T));
     if (e != cudaSuccess) {
         set_error("cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(e));
@@ -1088,6 +1106,180 @@ int fs2d_max_velocity(fs2d_sim* p, double* out) {
     int rc = run_diag(p);
     if (!rc && out) *out = H(p)->sim.stats_host->max_vel;
     return rc;
+}
+
+int fs2d_cfl(fs2d_sim* p, double* cfl, long long* particle) {
+    if (!p) return FS2D_ERR_INVALID;
+    double c = 0;
+    long long e = -1;
+    int rc = cfl_check(&H(p)->sim, &c, &e);
+    if (rc) return rc;
+    if (cfl) *cfl = c;
+    if (particle) *particle = e;
+    return FS2D_OK;
+}
+
+int fs2d_debug_fail_alloc(long long after) {
+    g_alloc_budget.store(after < 0 ? -1 : after);
+    return FS2D_OK;
+}
+
+// ---- checkpoint and resume ----
+
+}  // extern "C"
+
+namespace {
+
+struct CheckpointHeader {
+    char magic[8];            // "FS2DCKP1"
+    uint32_t version;         // 1
+    uint32_t header_bytes;    // sizeof(CheckpointHeader)
+    int32_t NX, NY, mode, pad;
+    uint64_t num_particles;
+    int64_t frames;
+    double dt, dx, rho, gx, gy, alpha, current_time, orig_volume, water_volume, volume_rate;
+};
+constexpr char kCheckpointMagic[8] = {'F', 'S', '2', 'D', 'C', 'K', 'P', '1'};
+
+struct File {
+    FILE* f = nullptr;
+    ~File() {
+        if (f) fclose(f);
+    }
+};
+
+// The arrays of a checkpoint after its header, in order: cell (padded to 8
+// bytes), phi, p, u, v, newU, newV, particles, particleVels.
+struct CheckpointArrays {
+    std::vector<uint8_t> cell;
+    std::vector<double> phi, p, u, v, nu, nv, pos, vel;
+    CheckpointArrays(const Sim* s, size_t np)
+        : cell((s->N + 7) / 8 * 8), phi(s->N), p(s->N), u(s->NU), v(s->NV), nu(s->NU), nv(s->NV), pos(2 * np),
+          vel(2 * np) {}
+    fs2d_state view(size_t np) {
+        fs2d_state st{};
+        st.cell = cell.data();
+        st.phi = phi.data();
+        st.p = p.data();
+        st.u = u.data();
+        st.v = v.data();
+        st.newU = nu.data();
+        st.newV = nv.data();
+        st.particles = np ? pos.data() : nullptr;
+        st.particleVels = np ? vel.data() : nullptr;
+        st.numParticles = np;
+        return st;
+    }
+    template <typename Fn>
+    bool each(Fn fn) {
+        return fn(cell.data(), cell.size()) && fn(phi.data(), phi.size() * 8) && fn(p.data(), p.size() * 8) &&
+               fn(u.data(), u.size() * 8) && fn(v.data(), v.size() * 8) && fn(nu.data(), nu.size() * 8) &&
+               fn(nv.data(), nv.size() * 8) && fn(pos.data(), pos.size() * 8) && fn(vel.data(), vel.size() * 8);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+int fs2d_save_checkpoint(fs2d_sim* p, const char* path) {
+    if (!p || !path) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    const size_t np = s->np;
+    CheckpointArrays a(s, np);
+    fs2d_state st = a.view(np);
+    int rc = fs2d_download_state(p, &st);
+    if (rc) return rc;
+    FrameStats fs;
+    FS2D_CUDA(cudaMemcpyAsync(&fs, s->stats, sizeof(fs), cudaMemcpyDeviceToHost, s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    CheckpointHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, kCheckpointMagic, 8);
+    h.version = 1;
+    h.header_bytes = sizeof(h);
+    h.NX = s->NX;
+    h.NY = s->NY;
+    h.mode = s->mode;
+    h.num_particles = np;
+    h.frames = s->frames;
+    h.dt = s->dt;
+    h.dx = s->dx;
+    h.rho = s->rho;
+    h.gx = s->gx;
+    h.gy = s->gy;
+    h.alpha = s->alpha;
+    h.current_time = s->current_time;
+    h.orig_volume = s->orig_volume;
+    h.water_volume = fs.volume;
+    h.volume_rate = s->volume_rate;
+    File f;
+    f.f = fopen(path, "wb");
+    if (!f.f) {
+        set_error("fs2d_save_checkpoint: cannot open %s for writing", path);
+        return FS2D_ERR_INVALID;
+    }
+    bool ok = fwrite(&h, sizeof(h), 1, f.f) == 1 &&
+              a.each([&](const void* d, size_t n) { return n == 0 || fwrite(d, 1, n, f.f) == n; });
+    ok = (fclose(f.f) == 0) && ok;
+    f.f = nullptr;
+    if (!ok) {
+        set_error("fs2d_save_checkpoint: writing %s failed", path);
+        return FS2D_ERR_INVALID;
+    }
+    return FS2D_OK;
+}
+
+int fs2d_load_checkpoint(fs2d_sim* p, const char* path) {
+    if (!p || !path) return FS2D_ERR_INVALID;
+    Sim* s = &H(p)->sim;
+    File f;
+    f.f = fopen(path, "rb");
+    if (!f.f) {
+        set_error("fs2d_load_checkpoint: cannot open %s", path);
+        return FS2D_ERR_INVALID;
+    }
+    CheckpointHeader h;
+    if (fread(&h, sizeof(h), 1, f.f) != 1 || memcmp(h.magic, kCheckpointMagic, 8) != 0 || h.version != 1 ||
+        h.header_bytes != sizeof(h)) {
+        set_error("fs2d_load_checkpoint: %s is not a version-1 checkpoint", path);
+        return FS2D_ERR_INVALID;
+    }
+    if (h.NX != s->NX || h.NY != s->NY || h.mode != s->mode || h.dx != s->dx || h.rho != s->rho) {
+        set_error("fs2d_load_checkpoint: %s holds a %d x %d grid (mode %d, dx %g, rho %g); the handle's is %d x %d "
+                  "(mode %d, dx %g, rho %g)",
+                  path, h.NX, h.NY, h.mode, h.dx, h.rho, s->NX, s->NY, s->mode, s->dx, s->rho);
+        return FS2D_ERR_INVALID;
+    }
+    if (h.num_particles > ((size_t)1 << 40)) {
+        set_error("fs2d_load_checkpoint: %s: implausible particle count", path);
+        return FS2D_ERR_INVALID;
+    }
+    const size_t np = (size_t)h.num_particles;
+    CheckpointArrays a(s, np);
+    bool ok = a.each([&](void* d, size_t n) { return n == 0 || fread(d, 1, n, f.f) == n; });
+    if (!ok || fgetc(f.f) != EOF) {
+        set_error("fs2d_load_checkpoint: %s is truncated or too long", path);
+        return FS2D_ERR_INVALID;
+    }
+    fs2d_state st = a.view(np);
+    int rc = fs2d_upload_state(p, &st);
+    if (rc) return rc;
+    if (!np) s->np = 0;   // fs2d_upload_state leaves the particles when none are given
+    s->gx = h.gx;
+    s->gy = h.gy;
+    s->alpha = h.alpha;
+    s->dt = h.dt;
+    s->current_time = h.current_time;
+    s->frames = h.frames;
+    s->orig_volume = h.orig_volume;
+    s->volume_rate = h.volume_rate;
+    s->generation++;
+    s->stats_host->volume = h.water_volume;
+    FS2D_CUDA(cudaMemcpyAsync(&s->stats->volume, &s->stats_host->volume, sizeof(double), cudaMemcpyHostToDevice,
+                              s->stream));
+    FS2D_CUDA(cudaStreamSynchronize(s->stream));
+    return FS2D_OK;
 }
 
 int fs2d_get_stage_times(fs2d_sim* p, float* ms, int cap, int* n) {

@@ -432,6 +432,9 @@ int extrapolate_core(Sim* s, cudaStream_t stream, const ExtrapScratch& x, double
                      const int W[2], const int H[2], int band);
 int exclusive_scan_u32(Sim* s, uint32_t* data, size_t n);
 
+// applyAdvection's CFL check (fs2d_cfl): the largest c > 0 and its first particle.
+int cfl_check(Sim* s, double* cfl, long long* particle);
+
 // Particle reseeding (fs2d_reseed): scratch of N + 1 (cells) or np + 1
 // (particles) words each.
 struct ReseedScratch {

@@ -142,6 +142,10 @@ SIGNATURES = {
     "fs2d_extrapolate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p]),
     "fs2d_get_kernel_times": (C.c_int, [C.c_void_p, C.c_char_p, C.c_size_t]),
     "fs2d_reseed": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_uint, C.POINTER(ReseedStats)]),
+    "fs2d_cfl": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_longlong)]),
+    "fs2d_save_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "fs2d_load_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p]),
+    "fs2d_debug_fail_alloc": (C.c_int, [C.c_longlong]),
     "fs2d_set_volume_correction": (C.c_int, [C.c_void_p, C.c_double]),
     "fs3d_add": (C.c_int, [C.POINTER(Array3D), C.POINTER(Array3D), C.c_void_p]),
     "fs3d_set_multiply_add": (C.c_int, [C.POINTER(Array3D), C.POINTER(Array3D), C.c_double, C.POINTER(Array3D),
@@ -388,6 +392,18 @@ class FluidSim2D:
         st = ReseedStats()
         _check(load().fs2d_reseed(self.h, minPerCell, maxPerCell, seed, C.byref(st)))
         return {"removed": st.removed, "added": st.added, "numParticles": st.numParticles}
+
+    def cfl(self):
+        """applyAdvection's CFL check (fs2d_cfl): (largest c, first particle)."""
+        c, e = C.c_double(), C.c_longlong()
+        _check(load().fs2d_cfl(self.h, C.byref(c), C.byref(e)))
+        return c.value, e.value
+
+    def save_checkpoint(self, path):
+        _check(load().fs2d_save_checkpoint(self.h, os.fsencode(path)))
+
+    def load_checkpoint(self, path):
+        _check(load().fs2d_load_checkpoint(self.h, os.fsencode(path)))
 
     def set_volume_correction(self, rate):
         """Volume correction in the projection (fs2d_set_volume_correction)."""

@@ -347,6 +347,28 @@ int fs2d_get_history(fs2d_sim* sim, double* volume, double* energy, double* part
 int fs2d_avg_pressure(fs2d_sim* sim, double* out);
 int fs2d_avg_pressure_in_fluid(fs2d_sim* sim, double* out);
 int fs2d_max_velocity(fs2d_sim* sim, double* out);
+/* The CFL check of applyAdvection (src/FluidSim2D.cpp:571-585), which the
+ * reference only logs when it exceeds 5: over the particles, the largest
+ * c = (vx + vy) * dt / dx above 0 (the reference's expression, without
+ * absolute values; NaN never counts) and the first particle reaching it;
+ * *cfl = 0 and *particle = -1 when no particle has c > 0.  Either pointer
+ * may be NULL. */
+int fs2d_cfl(fs2d_sim* sim, double* cfl, long long* particle);
+
+/* Checkpoint and resume (no reference counterpart: the reference keeps no
+ * state on disk).  fs2d_save_checkpoint writes the handle's whole state to
+ * one binary file: a header (magic "FS2DCKP1", version, grid, mode,
+ * particle count, frame count, time, dt, dx, rho, gravity, picFlipAlpha,
+ * the volume at creation and the current water volume, the volume
+ * correction rate), then cell, phi, p, u, v, newU, newV, particles and
+ * particleVels in the layouts of fs2d_state, in host byte order.
+ * fs2d_load_checkpoint restores it into a handle of the same grid, mode, dx
+ * and rho (FS2D_ERR_INVALID otherwise, or for a file that is not a complete
+ * checkpoint); frames after a resume are the frames the saved handle would
+ * have run, bit for bit on the reproducible paths.  The statistics history
+ * (fs2d_get_history) is not part of the file. */
+int fs2d_save_checkpoint(fs2d_sim* sim, const char* path);
+int fs2d_load_checkpoint(fs2d_sim* sim, const char* path);
 
 /* Per-stage device times (ms, CUDA events) of the last frame, in the
  * reference's stage order (src/FluidSim2D.cpp:100-133); *n = stage count
@@ -441,6 +463,14 @@ int fs2d_set_volume_correction(fs2d_sim* sim, double rate);
 #define FS2D_WAVE_MIC_FP64      4
 #define FS2D_WAVE_MIC_FP32      8
 int fs2d_debug_wavefront(fs2d_sim* sim, long long polls, int holdKinds, int holdStrip);
+
+/* Test hook of the allocation failure path (no reference counterpart; the
+ * reference exits when an allocation fails, include/Array2D.h:69-72): after
+ * `after` more device allocations of a handle's arrays succeed, every
+ * further one fails with FS2D_ERR_ALLOC as if the device were out of
+ * memory, until the hook is turned off with a negative value.  Process-wide;
+ * a create that fails this way frees what it had allocated. */
+int fs2d_debug_fail_alloc(long long after);
 
 /* Use `stream` (a cudaStream_t) for all subsequent work of this handle;
  * NULL restores the handle's own stream. */

@@ -66,6 +66,9 @@ def test_null_handles_are_refused():
     assert lib.fs2d_render_export(None, None) == INVALID
     assert lib.fs2d_reseed(None, 4, 8, 0, None) == INVALID
     assert lib.fs2d_set_volume_correction(None, 0.1) == INVALID
+    assert lib.fs2d_cfl(None, None, None) == INVALID
+    assert lib.fs2d_save_checkpoint(None, b"x") == INVALID
+    assert lib.fs2d_load_checkpoint(None, b"x") == INVALID
     assert lib.fs2d_destroy(None) == 0
     assert lib.fs2d_batch_destroy(None) == 0
 
