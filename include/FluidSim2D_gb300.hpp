@@ -446,6 +446,30 @@ struct FluidSim2D {
     // perf.csv and conservation.csv in the reference's formats (src/FluidSim2D.cpp:738-750).
     void saveStats() { check(fs2d_save_stats(device, "perf.csv", "conservation.csv"), "saveStats"); }
 
+    // Beyond the reference's API (include/fs2d.h): particle reseeding and
+    // volume correction (the README's TODOs), the CFL check applyAdvection
+    // only logs, and checkpoint / resume of the whole state.  They act on
+    // the device state: reseed and loadCheckpoint refresh the mirrors as a
+    // frame does under the sync policy.  gravity, picFlipAlpha and dt stay
+    // the mirror's, pushed at the next frame as always, also after a load.
+    fs2d_reseed_stats reseed(int minPerCell, int maxPerCell, unsigned int seed = 0) {
+        fs2d_reseed_stats out{};
+        check(fs2d_reseed(device, minPerCell, maxPerCell, seed, &out), "reseed");
+        afterDeviceWork();
+        return out;
+    }
+    void setVolumeCorrection(double rate) { check(fs2d_set_volume_correction(device, rate), "setVolumeCorrection"); }
+    double cfl(long long* particle = nullptr) {
+        double c = 0;
+        check(fs2d_cfl(device, &c, particle), "cfl");
+        return c;
+    }
+    void saveCheckpoint(const char* path) { check(fs2d_save_checkpoint(device, path), "saveCheckpoint"); }
+    void loadCheckpoint(const char* path) {
+        check(fs2d_load_checkpoint(device, path), "loadCheckpoint");
+        afterDeviceWork();
+    }
+
     vec2d clampPos(vec2d to) {
         constexpr double offset = 1e-3;
         const double lx = (1.0 + offset) * dx, hx = (sizeX - 1.0 - offset) * dx;

@@ -72,3 +72,34 @@ def test_c_abi_rollout_and_batch_run(tmp_path):
     exe = build_c(tmp_path)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout + r.stderr
+
+
+EXT_SNIPPET = r"""
+#include "FluidSim2D_gb300.hpp"
+// the extensions beyond the reference's API, as a caller writes them
+void use(FluidSim2D& sim) {
+    sim.setVolumeCorrection(0.05);
+    fs2d_reseed_stats r = sim.reseed(4, 8, 1u);
+    long long e = -1;
+    double c = sim.cfl(&e);
+    sim.saveCheckpoint("state.fs2d");
+    sim.loadCheckpoint("state.fs2d");
+    (void)r;
+    (void)c;
+}
+"""
+
+
+def test_cpp_api_extensions_compile(tmp_path):
+    """Reseeding, volume correction, the CFL check and checkpoints through
+    the C++ mirror compile without warnings (they run in the GPU tests of
+    the C ABI they wrap)."""
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("g++ not available")
+    src = tmp_path / "ext.cpp"
+    src.write_text(EXT_SNIPPET)
+    r = subprocess.run([gxx, "-std=c++17", "-Wall", "-Wextra", "-c", "-I", os.path.join(ROOT, "include"), str(src),
+                        "-o", str(tmp_path / "ext.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "warning" not in r.stderr, r.stderr
