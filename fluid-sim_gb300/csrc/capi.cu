@@ -1178,11 +1178,16 @@ struct CheckpointArrays {
     }
 };
 
+// Bytes after the header: exactly what CheckpointArrays::each reads or writes.
+size_t checkpoint_payload_bytes(const Sim* s, size_t np) {
+    return (s->N + 7) / 8 * 8 + sizeof(double) * (2 * s->N + 2 * s->NU + 2 * s->NV + 4 * np);
+}
+
 }  // namespace
 
 extern "C" {
 
-int fs2d_save_checkpoint(fs2d_sim* p, const char* path) {
+int fs2d_save_checkpoint(fs2d_sim* p, const char* path) try {
     if (!p || !path) return FS2D_ERR_INVALID;
     Sim* s = &H(p)->sim;
     const size_t np = s->np;
@@ -1228,9 +1233,12 @@ int fs2d_save_checkpoint(fs2d_sim* p, const char* path) {
         return FS2D_ERR_INVALID;
     }
     return FS2D_OK;
+} catch (const std::bad_alloc&) {
+    set_error("fs2d_save_checkpoint: out of host memory");
+    return FS2D_ERR_ALLOC;
 }
 
-int fs2d_load_checkpoint(fs2d_sim* p, const char* path) {
+int fs2d_load_checkpoint(fs2d_sim* p, const char* path) try {
     if (!p || !path) return FS2D_ERR_INVALID;
     Sim* s = &H(p)->sim;
     File f;
@@ -1256,6 +1264,15 @@ int fs2d_load_checkpoint(fs2d_sim* p, const char* path) {
         return FS2D_ERR_INVALID;
     }
     const size_t np = (size_t)h.num_particles;
+    // the file holds exactly the header and the arrays it announces: checked
+    // before any buffer is sized from the header
+    long long file_bytes = -1;
+    if (fseek(f.f, 0, SEEK_END) == 0) file_bytes = (long long)ftell(f.f);
+    if (file_bytes != (long long)(sizeof(h) + checkpoint_payload_bytes(s, np)) ||
+        fseek(f.f, (long)sizeof(h), SEEK_SET) != 0) {
+        set_error("fs2d_load_checkpoint: %s is truncated or too long for %zu particles", path, np);
+        return FS2D_ERR_INVALID;
+    }
     CheckpointArrays a(s, np);
     bool ok = a.each([&](void* d, size_t n) { return n == 0 || fread(d, 1, n, f.f) == n; });
     if (!ok || fgetc(f.f) != EOF) {
@@ -1280,6 +1297,9 @@ int fs2d_load_checkpoint(fs2d_sim* p, const char* path) {
                               s->stream));
     FS2D_CUDA(cudaStreamSynchronize(s->stream));
     return FS2D_OK;
+} catch (const std::bad_alloc&) {
+    set_error("fs2d_load_checkpoint: out of host memory");
+    return FS2D_ERR_ALLOC;
 }
 
 int fs2d_get_stage_times(fs2d_sim* p, float* ms, int cap, int* n) {

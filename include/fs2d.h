@@ -431,7 +431,9 @@ int fs2d_render_export(fs2d_sim* sim, fs2d_render* r);
  * velocity there (the PIC part of updateParticleVelocities).  Survivors
  * keep their order; new particles follow in row-major cell order.  0 <=
  * minPerCell <= 64, maxPerCell == 0 (no removal) or minPerCell <=
- * maxPerCell.  `out` (may be NULL) receives the counts. */
+ * maxPerCell.  `out` (may be NULL) receives the counts.  A cell over
+ * maxPerCell is ordered by one thread, in time that grows with the square
+ * of its particle count (a few to a few dozen in a simulation). */
 typedef struct fs2d_reseed_stats {
     size_t removed;
     size_t added;
