@@ -1,5 +1,7 @@
 // capi.cu — the C ABI (include/fs2d.h): handle lifetime, frame and stage
-// drivers, host <-> device state transfer, statistics and CSV output.
+// drivers, host <-> device state transfer, statistics and CSV output,
+// checkpoint / resume, and the host side of reseeding, volume correction,
+// the CFL check and the allocation-failure test hook.
 //
 // Mirrors FluidSim2D (include/FluidSim2D.h:65-176, src/FluidSim2D.cpp):
 // create seeds particles on the host with libc rand() in the reference's
