@@ -5,6 +5,8 @@ against libfs2d.so; every host method, run on exact rational inputs, equals
 the oracle restatement (oracle/restate/fs3d_oracle.c) bit for bit.
 GPU: the fs3d_device:: wrappers (the C ABI of include/fs3d.h) on the same
 inputs equal the host methods (tests/cpp/grid3d_api_test.cpp).
+CPU: a plain C11 program over include/fs3d.h (tests/cpp/fs3d_args_test.c)
+links and sees bad arguments refused before any device work.
 """
 import os
 import shutil
@@ -99,4 +101,23 @@ def test_device_wrappers_match_host_methods(tmp_path):
         pytest.skip("CUDA runtime headers not found")
     exe = build(tmp_path, gpu=True)
     r = subprocess.run([exe, "gpu"], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout + r.stderr
+
+
+C_SRC = os.path.join(ROOT, "tests", "cpp", "fs3d_args_test.c")
+
+
+def test_c_program_checks_arguments_without_a_device(tmp_path):
+    """include/fs3d.h compiles as C11 (no warnings), links, and refuses bad
+    arguments before any device work: the program runs here without a GPU."""
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    if not os.path.exists(os.path.join(LIBDIR, "libfs2d.so")):
+        pytest.skip("libfs2d.so not built")
+    exe = str(tmp_path / "fs3d_args_test")
+    r = subprocess.run([gcc, "-std=c11", "-O2", "-Wall", "-Wextra", "-I", os.path.join(ROOT, "include"), C_SRC, "-o",
+                        exe, "-L", LIBDIR, "-lfs2d", "-Wl,-rpath," + LIBDIR], capture_output=True, text=True)
+    assert r.returncode == 0 and "warning" not in r.stderr, r.stdout + r.stderr
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.startswith("OK"), r.stdout + r.stderr
