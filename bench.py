@@ -208,19 +208,17 @@ def workload(size):
     return scenes.pic_dam_break_disk(size)
 
 
-def config_dict(args, n_particles, extra=None):
-    d = {
+def config_dict(args, n_particles):
+    """The workload, identical for both arms; how each arm computes it (the
+    precision, threads, iteration counts) lives in top-level keys."""
+    return {
         "workload": f"PIC/FLIP dam break + disk r=0.1, {args.size}x{args.size}, dt=1/{int(round(960 * args.size / 1024))}, "
                     f"4 ppc, FLIP 0.95, MIC(0)-PCG tol {args.tol:g} rel (inf-norm), <=200 iters",
         "grid": [args.size, args.size],
         "particles": n_particles,
-        "precision": args.precision,
         "l2": "flushed between timed steps (256 MiB write)",
         "parallelism": f"replicas x{args.gpus}",
     }
-    if extra:
-        d.update(extra)
-    return d
 
 
 # ---------------------------------------------------------------- clocks
@@ -386,8 +384,8 @@ def reference_arm(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": frames, "warmup": warm, "ms_per_step": 1000 * dt / frames, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded dam break + disk)",
-        "config": config_dict(args, n_particles, {"precision": "fp64 (reference CPU path)",
-                                                  "cpu_threads": int(os.environ["OMP_NUM_THREADS"])}),
+        "config": config_dict(args, n_particles),
+        "precision": "fp64 (reference CPU path)", "cpu_threads": int(os.environ["OMP_NUM_THREADS"]),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": int(os.environ["OMP_NUM_THREADS"]), "kind": "port",
                          "sample": f"{frames} of {args.steps} requested frames after {warm} warm-up frame(s), "
                                    f"capped at {budget:.0f} s; oracle restatement of the reference step "
@@ -898,7 +896,8 @@ def main():
         "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32+f64",
         "data": "synthetic (seeded dam break + disk, libc rand() particle jitter)",
-        "config": config_dict(args, n_particles, {"pcg_iterations_per_step": iters}),
+        "config": config_dict(args, n_particles),
+        "precision": args.precision, "pcg_iterations_per_step": iters,
         "stage_ms_last_step": stage_ms,
         "fp64_path": fp64_path,
         "error_vs_oracle": oracle_err,
